@@ -99,6 +99,9 @@ int gbf_last_status(void);            /* sticky status of the last failing call 
 void gbf_clear_status(void);
 const char* gbf_status_string(int status);
 const char* gbf_version(void);
+/* sizeof of the ABI structs (0: gbf_model, 1: gbf_cells, 2: gbf_arrays), so
+   bindings can check their layout. */
+size_t gbf_abi_sizeof(int which);
 /* Fill *m with the reference's constants (defines.h:6-26) and the defaults of
    its defines.ini; grid sizes nx, ny, nz and dt are taken from the arguments. */
 void gbf_model_reference(gbf_model* m, int nx, int ny, int nz, double dt);
@@ -108,6 +111,16 @@ double gbf_stable_dt(const gbf_model* m, const gbf_cells* cells, double safety);
 /* Host-side validation of a model (sizes, positivity, S_e range of the Dirichlet
    patch, dt against the stability bound when check_dt != 0). */
 int gbf_model_validate(const gbf_model* m, const gbf_cells* cells, int check_dt);
+
+/* ------------------------------------------------ seeded synthetic fields
+ * Host functions (no GPU). Deterministic for a seed, whatever the thread
+ * count. K: log-normal, geometric mean K_geo, log-standard deviation
+ * sigma_lnK, built from white noise smoothed by a Gaussian of corr_cells
+ * cells and renormalised to unit variance. phi: base + amp * U(-1, 1).
+ */
+int gbf_fill_lognormal_K(int nx, int ny, int nz, uint64_t seed, double K_geo, double sigma_lnK, double corr_cells,
+                         float* K_out);
+int gbf_fill_porosity(int nx, int ny, int nz, uint64_t seed, double base, double amp, float* phi_out);
 
 /* --------------------------- per-function device entry points (FP64) ----
  * Device pointers (`d_arrays`, `d_cells`), one CUDA stream (NULL = legacy
@@ -121,6 +134,47 @@ int gbf_newton_f64(const gbf_model* m, gbf_arrays d_arrays, gbf_cells d_cells, v
 /* a5; `d_scratch` must hold gbf_boundary_scratch_doubles(m) doubles (device). */
 int gbf_boundary_f64(const gbf_model* m, gbf_arrays d_arrays, double* d_scratch, void* stream);
 size_t gbf_boundary_scratch_doubles(const gbf_model* m);
+
+/* ------------------------------------------------------- single domain ----
+ * One grid whose state lives in HBM between steps. `precision` is
+ * GBF_PREC_F64 (plain FP64: two passes per step — properties, then fluxes,
+ * mass update and Newton fused — plus a face pass for the boundaries) or
+ * GBF_PREC_SPLIT (FP32 P, S, K, phi and fluxes; FP64 per-cell phase masses
+ * and one FP64 residual per cell). All calls are ordered on the domain's
+ * stream; gbf_domain_step only enqueues work.
+ */
+typedef struct gbf_domain gbf_domain;
+/* Per-step outputs that are off by default (the hot path writes P, S only). */
+enum { GBF_OUT_MASS = 1,        /* phase masses after the mass update, every step */
+       GBF_OUT_VELOCITY = 2,    /* u1x..u2z of the reference's a2 (FP64 only)      */
+       GBF_OUT_MASS_ARRAYS = 4, /* roS1, roS2, roS1_old, roS2_old (FP64 only)       */
+       GBF_OUT_PROPS = 8 };     /* keep P2/Xi/ro of the last step readable        */
+int gbf_domain_create(const gbf_model* m, const gbf_cells* host_cells, int precision, gbf_domain** out);
+int gbf_domain_destroy(gbf_domain* d);
+int gbf_domain_set_outputs(gbf_domain* d, int out_flags, int mass_history_capacity);
+int gbf_domain_set_stream(gbf_domain* d, void* stream);
+/* Initial state from host arrays (nx*ny*nz doubles each). */
+int gbf_domain_upload(gbf_domain* d, const double* P1_host, const double* S2_host);
+/* Same from device arrays (e.g. torch tensors). */
+int gbf_domain_upload_device(gbf_domain* d, const double* P1_dev, const double* S2_dev);
+int gbf_domain_step(gbf_domain* d, int nsteps);
+/* Copy one field (GBF_FIELD_*) of the current state to the host; synchronises. */
+int gbf_domain_download(gbf_domain* d, int field, double* host);
+/* Phase masses [step][2] recorded since the last upload (GBF_OUT_MASS). */
+int gbf_domain_mass_history(gbf_domain* d, double* host, int max_steps, int* nsteps_out);
+/* Synchronise and return the device-side status (non-finite P/S, timeouts). */
+int gbf_domain_status(gbf_domain* d);
+int gbf_domain_sync(gbf_domain* d);
+long long gbf_domain_steps_done(gbf_domain* d);
+/* Kernels launched per step (for launch accounting). */
+int gbf_domain_launches_per_step(gbf_domain* d);
+/* Per-kernel CUDA-event timing on the domain's stream (off by default):
+   gbf_domain_kernel_times synchronises, returns milliseconds and launch
+   counts per kernel kind (gbf_kernel_name) since the last call, and resets. */
+int gbf_domain_set_timing(gbf_domain* d, int on);
+int gbf_domain_kernel_times(gbf_domain* d, double* ms, int* launches, int nkinds);
+int gbf_kernel_kinds(void);
+const char* gbf_kernel_name(int kind);
 
 #ifdef __cplusplus
 }

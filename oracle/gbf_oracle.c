@@ -19,6 +19,11 @@
  *   orc_step        main.cpp:83-94         (time_step_function, single domain)
  *   orc_initial     main.cpp:97-138        (initial_data, single domain)
  *
+ * The loops of orc_props/velocity/mass/newton run in parallel over i with
+ * OpenMP (each iteration writes only its own cells and reads arrays the loop
+ * does not write, so the result does not depend on the thread count); the
+ * boundary sweep and the mass sums stay serial.
+ *
  * Extensions (all off in reference mode, see gbf_model): per-cell K and
  * porosity, vertical anisotropy kv, mass-rate injection, hydrostatic side
  * boundaries with a no-flow bottom, and a Newton tolerance stop.
@@ -62,6 +67,7 @@ int orc_in_rate_patch(const gbf_model* m, int i, int k) {
    densities; every cell (cpu.cpp:57-74). */
 void orc_props(const gbf_model* m, const gbf_cells* cells, gbf_arrays a) {
   const int nx = m->nx, ny = m->ny, nz = m->nz;
+#pragma omp parallel for schedule(static)
   for (int i = 0; i < nx; i++)
     for (int j = 0; j < ny; j++)
       for (int k = 0; k < nz; k++) {
@@ -85,6 +91,7 @@ void orc_props(const gbf_model* m, const gbf_cells* cells, gbf_arrays a) {
 void orc_velocity(const gbf_model* m, gbf_arrays a) {
   const int nx = m->nx, ny = m->ny, nz = m->nz;
   const double kv = m->kv;
+#pragma omp parallel for schedule(static)
   for (int i = 0; i < nx; i++)
     for (int j = 0; j < ny; j++)
       for (int k = 0; k < nz; k++) {
@@ -158,6 +165,7 @@ void orc_mass(const gbf_model* m, const gbf_cells* cells, gbf_arrays a) {
   const double src = (m->source_mode == GBF_SOURCE_RATE && m->rate_cells > 0)
                          ? m->rate / (double)(m->rate_cells * m->rate_cells) / (m->h1 * m->h2 * m->h3)
                          : 0.0;
+#pragma omp parallel for schedule(static)
   for (int i = 0; i < nx; i++)
     for (int j = 0; j < ny; j++)
       for (int k = 0; k < nz; k++) {
@@ -210,6 +218,7 @@ void orc_mass(const gbf_model* m, const gbf_cells* cells, gbf_arrays a) {
 /* a4: per-cell 2x2 Newton for (P1, S2) from the phase masses (cpu.cpp:293-320). */
 void orc_newton(const gbf_model* m, const gbf_cells* cells, gbf_arrays a) {
   const int nx = m->nx, ny = m->ny, nz = m->nz;
+#pragma omp parallel for schedule(static)
   for (int i = 0; i < nx; i++)
     for (int j = 0; j < ny; j++)
       for (int k = 0; k < nz; k++) {

@@ -17,6 +17,7 @@ GBF_OK, GBF_ERR_ARG, GBF_ERR_CUDA, GBF_ERR_NOMEM, GBF_ERR_NONFINITE, GBF_ERR_UNS
 GBF_SOURCE_DIRICHLET_PATCH, GBF_SOURCE_RATE = 0, 1
 GBF_BC_REFERENCE, GBF_BC_HYDROSTATIC_SIDES = 0, 1
 GBF_PREC_F64, GBF_PREC_SPLIT = 0, 1
+GBF_OUT_MASS, GBF_OUT_VELOCITY, GBF_OUT_MASS_ARRAYS, GBF_OUT_PROPS = 1, 2, 4, 8
 
 FIELDS = ["P1", "S2", "P2", "ro1", "ro2", "Xi1", "Xi2", "u1x", "u1y", "u1z",
           "u2x", "u2y", "u2z", "roS1", "roS2", "roS1_old", "roS2_old"]
@@ -124,6 +125,29 @@ def _declare(lib) -> None:
         "gbf_newton_f64": (c_int, [PM, GbfArrays, GbfCells, c_void_p]),
         "gbf_boundary_f64": (c_int, [PM, GbfArrays, c_void_p, c_void_p]),
         "gbf_boundary_scratch_doubles": (c_size_t, [PM]),
+        "gbf_abi_sizeof": (c_size_t, [c_int]),
+        "gbf_domain_create": (c_int, [PM, PC, c_int, ctypes.POINTER(c_void_p)]),
+        "gbf_domain_destroy": (c_int, [c_void_p]),
+        "gbf_domain_set_outputs": (c_int, [c_void_p, c_int, c_int]),
+        "gbf_domain_set_stream": (c_int, [c_void_p, c_void_p]),
+        "gbf_domain_upload": (c_int, [c_void_p, c_void_p, c_void_p]),
+        "gbf_domain_upload_device": (c_int, [c_void_p, c_void_p, c_void_p]),
+        "gbf_domain_step": (c_int, [c_void_p, c_int]),
+        "gbf_domain_download": (c_int, [c_void_p, c_int, c_void_p]),
+        "gbf_domain_mass_history": (c_int, [c_void_p, c_void_p, c_int, ctypes.POINTER(c_int)]),
+        "gbf_domain_status": (c_int, [c_void_p]),
+        "gbf_domain_sync": (c_int, [c_void_p]),
+        "gbf_domain_steps_done": (ctypes.c_longlong, [c_void_p]),
+        "gbf_domain_launches_per_step": (c_int, [c_void_p]),
+        "gbf_dropin_set_mode": (c_int, [c_int]),
+        "gbf_dropin_get_mode": (c_int, []),
+        "gbf_fill_lognormal_K": (c_int, [c_int, c_int, c_int, ctypes.c_uint64, c_double, c_double, c_double,
+                                         c_void_p]),
+        "gbf_fill_porosity": (c_int, [c_int, c_int, c_int, ctypes.c_uint64, c_double, c_double, c_void_p]),
+        "gbf_domain_set_timing": (c_int, [c_void_p, c_int]),
+        "gbf_domain_kernel_times": (c_int, [c_void_p, c_void_p, c_void_p, c_int]),
+        "gbf_kernel_kinds": (c_int, []),
+        "gbf_kernel_name": (ctypes.c_char_p, [c_int]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
