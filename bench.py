@@ -124,17 +124,30 @@ def barrier(world):
 
 # ------------------------------------------------------------------ workloads
 
+PRECISIONS = {"f64": ("GBF_PREC_F64", "plain FP64"),
+              "split": ("GBF_PREC_SPLIT", "FP32 state and fluxes, FP64 masses and residual"),
+              "splitdf": ("GBF_PREC_SPLIT_DF", "FP32 state and fluxes, FP32-pair masses and residual")}
+
+
 def make_workload(pkg, lib, name, cube):
     from importlib import import_module
     wl = import_module(pkg.__name__ + ".workloads")
-    if name == "config1_f64":
+    cfg, _, p = name.partition("_")
+    if p not in PRECISIONS:
+        raise SystemExit(f"unknown workload {name}")
+    prec = getattr(pkg.abi, PRECISIONS[p][0])
+    if cfg == "config1":
         mem = wl.config1(lib, n=cube or 256)
-        return {"members": [mem], "precision": pkg.abi.GBF_PREC_F64,
-                "desc": f"config 1: {mem.model.nx}^3 heterogeneous single grid, plain FP64"}
-    if name == "config0_f64":
+        desc = f"config 1: {mem.model.nx}^3 heterogeneous single grid"
+    elif cfg == "config0":
         mem = wl.config0(lib)
-        return {"members": [mem], "precision": pkg.abi.GBF_PREC_F64, "desc": "config 0: 40^3 homogeneous, FP64"}
-    raise SystemExit(f"unknown workload {name}")
+        desc = "config 0: 40^3 homogeneous"
+    elif cfg == "config2":
+        mem = wl.config2(lib)
+        desc = "config 2: 512x512x256 heterogeneous single grid (sigma_lnK 1.5)"
+    else:
+        raise SystemExit(f"unknown workload {name}")
+    return {"members": [mem], "precision": prec, "desc": f"{desc}, {PRECISIONS[p][1]}"}
 
 
 # Algorithmic bytes per cell of each kernel (compulsory DRAM traffic of its
@@ -142,8 +155,9 @@ def make_workload(pkg, lib, name, cube):
 ALGO_BYTES = {
     "f64_props": 60.0,        # read P, S (16), K (4) = 20; write L1, L2, ro1, ro2, lnSe (40)
     "f64_flux_newton": 76.0,  # read P, S, L1, L2, ro1, ro2, lnSe (56), phi (4); write P, S (16)
+    "split_step": 56.0,       # read dP, S, K, phi (16), M1, M2 (16); write dP, S (8), M1, M2 (16)
 }
-KERNEL_CELLS = {"f64_props": "all", "f64_flux_newton": "interior"}
+KERNEL_CELLS = {"f64_props": "all", "f64_flux_newton": "interior", "split_step": "interior"}
 
 
 def cells_of(m, which):
@@ -264,7 +278,9 @@ def run_ours(args, rank, world):
     mass = dom.mass_history(args.warmup + args.steps)
     out = {"metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": "f64" if wl["precision"] == abi.GBF_PREC_F64 else "f32+f64",
+           "vs_baseline": None,
+           "dtype": {abi.GBF_PREC_F64: "f64", abi.GBF_PREC_SPLIT: "f32+f64",
+                     abi.GBF_PREC_SPLIT_DF: "f32+f32x2"}[wl["precision"]],
            "data": "synthetic (seeded fields with the configuration's shapes and statistics)",
            "config": {"workload": args.workload, "desc": wl["desc"], "cells": cells,
                       "grid": [m.nx, m.ny, m.nz], "dt_used": m.dt,

@@ -42,7 +42,9 @@ enum { GBF_BC_REFERENCE = 0,           /* reference Border_S2/Border_P1 rules   
        GBF_BC_HYDROSTATIC_SIDES = 1 }; /* Dirichlet hydrostatic P on i/k sides,
                                           no-flow bottom face for both phases          */
 enum { GBF_PREC_F64 = 0,               /* plain FP64 state and arithmetic               */
-       GBF_PREC_SPLIT = 1 };           /* FP32 P,S,K,fluxes; FP64 phase masses and residual */
+       GBF_PREC_SPLIT = 1,             /* FP32 P,S,K,fluxes; FP64 phase masses and residual */
+       GBF_PREC_SPLIT_DF = 2 };        /* as SPLIT, masses and residual as FP32 pairs
+                                          (about 48 significant bits, FP32 pipes only)  */
 
 /* Fields that can be read back (gbf_domain_download / ensemble download). */
 enum {

@@ -140,7 +140,8 @@ int gbf_domain_create(const gbf_model* m, const gbf_cells* host_cells, int preci
   if (!out) return gbf_fail(GBF_ERR_ARG, "gbf_domain_create: out");
   *out = nullptr;
   if (int s = gbf_model_validate(m, host_cells, 0)) return s;
-  if (precision != GBF_PREC_F64 && precision != GBF_PREC_SPLIT) return gbf_fail(GBF_ERR_ARG, "precision");
+  if (precision != GBF_PREC_F64 && precision != GBF_PREC_SPLIT && precision != GBF_PREC_SPLIT_DF)
+    return gbf_fail(GBF_ERR_ARG, "precision");
   gbf_domain* d = new gbf_domain();
   d->m = *m;
   d->d = gbf_derive(*m);
@@ -158,7 +159,7 @@ int gbf_domain_create(const gbf_model* m, const gbf_cells* host_cells, int preci
     }
     if (!s) s = alloc_f64_work(d);
   }
-  if (!s && precision == GBF_PREC_SPLIT) s = gbf_split_alloc(d);
+  if (!s && precision != GBF_PREC_F64) s = gbf_split_alloc(d);
   if (s) {
     free_all(d);
     delete d;
@@ -187,7 +188,7 @@ int gbf_domain_set_stream(gbf_domain* d, void* stream) {
 
 int gbf_domain_set_outputs(gbf_domain* d, int flags, int mass_cap) {
   if (!d || mass_cap < 0) return gbf_fail(GBF_ERR_ARG, "gbf_domain_set_outputs");
-  if (d->precision == GBF_PREC_SPLIT && (flags & (GBF_OUT_VELOCITY | GBF_OUT_MASS_ARRAYS)))
+  if (d->precision != GBF_PREC_F64 && (flags & (GBF_OUT_VELOCITY | GBF_OUT_MASS_ARRAYS)))
     return gbf_fail(GBF_ERR_ARG, "velocity/mass arrays are FP64-only outputs");
   const size_t n = gbf_geo(d->m).n, b = n * sizeof(double);
   if ((flags & GBF_OUT_MASS) && mass_cap > d->mass_cap) {
@@ -217,7 +218,7 @@ int gbf_domain_set_outputs(gbf_domain* d, int flags, int mass_cap) {
 int gbf_domain_upload_device(gbf_domain* d, const double* P1, const double* S2) {
   if (!d || !P1 || !S2) return gbf_fail(GBF_ERR_ARG, "gbf_domain_upload_device");
   const size_t b = gbf_geo(d->m).n * sizeof(double);
-  if (d->precision == GBF_PREC_SPLIT) {
+  if (d->precision != GBF_PREC_F64) {
     if (int s = gbf_split_upload(d, P1, S2, cudaMemcpyDeviceToDevice)) return s;
   } else {
     d->cur = 0;
@@ -234,7 +235,7 @@ int gbf_domain_upload_device(gbf_domain* d, const double* P1, const double* S2) 
 int gbf_domain_upload(gbf_domain* d, const double* P1, const double* S2) {
   if (!d || !P1 || !S2) return gbf_fail(GBF_ERR_ARG, "gbf_domain_upload");
   const size_t b = gbf_geo(d->m).n * sizeof(double);
-  if (d->precision == GBF_PREC_SPLIT) {
+  if (d->precision != GBF_PREC_F64) {
     if (int s = gbf_split_upload(d, P1, S2, cudaMemcpyHostToDevice)) return s;
   } else {
     d->cur = 0;
@@ -255,7 +256,7 @@ int gbf_domain_step(gbf_domain* d, int nsteps) {
   if (d->outs.Xi1) pf |= GBF_PF_WRITE_XI_P2;
   if (d->outs.u1x && (d->out_flags & GBF_OUT_VELOCITY)) pf |= GBF_PF_WRITE_U;
   for (int s = 0; s < nsteps; s++) {
-    int st = (d->precision == GBF_PREC_SPLIT) ? gbf_split_step(d) : f64_step(d, pf);
+    int st = (d->precision != GBF_PREC_F64) ? gbf_split_step(d) : f64_step(d, pf);
     if (st) return st;
   }
   return GBF_OK;
@@ -263,7 +264,7 @@ int gbf_domain_step(gbf_domain* d, int nsteps) {
 
 int gbf_domain_launches_per_step(gbf_domain* d) {
   if (!d) return 0;
-  if (d->precision == GBF_PREC_SPLIT) return gbf_split_launches_per_step(d);
+  if (d->precision != GBF_PREC_F64) return gbf_split_launches_per_step(d);
   return 3 + ((d->out_flags & GBF_OUT_MASS) ? 1 : 0);
 }
 
@@ -299,7 +300,7 @@ int gbf_domain_kernel_times(gbf_domain* d, double* ms, int* launches, int nkinds
 int gbf_domain_download(gbf_domain* d, int field, double* host) {
   if (!d || !host || field < 0 || field >= GBF_FIELD_COUNT) return gbf_fail(GBF_ERR_ARG, "gbf_domain_download");
   const size_t n = gbf_geo(d->m).n, b = n * sizeof(double);
-  if (d->precision == GBF_PREC_SPLIT) return gbf_split_download(d, field, host);
+  if (d->precision != GBF_PREC_F64) return gbf_split_download(d, field, host);
   const double* src = nullptr;
   switch (field) {
     case GBF_FIELD_P1: src = d->P[d->cur]; break;

@@ -64,6 +64,7 @@ struct gbf_domain {
   // split-precision state (gbf_split.cu)
   float *Pf[2] = {nullptr, nullptr}, *Sf[2] = {nullptr, nullptr};
   double *M1 = nullptr, *M2 = nullptr;
+  double* split_partials = nullptr;
   // mass tracking
   double* mass_partials = nullptr;
   double* mass_hist = nullptr;

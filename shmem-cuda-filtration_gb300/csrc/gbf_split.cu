@@ -1,14 +1,318 @@
-// gbf_split.cu — split-precision step (FP32 P, S, K, fluxes; FP64 masses).
-#include "gbf_split.h"
+// gbf_split.cu — split-precision step: FP32 pressure, saturation, K, phi and
+// fluxes; FP64 (or FP32-pair) per-cell phase masses and one wide-precision
+// residual per cell.
+//
+// State (per cell):
+//   dP  = P - P_hs(j), FP32, with P_hs(j) = P_atm + j rho01 g h2 the
+//         hydrostatic profile of the initial state (main.cpp:114). Vertical
+//         potentials then read -(dP(j+1) - dP(j))/h2 + (rho_c - rho01) g: the
+//         two large hydrostatic terms cancel exactly before anything is rounded.
+//   S   = S2, FP32.
+//   M1, M2 (interior cells): the phase masses per pore volume the
+//         reference's mass update starts from, ro1 (1 - S2) and ro2 S2 with
+//         ro2 at P2 = P1 (cpu.cpp:224-225), in FP64 (GBF_PREC_SPLIT) or as an
+//         unevaluated sum of two FP32 (GBF_PREC_SPLIT_DF).
+// The tile routine (gbf_split_tile.cuh) does the fused update of one column
+// tile; this file holds the single-domain kernels and the host side.
+#include <math.h>
 
-int gbf_split_alloc(gbf_domain* d) { (void)d; return gbf_fail(GBF_ERR_ARG, "split precision not built yet"); }
+#include "gbf_split_tile.cuh"
+
+GbfSplitConsts gbf_split_consts(const gbf_model& m) {
+  GbfSplitConsts C = {};
+  C.nx = m.nx; C.ny = m.ny; C.nz = m.nz;
+  C.noflow_bottom = (m.bc_mode == GBF_BC_HYDROSTATIC_SIDES);
+  const double V = m.h1 * m.h2 * m.h3;
+  double src = 0.0;
+  if (m.source_mode == GBF_SOURCE_RATE && m.rate_cells > 0) {
+    C.rn = m.rate_cells;
+    C.ri0 = m.nx / 2 - m.rate_cells / 2;
+    C.rk0 = m.nz / 2 - m.rate_cells / 2;
+    src = m.rate / (double)(m.rate_cells * m.rate_cells) / V;
+  }
+  C.inv_h1 = (float)(1.0 / m.h1); C.inv_h2 = (float)(1.0 / m.h2); C.inv_h3 = (float)(1.0 / m.h3);
+  C.kv = (float)m.kv;
+  C.dt = (float)m.dt;
+  const double H = m.ro01 * m.g * m.h2;
+  C.H = (float)H;
+  C.ro01 = (float)m.ro01; C.ro02 = (float)m.ro02; C.beta1 = (float)m.beta1; C.beta2 = (float)m.beta2;
+  C.g_ro01_b1 = (float)(m.g * m.ro01 * m.beta1);
+  C.g_ro02_b2 = (float)(m.g * m.ro02 * m.beta2);
+  C.g_dro = (float)(m.g * (m.ro02 - m.ro01));
+  C.neg_inv_mu1 = (float)(-1.0 / m.mu1);
+  C.neg_inv_mu2 = (float)(-1.0 / m.mu2);
+  for (int md = 0; md < 2; md++) {
+    const double lam = m.lambda[md], swr = m.S_wr[md];
+    C.K[md] = (float)m.K[md];
+    C.m[md] = (float)m.m[md];
+    C.swr[md] = (float)swr;
+    C.inv_1mswr[md] = (float)(1.0 / (1.0 - swr));
+    C.e1[md] = (float)((2. + 3. * lam) / lam);
+    C.e2[md] = (float)((2. + lam) / lam);
+    C.m_inv_lam[md] = (float)(-1. / lam);
+    C.inv_lam_1mswr[md] = (float)(1.0 / (lam * (1.0 - swr)));
+    C.P_d[md] = (float)m.P_d[md];
+  }
+  C.H_d = H; C.beta1_d = m.beta1; C.beta2_d = m.beta2; C.ro01_d = m.ro01; C.ro02_d = m.ro02;
+  C.dtsrc_d = m.dt * src;
+  C.V = V;
+  C.H_df = gbf_df_from_double(H);
+  C.beta1_df = gbf_df_from_double(m.beta1);
+  C.beta2_df = gbf_df_from_double(m.beta2);
+  C.ro01_df = gbf_df_from_double(m.ro01);
+  C.ro02_df = gbf_df_from_double(m.ro02);
+  C.dtsrc_df = gbf_df_from_double(C.dtsrc_d);
+  for (int md = 0; md < 2; md++) {
+    C.m_d[md] = m.m[md];
+    C.m_df[md] = gbf_df_from_double(m.m[md]);
+    C.dtsrc_m_d[md] = C.dtsrc_d / m.m[md];
+    C.dtsrc_m_df[md] = gbf_df_from_double(C.dtsrc_m_d[md]);
+  }
+  return C;
+}
+
+namespace {
+
+constexpr int kThreads = 256;
+
+int tiles_x(const GbfSplitConsts& C) { return (C.nx - 2 + kSplitTX - 1) / kSplitTX; }
+int tiles_y(const GbfSplitConsts& C) { return (C.ny - 2 + kSplitTY - 1) / kSplitTY; }
+
+template <bool DF>
+__global__ void __launch_bounds__(kSplitThreads) k_split_step(const GbfSplitConsts C, const GbfSplitGrid G,
+                                                              const int kchunk) {
+  __shared__ GbfSplitPlane pl[2];
+  const int ntx = (C.nx - 2 + kSplitTX - 1) / kSplitTX, nty = (C.ny - 2 + kSplitTY - 1) / kSplitTY;
+  const int b = blockIdx.x;
+  const int tx = b % ntx, ty = (b / ntx) % nty, kc = b / (ntx * nty);
+  const int k0 = 1 + kc * kchunk;
+  const int k1 = min(k0 + kchunk, C.nz - 1);
+  GbfSplitAcc<DF> acc;
+  split_tile<DF>(C, G, 1 + tx * kSplitTX, 1 + ty * kSplitTY, k0, k1, pl, acc);
+  if (acc.bad) atomicOr(G.status, GBF_DEV_NONFINITE);
+  if (G.mass_partials) split_block_mass<DF>(acc, C.V, G.mass_partials + 2 * blockIdx.x);
+}
+
+// Value the reference's boundary sweep leaves in P1 (cpu.cpp:366-403), in
+// the dP = P - P_hs(j) representation: copies within a row keep dP, the top
+// (P_atm) and the hydrostatic sides (P_hs) are dP = 0, and the bottom rule
+// P(ny-1) = P(ny-2) + ro1(i,1,0) g h2 becomes dP(ny-2) + (ro1(i,1,0) - rho01) g h2.
+__device__ float sweep_dP(const gbf_model& m, const GbfGeo& g, const float* cur, const float* old, int i, int j,
+                          int k, float H) {
+  bool has_add = false;
+  float add = 0.f, base = NAN;
+  for (int hop = 0; hop < 6; ++hop) {
+    if (m.bc_mode == GBF_BC_HYDROSTATIC_SIDES && (i == 0 || i == g.nx - 1 || k == 0 || k == g.nz - 1)) {
+      base = 0.f;
+      break;
+    }
+    if (i == 0) { base = gbf_later(g, cur, old, 1, j, k); break; }
+    if (i == g.nx - 1) {
+      i = g.nx - 2;
+      if (!gbf_is_boundary(g, i, j, k)) { base = cur[gbf_idx(g, i, j, k)]; break; }
+      continue;
+    }
+    if (j == g.ny - 1) {
+      // start-of-step water density at (i, 1, 0): P - P_atm = dP_old + H
+      const float pp = old[(size_t)i + (size_t)g.nx] + H;
+      add = (float)(m.ro01 * m.beta1 * m.g * m.h2) * pp;
+      has_add = true;
+      j = g.ny - 2;
+      if (!gbf_is_boundary(g, i, j, k)) { base = cur[gbf_idx(g, i, j, k)]; break; }
+      continue;
+    }
+    if (j == 0) { base = 0.f; break; }
+    if (k == 0) { base = gbf_later(g, cur, old, i, j, 1); break; }
+    if (k == g.nz - 1) {
+      k = g.nz - 2;
+      if (!gbf_is_boundary(g, i, j, k)) { base = cur[gbf_idx(g, i, j, k)]; break; }
+      continue;
+    }
+    base = cur[gbf_idx(g, i, j, k)];
+    break;
+  }
+  return has_add ? base + add : base;
+}
+
+__global__ void __launch_bounds__(kThreads) k_split_boundary(const gbf_model m, const GbfSplitGrid G, float H) {
+  const GbfGeo g = gbf_geo(m);
+  const size_t nb = gbf_boundary_count(g);
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < nb; t += (size_t)gridDim.x * blockDim.x) {
+    int i, j, k;
+    gbf_boundary_cell(g, t, i, j, k);
+    const size_t c = gbf_idx(g, i, j, k);
+    G.Sn[c] = gbf_sweep_S<float>(m, g, G.Sn, G.S, i, j, k);
+    G.dPn[c] = sweep_dP(m, g, G.dPn, G.dP, i, j, k, H);
+  }
+}
+
+__global__ void k_split_mass_tail(const double* partials, int nblocks, double* out) {
+  __shared__ double red[2][256];
+  double a = 0., b = 0.;
+  for (int q = threadIdx.x; q < nblocks; q += blockDim.x) { a += partials[2 * q]; b += partials[2 * q + 1]; }
+  red[0][threadIdx.x] = a;
+  red[1][threadIdx.x] = b;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) { red[0][threadIdx.x] += red[0][threadIdx.x + o]; red[1][threadIdx.x] += red[1][threadIdx.x + o]; }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) { out[0] = red[0][0]; out[1] = red[1][0]; }
+}
+
+__global__ void k_split_init(const gbf_model m, const double* P, const double* S, float* dPf, float* Sf,
+                             double* M1, double* M2, int df) {
+  const GbfGeo g = gbf_geo(m);
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < g.n; c += (size_t)gridDim.x * blockDim.x) {
+    const int j = (int)((c / g.nx) % g.ny);
+    const double p = P[c], s = S[c];
+    dPf[c] = (float)(p - gbf_p_hydrostatic(m, j));
+    Sf[c] = (float)s;
+    // ro1 (1 - S2), ro2 S2 with P2 = P1 (cpu.cpp:72-73, 224-225)
+    const double m1 = m.ro01 * (1. + m.beta1 * (p - m.P_atm)) * (1. - s);
+    const double m2 = m.ro02 * (1. + m.beta2 * (p - m.P_atm)) * s;
+    if (df) {
+      reinterpret_cast<float2*>(M1)[c] = gbf_df_from_double(m1);
+      reinterpret_cast<float2*>(M2)[c] = gbf_df_from_double(m2);
+    } else {
+      M1[c] = m1;
+      M2[c] = m2;
+    }
+  }
+}
+
+__global__ void k_split_to_f64(const gbf_model m, const float* dPf, const float* Sf, double* P, double* S) {
+  const GbfGeo g = gbf_geo(m);
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < g.n; c += (size_t)gridDim.x * blockDim.x) {
+    const int j = (int)((c / g.nx) % g.ny);
+    if (P) P[c] = gbf_p_hydrostatic(m, j) + (double)dPf[c];
+    if (S) S[c] = (double)Sf[c];
+  }
+}
+
+}  // namespace
+
+// k planes per CTA: enough CTAs to fill the GPU several times over, long
+// enough runs that the one-plane prologue stays small.
+int gbf_split_kchunk(const GbfSplitConsts& C) {
+  const long long tiles = (long long)tiles_x(C) * tiles_y(C);
+  const long long want = 6LL * gbf_num_sms();
+  int chunks = (int)((want + tiles - 1) / tiles);
+  if (chunks < 1) chunks = 1;
+  int kchunk = (C.nz - 2 + chunks - 1) / chunks;
+  if (kchunk < 16) kchunk = 16;
+  return kchunk;
+}
+
+int gbf_split_launch_domain(const gbf_model& m, const GbfSplitConsts& C, const GbfSplitGrid& G, bool df,
+                            double* mass_out, cudaStream_t st, GbfTimer* tm) {
+  const int kchunk = gbf_split_kchunk(C);
+  const int nkc = (C.nz - 2 + kchunk - 1) / kchunk;
+  const unsigned blocks = (unsigned)(tiles_x(C) * tiles_y(C) * nkc);
+  cudaEvent_t e = gbf_timer_begin(tm, st);
+  if (df)
+    k_split_step<true><<<blocks, kSplitThreads, 0, st>>>(C, G, kchunk);
+  else
+    k_split_step<false><<<blocks, kSplitThreads, 0, st>>>(C, G, kchunk);
+  gbf_timer_end(tm, GBF_K_SPLIT_STEP, e, st);
+  e = gbf_timer_begin(tm, st);
+  k_split_boundary<<<gbf_grid_for(gbf_boundary_count(gbf_geo(m)), kThreads, 4), kThreads, 0, st>>>(m, G, C.H);
+  gbf_timer_end(tm, GBF_K_SPLIT_BOUNDARY, e, st);
+  if (G.mass_partials && mass_out) {
+    e = gbf_timer_begin(tm, st);
+    k_split_mass_tail<<<1, 256, 0, st>>>(G.mass_partials, (int)blocks, mass_out);
+    gbf_timer_end(tm, GBF_K_MASS_TAIL, e, st);
+  }
+  cudaError_t err = cudaGetLastError();
+  return err == cudaSuccess ? GBF_OK : gbf_cuda_check(err, "gbf_split_launch_domain");
+}
+
+unsigned gbf_split_blocks(const gbf_model& m) {
+  const GbfSplitConsts C = gbf_split_consts(m);
+  const int kchunk = gbf_split_kchunk(C);
+  return (unsigned)(tiles_x(C) * tiles_y(C) * ((C.nz - 2 + kchunk - 1) / kchunk));
+}
+
+// ----------------------------------------------------------------- host side
+
+int gbf_split_alloc(gbf_domain* d) {
+  const size_t n = gbf_geo(d->m).n;
+  int s = GBF_OK;
+  for (int b = 0; b < 2 && !s; b++) {
+    s |= gbf_domain_alloc(d, (void**)&d->Pf[b], n * sizeof(float));
+    s |= gbf_domain_alloc(d, (void**)&d->Sf[b], n * sizeof(float));
+  }
+  // FP64 masses or FP32 pairs: 8 bytes per cell and phase either way
+  if (!s) s |= gbf_domain_alloc(d, (void**)&d->M1, n * sizeof(double));
+  if (!s) s |= gbf_domain_alloc(d, (void**)&d->M2, n * sizeof(double));
+  // per-block mass partials of the split step kernel
+  if (!s) s |= gbf_domain_alloc(d, (void**)&d->split_partials, 2 * sizeof(double) * gbf_split_blocks(d->m));
+  return s ? GBF_ERR_NOMEM : GBF_OK;
+}
+
 int gbf_split_upload(gbf_domain* d, const double* P1, const double* S2, cudaMemcpyKind kind) {
-  (void)d; (void)P1; (void)S2; (void)kind;
-  return gbf_fail(GBF_ERR_ARG, "split precision not built yet");
+  const size_t n = gbf_geo(d->m).n, b = n * sizeof(double);
+  const double *P = P1, *S = S2;
+  double* tmp = nullptr;
+  if (kind == cudaMemcpyHostToDevice) {  // stage through device memory
+    GBF_CUDA(cudaMallocAsync((void**)&tmp, 2 * b, d->stream));
+    GBF_CUDA(cudaMemcpyAsync(tmp, P1, b, cudaMemcpyHostToDevice, d->stream));
+    GBF_CUDA(cudaMemcpyAsync(tmp + n, S2, b, cudaMemcpyHostToDevice, d->stream));
+    P = tmp;
+    S = tmp + n;
+  }
+  d->cur = 0;
+  k_split_init<<<gbf_grid_for(n, kThreads, 4), kThreads, 0, d->stream>>>(
+      d->m, P, S, d->Pf[0], d->Sf[0], d->M1, d->M2, d->precision == GBF_PREC_SPLIT_DF);
+  GBF_CUDA(cudaGetLastError());
+  // the next-state buffer's faces are rewritten every step; start them equal
+  GBF_CUDA(cudaMemcpyAsync(d->Pf[1], d->Pf[0], n * sizeof(float), cudaMemcpyDeviceToDevice, d->stream));
+  GBF_CUDA(cudaMemcpyAsync(d->Sf[1], d->Sf[0], n * sizeof(float), cudaMemcpyDeviceToDevice, d->stream));
+  if (tmp) GBF_CUDA(cudaFreeAsync(tmp, d->stream));
+  return GBF_OK;
 }
-int gbf_split_step(gbf_domain* d) { (void)d; return gbf_fail(GBF_ERR_ARG, "split precision not built yet"); }
+
+int gbf_split_step(gbf_domain* d) {
+  const int nxt = d->cur ^ 1;
+  GbfSplitGrid G;
+  G.dP = d->Pf[d->cur];
+  G.S = d->Sf[d->cur];
+  G.dPn = d->Pf[nxt];
+  G.Sn = d->Sf[nxt];
+  G.K = d->cells.K;
+  G.phi = d->cells.phi;
+  G.media = d->cells.media;
+  G.M1 = d->M1;
+  G.M2 = d->M2;
+  G.mass_partials = nullptr;
+  G.status = d->status;
+  double* mass_out = nullptr;
+  if ((d->out_flags & GBF_OUT_MASS) && d->mass_hist && d->mass_count < d->mass_cap) {
+    G.mass_partials = d->split_partials;
+    mass_out = d->mass_hist + 2 * d->mass_count;
+    d->mass_count++;
+  }
+  const GbfSplitConsts C = gbf_split_consts(d->m);
+  int s = gbf_split_launch_domain(d->m, C, G, d->precision == GBF_PREC_SPLIT_DF, mass_out, d->stream, &d->timer);
+  if (s) return s;
+  d->cur = nxt;
+  d->steps++;
+  return GBF_OK;
+}
+
 int gbf_split_download(gbf_domain* d, int field, double* host) {
-  (void)d; (void)field; (void)host;
-  return gbf_fail(GBF_ERR_ARG, "split precision not built yet");
+  const size_t n = gbf_geo(d->m).n, b = n * sizeof(double);
+  if (field != GBF_FIELD_P1 && field != GBF_FIELD_S2)
+    return gbf_fail(GBF_ERR_STATE, "split precision keeps P1 and S2 only");
+  double* tmp = nullptr;
+  GBF_CUDA(cudaMallocAsync((void**)&tmp, b, d->stream));
+  k_split_to_f64<<<gbf_grid_for(n, kThreads, 4), kThreads, 0, d->stream>>>(
+      d->m, d->Pf[d->cur], d->Sf[d->cur], field == GBF_FIELD_P1 ? tmp : nullptr, field == GBF_FIELD_S2 ? tmp : nullptr);
+  GBF_CUDA(cudaGetLastError());
+  GBF_CUDA(cudaMemcpyAsync(host, tmp, b, cudaMemcpyDeviceToHost, d->stream));
+  GBF_CUDA(cudaFreeAsync(tmp, d->stream));
+  GBF_CUDA(cudaStreamSynchronize(d->stream));
+  return GBF_OK;
 }
-int gbf_split_launches_per_step(gbf_domain* d) { (void)d; return 0; }
+
+int gbf_split_launches_per_step(gbf_domain* d) { return 2 + ((d->out_flags & GBF_OUT_MASS) ? 1 : 0); }

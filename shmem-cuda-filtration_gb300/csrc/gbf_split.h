@@ -1,10 +1,50 @@
-// gbf_split.h — split-precision (FP32 state, FP64 masses) domain launchers.
+// gbf_split.h — split-precision (FP32 state, FP64 or FP32-pair masses)
+// launchers and the constants of its kernels.
 #pragma once
 
 #include "gbf_domain.h"
+
+// Model constants of the split kernels, derived once on the host. FP32 for
+// the FP32 arithmetic; FP64 and FP32-pair copies for the wide residual.
+struct GbfSplitConsts {
+  int nx, ny, nz;
+  int noflow_bottom;
+  int ri0, rk0, rn;  // rate-injection patch on the j = 1 layer (rn = 0: none)
+  float inv_h1, inv_h2, inv_h3, kv, dt;
+  float H;  // rho01 g h2: hydrostatic pressure step per cell (main.cpp:114)
+  float ro01, ro02, beta1, beta2;
+  float g_ro01_b1, g_ro02_b2, g_dro;  // g rho01 beta1, g rho02 beta2, g (rho02 - rho01)
+  float neg_inv_mu1, neg_inv_mu2;
+  float K[2], m[2], swr[2], inv_1mswr[2], e1[2], e2[2], m_inv_lam[2], inv_lam_1mswr[2], P_d[2];
+  double H_d, beta1_d, beta2_d, ro01_d, ro02_d, dtsrc_d, V;
+  float2 H_df, beta1_df, beta2_df, ro01_df, ro02_df, dtsrc_df;
+  // media-table porosity and dt*src/phi in wide precision: the table values
+  // (e.g. 0.4) are not FP32 numbers, and the phase masses must not inherit
+  // the FP32 rounding of phi
+  double m_d[2], dtsrc_m_d[2];
+  float2 m_df[2], dtsrc_m_df[2];
+};
+GbfSplitConsts gbf_split_consts(const gbf_model& m);
+
+// Arrays of one grid's split-precision step.
+struct GbfSplitGrid {
+  const float* dP;  // current state
+  const float* S;
+  float* dPn;       // next state
+  float* Sn;
+  const float* K;   // NULL: media table
+  const float* phi;
+  const int* media;
+  double* M1;       // FP64, or float2 pairs in the same 8 bytes
+  double* M2;
+  double* mass_partials;  // NULL: no phase-mass sums
+  unsigned* status;
+};
 
 int gbf_split_alloc(gbf_domain* d);
 int gbf_split_upload(gbf_domain* d, const double* P1, const double* S2, cudaMemcpyKind kind);
 int gbf_split_step(gbf_domain* d);
 int gbf_split_download(gbf_domain* d, int field, double* host);
 int gbf_split_launches_per_step(gbf_domain* d);
+int gbf_split_launch_domain(const gbf_model& m, const GbfSplitConsts& C, const GbfSplitGrid& G, bool df,
+                            double* mass_out, cudaStream_t st, GbfTimer* tm);

@@ -1,0 +1,316 @@
+// gbf_split_tile.cuh — the split-precision z-marching tile (device code);
+// included by gbf_split.cu and gbf_ensemble.cu.
+#pragma once
+
+#include <math.h>
+
+#include "gbf_split.h"
+
+// ------------------------------------------------------------ FP32 pairs
+// Unevaluated sums hi + lo of two FP32 numbers ("double-float", about 48
+// significant bits) built on the error-free transformations TwoSum (Knuth,
+// TAOCP vol. 2, sec. 4.2.2), FastTwoSum (Dekker 1971) and TwoProduct through
+// FMA. Used for the phase masses and the residual in GBF_PREC_SPLIT_DF.
+struct GbfDF {
+  float hi, lo;
+};
+__device__ __forceinline__ GbfDF df_two_sum(float a, float b) {
+  float s = a + b, bb = s - a;
+  return {s, (a - (s - bb)) + (b - bb)};
+}
+__device__ __forceinline__ GbfDF df_fast_two_sum(float a, float b) {
+  float s = a + b;
+  return {s, b - (s - a)};
+}
+__device__ __forceinline__ GbfDF df_add(GbfDF a, GbfDF b) {
+  GbfDF s = df_two_sum(a.hi, b.hi);
+  return df_fast_two_sum(s.hi, s.lo + (a.lo + b.lo));
+}
+__device__ __forceinline__ GbfDF df_neg(GbfDF a) { return {-a.hi, -a.lo}; }
+__device__ __forceinline__ GbfDF df_mul(GbfDF a, GbfDF b) {
+  float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, e));
+  return df_fast_two_sum(p, e);
+}
+// a / b for an FP32 divisor: one correction of the FP32 quotient.
+__device__ __forceinline__ GbfDF df_div_f(GbfDF a, float b) {
+  float q1 = a.hi / b;
+  float p = q1 * b, pe = fmaf(q1, b, -p);
+  float r = ((a.hi - p) - pe) + a.lo;
+  return df_fast_two_sum(q1, r / b);
+}
+__host__ __device__ __forceinline__ float2 gbf_df_from_double(double d) {
+  float h = (float)d;
+  return make_float2(h, (float)(d - (double)h));
+}
+
+// Wide arithmetic of the masses and the residual: FP64 or FP32 pairs.
+template <bool DF> struct Wide;
+template <> struct Wide<false> {
+  using T = double;
+  static __device__ __forceinline__ T f(float x) { return (double)x; }
+  static __device__ __forceinline__ T c(double d, float2) { return d; }
+  static __device__ __forceinline__ T add(T a, T b) { return a + b; }
+  static __device__ __forceinline__ T sub(T a, T b) { return a - b; }
+  static __device__ __forceinline__ T mul(T a, T b) { return a * b; }
+  static __device__ __forceinline__ T div_f(T a, float b) { return a / (double)b; }
+  static __device__ __forceinline__ float tof(T a) { return (float)a; }
+  static __device__ __forceinline__ double tod(T a) { return a; }
+  static __device__ __forceinline__ T load(const double* p, size_t i) { return p[i]; }
+  static __device__ __forceinline__ void store(double* p, size_t i, T v) { p[i] = v; }
+};
+template <> struct Wide<true> {
+  using T = GbfDF;
+  static __device__ __forceinline__ T f(float x) { return {x, 0.f}; }
+  static __device__ __forceinline__ T c(double, float2 v) { return {v.x, v.y}; }
+  static __device__ __forceinline__ T add(T a, T b) { return df_add(a, b); }
+  static __device__ __forceinline__ T sub(T a, T b) { return df_add(a, df_neg(b)); }
+  static __device__ __forceinline__ T mul(T a, T b) { return df_mul(a, b); }
+  static __device__ __forceinline__ T div_f(T a, float b) { return df_div_f(a, b); }
+  static __device__ __forceinline__ float tof(T a) { return a.hi + a.lo; }
+  static __device__ __forceinline__ double tod(T a) { return (double)a.hi + (double)a.lo; }
+  static __device__ __forceinline__ T load(const double* p, size_t i) {
+    float2 v = reinterpret_cast<const float2*>(p)[i];
+    return {v.x, v.y};
+  }
+  static __device__ __forceinline__ void store(double* p, size_t i, T v) {
+    reinterpret_cast<float2*>(p)[i] = make_float2(v.hi, v.lo);
+  }
+};
+
+// ------------------------------------------------------------- tile shape
+constexpr int kSplitTX = 32, kSplitTY = 8;
+constexpr int kSplitThreads = kSplitTX * kSplitTY;
+constexpr int kSplitHX = kSplitTX + 2, kSplitHY = kSplitTY + 2, kSplitHN = kSplitHX * kSplitHY;
+constexpr int kSplitSlots = (kSplitHN + kSplitThreads - 1) / kSplitThreads;  // halo elements per thread
+
+// One x-y plane of the tile with its 1-cell halo.
+struct GbfSplitPlane {
+  float dP[kSplitHN], S[kSplitHN], L1[kSplitHN], L2[kSplitHN];
+};
+
+// Mobility x density of both phases at one cell (FP32): Brooks-Corey kr
+// (cpu.cpp:60-62) from one log2 and two exp2, Xi = -K kr / mu, densities at
+// P2 = P1 (cpu.cpp:63, 72-73).
+__device__ __forceinline__ void split_props(const GbfSplitConsts& C, int md, float K, float dP, float S, int j,
+                                            float& L1, float& L2) {
+  const float Pp = fmaf((float)j, C.H, dP);  // P - P_atm
+  const float Se = (1.f - S - C.swr[md]) * C.inv_1mswr[md];
+  const float l2 = __log2f(Se);
+  const float kr1 = exp2f(C.e1[md] * l2);
+  const float om = 1.f - Se;
+  const float kr2 = om * om * (1.f - exp2f(C.e2[md] * l2));
+  const float ro1 = C.ro01 * fmaf(C.beta1, Pp, 1.f);
+  const float ro2 = C.ro02 * fmaf(C.beta2, Pp, 1.f);
+  L1 = K * kr1 * C.neg_inv_mu1 * ro1;
+  L2 = K * kr2 * C.neg_inv_mu2 * ro2;
+}
+
+// Donor-cell flux difference of one direction (see gbf_f64.cu): max/min
+// forms of the reference's (x +- |x|)/2 (cpu.cpp:260-262).
+__device__ __forceinline__ float split_donor(float x1, float x2, float Lc, float Lm, float Lp) {
+  const float x2p = fmaxf(x2, 0.f), x2m = fminf(x2, 0.f);
+  const float x1p = fmaxf(x1, 0.f), x1m = fminf(x1, 0.f);
+  return (x1p * Lm - (x2p - x1m) * Lc) - x2m * Lp;
+}
+
+// Brooks-Corey capillary pressure P_d S_e^(-1/lambda) and its S-derivative (cpu.cpp:303-308).
+__device__ __forceinline__ float split_Pk(const GbfSplitConsts& C, int md, float S, float& dPk_dS) {
+  const float Se = (1.f - S - C.swr[md]) * C.inv_1mswr[md];
+  const float Pk = C.P_d[md] * exp2f(C.m_inv_lam[md] * __log2f(Se));
+  dPk_dS = Pk * C.inv_lam_1mswr[md] / Se;
+  return Pk;
+}
+
+template <bool DF>
+struct GbfSplitAcc {
+  typename Wide<DF>::T m1, m2;
+  unsigned bad;
+  __device__ GbfSplitAcc() : m1(Wide<DF>::f(0.f)), m2(Wide<DF>::f(0.f)), bad(0) {}
+};
+
+// One CTA: interior cells [i0, i0+TX) x [j0, j0+TY) of planes [k0, k1); i0,
+// j0, k0 >= 1. `pl` points to two planes of shared memory.
+template <bool DF>
+__device__ void split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i0, int j0, int k0, int k1,
+                           GbfSplitPlane* pl, GbfSplitAcc<DF>& acc) {
+  using W = Wide<DF>;
+  using WT = typename W::T;
+  const int nx = C.nx, ny = C.ny, nz = C.nz;
+  const size_t pln = (size_t)nx * ny;
+  const int tx = threadIdx.x % kSplitTX, ty = threadIdx.x / kSplitTX;
+  const int i = i0 + tx, j = j0 + ty;
+  const bool active = (i <= nx - 2) && (j <= ny - 2);
+  const int hc = (ty + 1) * kSplitHX + (tx + 1);  // own cell in the halo plane
+
+  // halo elements of this thread: plane index, global column offset (or -1), row j
+  int hq[kSplitSlots], hj[kSplitSlots];
+  long long hcol[kSplitSlots];
+#pragma unroll
+  for (int s = 0; s < kSplitSlots; s++) {
+    const int q = threadIdx.x + s * kSplitThreads;
+    hq[s] = q;
+    hcol[s] = -1;
+    hj[s] = 0;
+    if (q < kSplitHN) {
+      const int gi = i0 - 1 + q % kSplitHX, gj = j0 - 1 + q / kSplitHX;
+      if (gi < nx && gj < ny) {
+        hcol[s] = (long long)gi + (long long)gj * nx;
+        hj[s] = gj;
+      }
+    }
+  }
+  // raw inputs of the next plane, prefetched one plane ahead
+  float rP[kSplitSlots], rS[kSplitSlots], rK[kSplitSlots];
+  int rM[kSplitSlots];
+  auto fetch = [&](int k) {
+#pragma unroll
+    for (int s = 0; s < kSplitSlots; s++) {
+      rP[s] = 0.f; rS[s] = 0.f; rK[s] = 0.f; rM[s] = 0;
+      if (hcol[s] >= 0 && k < nz) {
+        const size_t c = (size_t)hcol[s] + (size_t)k * pln;
+        rP[s] = __ldg(G.dP + c);
+        rS[s] = __ldg(G.S + c);
+        rM[s] = G.media ? __ldg(G.media + c) : 0;
+        rK[s] = G.K ? __ldg(G.K + c) : C.K[rM[s]];
+      }
+    }
+  };
+  auto build = [&](GbfSplitPlane& P) {
+#pragma unroll
+    for (int s = 0; s < kSplitSlots; s++) {
+      if (hcol[s] >= 0) {
+        float L1, L2;
+        split_props(C, rM[s], rK[s], rP[s], rS[s], hj[s], L1, L2);
+        P.dP[hq[s]] = rP[s];
+        P.S[hq[s]] = rS[s];
+        P.L1[hq[s]] = L1;
+        P.L2[hq[s]] = L2;
+      }
+    }
+  };
+
+  // prologue: own column at k0 - 1 (registers), plane k0 (shared)
+  float dPm = 0.f, L1m = 0.f, L2m = 0.f;
+  if (active) {
+    const size_t c = (size_t)i + (size_t)j * nx + (size_t)(k0 - 1) * pln;
+    const int md = G.media ? G.media[c] : 0;
+    const float Kc = G.K ? G.K[c] : C.K[md];
+    dPm = G.dP[c];
+    split_props(C, md, Kc, dPm, G.S[c], j, L1m, L2m);
+  }
+  fetch(k0);
+  build(pl[0]);
+  fetch(k0 + 1);
+  __syncthreads();
+  int cur = 0;
+  const WT H = W::c(C.H_d, C.H_df), B1 = W::c(C.beta1_d, C.beta1_df), B2 = W::c(C.beta2_d, C.beta2_df);
+  const WT R01 = W::c(C.ro01_d, C.ro01_df), R02 = W::c(C.ro02_d, C.ro02_df), ONE = W::f(1.f);
+  for (int k = k0; k < k1; k++) {
+    GbfSplitPlane& Pc = pl[cur];
+    GbfSplitPlane& Pn = pl[cur ^ 1];
+    build(Pn);     // plane k + 1 from the prefetched raw values
+    fetch(k + 2);  // prefetch plane k + 2
+    __syncthreads();
+    if (active) {
+      const size_t c = (size_t)i + (size_t)j * nx + (size_t)k * pln;
+      const int md = G.media ? __ldg(G.media + c) : 0;
+      const float phi = G.phi ? __ldg(G.phi + c) : C.m[md];
+      const WT M1 = W::load(G.M1, c), M2 = W::load(G.M2, c);
+      const float dPc = Pc.dP[hc], S0 = Pc.S[hc], L1c = Pc.L1[hc], L2c = Pc.L2[hc];
+      const float dPp = Pn.dP[hc], L1p = Pn.L1[hc], L2p = Pn.L2[hc];
+      // face potentials relative to the hydrostatic profile (P2 = P1)
+      const float x1 = (Pc.dP[hc - 1] - dPc) * C.inv_h1, x2 = (dPc - Pc.dP[hc + 1]) * C.inv_h1;
+      const float yb1 = (Pc.dP[hc - kSplitHX] - dPc) * C.inv_h2;
+      const float yb2 = (dPc - Pc.dP[hc + kSplitHX]) * C.inv_h2;
+      const float z1 = (dPm - dPc) * C.inv_h3, z2 = (dPc - dPp) * C.inv_h3;
+      const bool noflow = C.noflow_bottom && (j == ny - 2);
+      const float Pp = fmaf((float)j, C.H, dPc);  // P - P_atm
+      const float gd1 = C.g_ro01_b1 * Pp;         // (rho1 - rho01) g
+      const float gd2 = fmaf(C.g_ro02_b2, Pp, C.g_dro);
+      const float y11 = yb1 + gd1, y21 = noflow ? 0.f : yb2 + gd1;
+      const float y12 = yb1 + gd2, y22 = noflow ? 0.f : yb2 + gd2;
+      const float f = split_donor(x1, x2, L1c, Pc.L1[hc - 1], Pc.L1[hc + 1]) * C.inv_h1 +
+                      C.kv * split_donor(y11, y21, L1c, Pc.L1[hc - kSplitHX], Pc.L1[hc + kSplitHX]) * C.inv_h2 +
+                      split_donor(z1, z2, L1c, L1m, L1p) * C.inv_h3;
+      const float gs = split_donor(x1, x2, L2c, Pc.L2[hc - 1], Pc.L2[hc + 1]) * C.inv_h1 +
+                       C.kv * split_donor(y12, y22, L2c, Pc.L2[hc - kSplitHX], Pc.L2[hc + kSplitHX]) * C.inv_h2 +
+                       split_donor(z1, z2, L2c, L2m, L2p) * C.inv_h3;
+      const float dtphi = C.dt / phi;
+      // mass targets (wide)
+      const WT T1 = W::add(M1, W::f(-dtphi * f));
+      WT T2 = W::add(M2, W::f(-dtphi * gs));
+      if (j == 1 && i >= C.ri0 && i < C.ri0 + C.rn && k >= C.rk0 && k < C.rk0 + C.rn)
+        T2 = W::add(T2, G.phi ? W::div_f(W::c(C.dtsrc_d, C.dtsrc_df), phi)
+                              : W::c(C.dtsrc_m_d[md], C.dtsrc_m_df[md]));
+      // residual r = F(P, S) - T at the stored state (wide), cpu.cpp:305-306
+      float dPk0;
+      const float Pk0 = split_Pk(C, md, S0, dPk0);
+      const WT pp = W::add(W::f(dPc), W::mul(W::f((float)j), H));
+      const WT a1w = W::add(ONE, W::mul(B1, pp));
+      const float r1 = W::tof(W::sub(W::mul(W::mul(R01, a1w), W::sub(ONE, W::f(S0))), T1));
+      const WT a2w = W::add(ONE, W::mul(B2, W::add(pp, W::f(Pk0))));
+      const float r2 = W::tof(W::sub(W::mul(W::mul(R02, a2w), W::f(S0)), T2));
+      // FP32 Newton on d = (dp, ds): r + [F(x + d) - F(x)] = 0, the bracket
+      // written in increments (no large terms cancel)
+      const float a0 = fmaf(C.beta1, Pp, 1.f);
+      const float b0 = fmaf(C.beta2, Pp + Pk0, 1.f);
+      float dp = 0.f, ds = 0.f, Pk = Pk0, dPk = dPk0;
+#pragma unroll 1
+      for (int it = 0; it < 4; it++) {
+        const float S1 = S0 + ds;
+        const float G1 = r1 + C.ro01 * (C.beta1 * dp * (1.f - S1) - a0 * ds);
+        const float G2 = r2 + C.ro02 * (b0 * ds + C.beta2 * (dp + (Pk - Pk0)) * S1);
+        const float J11 = C.ro01 * C.beta1 * (1.f - S1);
+        const float J12 = -C.ro01 * (a0 + C.beta1 * dp);
+        const float J21 = C.ro02 * C.beta2 * S1;
+        const float J22 = C.ro02 * (b0 + C.beta2 * (dp + (Pk - Pk0)) + C.beta2 * dPk * S1);
+        const float inv = 1.f / (J11 * J22 - J12 * J21);
+        const float ep = inv * (J22 * G1 - J12 * G2);
+        const float es = inv * (J11 * G2 - J21 * G1);
+        dp -= ep;
+        ds -= es;
+        Pk = split_Pk(C, md, S0 + ds, dPk);
+        if (fabsf(es) <= 1e-7f * fmaxf(fabsf(ds), 1e-6f) && fabsf(ep) <= 1e-7f * fmaxf(fabsf(dp), 1e-2f)) break;
+      }
+      const float dPn = dPc + dp, Sn = S0 + ds;
+      G.dPn[c] = dPn;
+      G.Sn[c] = Sn;
+      W::store(G.M1, c, T1);
+      // next step's ro2 S2 is taken at P2 = P1, without P_k (cpu.cpp:63 vs :306)
+      W::store(G.M2, c, W::sub(T2, W::f(C.ro02 * C.beta2 * Pk * Sn)));
+      if (G.mass_partials) {
+        const WT phw = G.phi ? W::f(phi) : W::c(C.m_d[md], C.m_df[md]);
+        acc.m1 = W::add(acc.m1, W::mul(phw, T1));
+        acc.m2 = W::add(acc.m2, W::mul(phw, T2));
+      }
+      if (!isfinite(dPn) || !isfinite(Sn)) acc.bad = 1;
+      dPm = dPc;
+      L1m = L1c;
+      L2m = L2c;
+    }
+    __syncthreads();
+    cur ^= 1;
+  }
+}
+
+// Deterministic block reduction of the phase-mass partial sums (FP64).
+template <bool DF>
+__device__ __forceinline__ void split_block_mass(const GbfSplitAcc<DF>& acc, double V, double* out2) {
+  __shared__ double red[2][kSplitThreads / 32];
+  double a = Wide<DF>::tod(acc.m1), b = Wide<DF>::tod(acc.m2);
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_down_sync(0xffffffffu, a, o);
+    b += __shfl_down_sync(0xffffffffu, b, o);
+  }
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) { red[0][w] = a; red[1][w] = b; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double x = 0., y = 0.;
+    for (int q = 0; q < kSplitThreads / 32; q++) { x += red[0][q]; y += red[1][q]; }
+    out2[0] = x * V;
+    out2[1] = y * V;
+  }
+}

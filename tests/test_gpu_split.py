@@ -1,0 +1,116 @@
+"""Split-precision forms against the FP64 oracle (and, at sizes the oracle
+cannot finish quickly, against the FP64 GPU path that the oracle pins).
+
+Bars (the precision form's targets): max |dS| <= 1e-5 against the FP64
+oracle; relative L2 of P reported and bounded; relative phase-mass drift
+<= 1e-9 per step where DNAPL enters through the mass-rate source (the wide
+source term is exact to ~1e-15). Where it enters through the reference's
+Dirichlet patch instead, every kilogram of it crosses an FP32 face flux, so
+its total carries FP32 rounding (bound 1e-6 there).
+"""
+import numpy as np
+import pytest
+
+from gpu_util import rel_l2
+from test_gpu_f64 import make_case
+
+pytestmark = pytest.mark.gpu
+
+SPLITS = ["split", "split_df"]
+DS_TOL = 1e-5
+
+
+def prec(abi, name):
+    return {"split": abi.GBF_PREC_SPLIT, "split_df": abi.GBF_PREC_SPLIT_DF, "f64": abi.GBF_PREC_F64}[name]
+
+
+def domain_cls(pkg):
+    from importlib import import_module
+    return import_module(pkg.__name__ + ".domain").Domain
+
+
+@pytest.mark.parametrize("case", ["reference_ini_16", "reference_odd_5x7x6", "c0_rate_hydrostatic_40",
+                                  "heterogeneous_aniso_24x20x18"])
+@pytest.mark.parametrize("form", SPLITS)
+def test_split_matches_fp64_oracle(gpu_lib, abi, O, oracle, pkg, case, form):
+    Domain = domain_cls(pkg)
+    m, st, steps = make_case(abi, O, gpu_lib, case)
+    m.newton_tol = 0.0
+    st.model = m
+    oracle.initial(st)
+    P0, S0 = st["P1"].copy(), st["S2"].copy()
+    dom = Domain(m, st.media, st.K, st.phi, precision=prec(abi, form))
+    dom.set_outputs(abi.GBF_OUT_MASS, steps)
+    dom.upload(P0, S0)
+    ref_mass = oracle.step(st, steps, want_mass=True)
+    dom.step(steps)
+    assert dom.status() == abi.GBF_OK
+    P, S = dom.download("P1"), dom.download("S2")
+    ds = float(np.abs(S - st["S2"]).max())
+    assert ds <= DS_TOL, f"max|dS| {ds:.3e}"
+    assert np.abs(st["S2"] - S0).max() > 1e-8
+    # pressure: FP32 storage of the deviation from hydrostatic
+    assert rel_l2(P, st["P1"]) <= 1e-6
+    mass = dom.mass_history(steps)
+    assert mass.shape == (steps, 2)
+    rate_mode = m.source_mode == abi.GBF_SOURCE_RATE
+    for ph in range(2):
+        ref = ref_mass[:, ph]
+        mask = np.abs(ref) > 0
+        if not mask.any():
+            continue
+        drift = np.abs(mass[mask, ph] - ref[mask]) / np.abs(ref[mask])
+        bar = 1e-9 if (rate_mode or ph == 0) else 1e-6
+        assert drift.max() <= bar, f"phase {ph + 1} drift {drift.max():.3e} > {bar:.0e}"
+    dom.close()
+
+
+@pytest.mark.parametrize("form", SPLITS)
+def test_split_matches_fp64_gpu_at_96_cubed(gpu_lib, abi, pkg, form):
+    """A 96^3 heterogeneous rate-injection grid (config-1 fields) with the
+    reference ini's compressibilities, so that the saturation moves within
+    the run: split form against the FP64 GPU path (itself pinned to the
+    oracle) after 60 steps."""
+    from importlib import import_module
+    wl = import_module(pkg.__name__ + ".workloads")
+    Domain = domain_cls(pkg)
+    mem = wl.config1(gpu_lib, n=96, seed=1234)
+    mem.model.beta1, mem.model.beta2 = 1e-4, 1e-8
+    mem.model.rate = 2.0
+    wl.set_stable_dt(gpu_lib, mem, 0.5)
+    mem.model.newton_tol = 1e-11
+    P0, S0 = mem.initial_state()
+    ref = Domain(mem.model, mem.media, mem.K, mem.phi, precision=abi.GBF_PREC_F64)
+    ref.set_outputs(abi.GBF_OUT_MASS, 60)
+    ref.upload(P0, S0)
+    ref.step(60)
+    dut = Domain(mem.model, mem.media, mem.K, mem.phi, precision=prec(abi, form))
+    dut.set_outputs(abi.GBF_OUT_MASS, 60)
+    dut.upload(P0, S0)
+    dut.step(60)
+    assert ref.status() == abi.GBF_OK and dut.status() == abi.GBF_OK
+    Sr, Sd = ref.download("S2"), dut.download("S2")
+    assert Sr.max() > 1e-3
+    assert np.abs(Sd - Sr).max() <= DS_TOL
+    assert rel_l2(dut.download("P1"), ref.download("P1")) <= 1e-6
+    mr, md = ref.mass_history(60), dut.mass_history(60)
+    for ph in range(2):
+        drift = np.abs(md[:, ph] - mr[:, ph]) / np.abs(mr[:, ph])
+        assert drift.max() <= 1e-9, (ph, drift.max())
+    ref.close()
+    dut.close()
+
+
+def test_split_nonfinite_status(gpu_lib, abi, O, oracle, pkg):
+    Domain = domain_cls(pkg)
+    m = abi.reference_model(40, 12, 12, 0.01)
+    st = O.State(m)
+    oracle.initial(st)
+    S = st["S2"].copy()
+    S[5, 5, 17] = np.nan
+    dom = Domain(m, precision=abi.GBF_PREC_SPLIT_DF)
+    dom.upload(st["P1"], S)
+    dom.step(2)
+    assert dom.status() == abi.GBF_ERR_NONFINITE
+    gpu_lib.gbf_clear_status()
+    dom.close()
