@@ -204,6 +204,8 @@ double gbf_stable_dt(const gbf_model* m, const gbf_cells* cells, double safety) 
 int gbf_model_validate(const gbf_model* m, const gbf_cells* cells, int check_dt) {
   if (!m) return gbf_fail(GBF_ERR_ARG, "model is NULL");
   if (m->nx < 3 || m->ny < 3 || m->nz < 3) return gbf_fail(GBF_ERR_ARG, "grid dimensions must be >= 3");
+  // kernels index one grid with 32-bit offsets
+  if ((double)m->nx * m->ny * m->nz >= 2147483648.0) return gbf_fail(GBF_ERR_ARG, "grid holds 2^31 cells or more");
   if (!(m->h1 > 0 && m->h2 > 0 && m->h3 > 0 && m->dt > 0)) return gbf_fail(GBF_ERR_ARG, "h and dt must be > 0");
   if (!(m->mu1 > 0 && m->mu2 > 0 && m->ro01 > 0 && m->ro02 > 0)) return gbf_fail(GBF_ERR_ARG, "fluid constants");
   if (m->newton_iterations < 1 || m->newton_iterations > 64) return gbf_fail(GBF_ERR_ARG, "newton_iterations");

@@ -79,7 +79,7 @@ int tiles_x(const GbfSplitConsts& C) { return (C.nx - 2 + kSplitTX - 1) / kSplit
 int tiles_y(const GbfSplitConsts& C) { return (C.ny - 2 + kSplitTY - 1) / kSplitTY; }
 
 template <bool DF>
-__global__ void __launch_bounds__(kSplitThreads) k_split_step(const GbfSplitConsts C, const GbfSplitGrid G,
+__global__ void __launch_bounds__(kSplitThreads, 4) k_split_step(const GbfSplitConsts C, const GbfSplitGrid G,
                                                               const int kchunk) {
   __shared__ GbfSplitPlane pl[2];
   const int ntx = (C.nx - 2 + kSplitTX - 1) / kSplitTX, nty = (C.ny - 2 + kSplitTY - 1) / kSplitTY;

@@ -55,6 +55,7 @@ template <> struct Wide<false> {
   static __device__ __forceinline__ T sub(T a, T b) { return a - b; }
   static __device__ __forceinline__ T mul(T a, T b) { return a * b; }
   static __device__ __forceinline__ T div_f(T a, float b) { return a / (double)b; }
+  static __device__ __forceinline__ T mulf(T a, float b) { return a * (double)b; }
   static __device__ __forceinline__ float tof(T a) { return (float)a; }
   static __device__ __forceinline__ double tod(T a) { return a; }
   static __device__ __forceinline__ T load(const double* p, size_t i) { return p[i]; }
@@ -68,6 +69,12 @@ template <> struct Wide<true> {
   static __device__ __forceinline__ T sub(T a, T b) { return df_add(a, df_neg(b)); }
   static __device__ __forceinline__ T mul(T a, T b) { return df_mul(a, b); }
   static __device__ __forceinline__ T div_f(T a, float b) { return df_div_f(a, b); }
+  static __device__ __forceinline__ T mulf(T a, float b) {  // pair times FP32
+    float p = a.hi * b;
+    float e = fmaf(a.hi, b, -p);
+    e = fmaf(a.lo, b, e);
+    return df_fast_two_sum(p, e);
+  }
   static __device__ __forceinline__ float tof(T a) { return a.hi + a.lo; }
   static __device__ __forceinline__ double tod(T a) { return (double)a.hi + (double)a.lo; }
   static __device__ __forceinline__ T load(const double* p, size_t i) {
@@ -138,7 +145,7 @@ __device__ void split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i
   using W = Wide<DF>;
   using WT = typename W::T;
   const int nx = C.nx, ny = C.ny, nz = C.nz;
-  const size_t pln = (size_t)nx * ny;
+  const unsigned pln = (unsigned)nx * (unsigned)ny;  // grids hold < 2^32 cells (checked on the host)
   const int tx = threadIdx.x % kSplitTX, ty = threadIdx.x / kSplitTX;
   const int i = i0 + tx, j = j0 + ty;
   const bool active = (i <= nx - 2) && (j <= ny - 2);
@@ -146,7 +153,7 @@ __device__ void split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i
 
   // halo elements of this thread: plane index, global column offset (or -1), row j
   int hq[kSplitSlots], hj[kSplitSlots];
-  long long hcol[kSplitSlots];
+  int hcol[kSplitSlots];
 #pragma unroll
   for (int s = 0; s < kSplitSlots; s++) {
     const int q = threadIdx.x + s * kSplitThreads;
@@ -156,7 +163,7 @@ __device__ void split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i
     if (q < kSplitHN) {
       const int gi = i0 - 1 + q % kSplitHX, gj = j0 - 1 + q / kSplitHX;
       if (gi < nx && gj < ny) {
-        hcol[s] = (long long)gi + (long long)gj * nx;
+        hcol[s] = gi + gj * nx;
         hj[s] = gj;
       }
     }
@@ -169,7 +176,7 @@ __device__ void split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i
     for (int s = 0; s < kSplitSlots; s++) {
       rP[s] = 0.f; rS[s] = 0.f; rK[s] = 0.f; rM[s] = 0;
       if (hcol[s] >= 0 && k < nz) {
-        const size_t c = (size_t)hcol[s] + (size_t)k * pln;
+        const unsigned c = (unsigned)hcol[s] + (unsigned)k * pln;
         rP[s] = __ldg(G.dP + c);
         rS[s] = __ldg(G.S + c);
         rM[s] = G.media ? __ldg(G.media + c) : 0;
@@ -194,7 +201,7 @@ __device__ void split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i
   // prologue: own column at k0 - 1 (registers), plane k0 (shared)
   float dPm = 0.f, L1m = 0.f, L2m = 0.f;
   if (active) {
-    const size_t c = (size_t)i + (size_t)j * nx + (size_t)(k0 - 1) * pln;
+    const unsigned c = (unsigned)(i + j * nx) + (unsigned)(k0 - 1) * pln;
     const int md = G.media ? G.media[c] : 0;
     const float Kc = G.K ? G.K[c] : C.K[md];
     dPm = G.dP[c];
@@ -205,8 +212,7 @@ __device__ void split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i
   fetch(k0 + 1);
   __syncthreads();
   int cur = 0;
-  const WT H = W::c(C.H_d, C.H_df), B1 = W::c(C.beta1_d, C.beta1_df), B2 = W::c(C.beta2_d, C.beta2_df);
-  const WT R01 = W::c(C.ro01_d, C.ro01_df), R02 = W::c(C.ro02_d, C.ro02_df), ONE = W::f(1.f);
+  const WT R01 = W::c(C.ro01_d, C.ro01_df), R02 = W::c(C.ro02_d, C.ro02_df);
   for (int k = k0; k < k1; k++) {
     GbfSplitPlane& Pc = pl[cur];
     GbfSplitPlane& Pn = pl[cur ^ 1];
@@ -214,7 +220,7 @@ __device__ void split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i
     fetch(k + 2);  // prefetch plane k + 2
     __syncthreads();
     if (active) {
-      const size_t c = (size_t)i + (size_t)j * nx + (size_t)k * pln;
+      const unsigned c = (unsigned)(i + j * nx) + (unsigned)k * pln;
       const int md = G.media ? __ldg(G.media + c) : 0;
       const float phi = G.phi ? __ldg(G.phi + c) : C.m[md];
       const WT M1 = W::load(G.M1, c), M2 = W::load(G.M2, c);
@@ -238,42 +244,58 @@ __device__ void split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i
                        C.kv * split_donor(y12, y22, L2c, Pc.L2[hc - kSplitHX], Pc.L2[hc + kSplitHX]) * C.inv_h2 +
                        split_donor(z1, z2, L2c, L2m, L2p) * C.inv_h3;
       const float dtphi = C.dt / phi;
-      // mass targets (wide)
-      const WT T1 = W::add(M1, W::f(-dtphi * f));
-      WT T2 = W::add(M2, W::f(-dtphi * gs));
-      if (j == 1 && i >= C.ri0 && i < C.ri0 + C.rn && k >= C.rk0 && k < C.rk0 + C.rn)
-        T2 = W::add(T2, G.phi ? W::div_f(W::c(C.dtsrc_d, C.dtsrc_df), phi)
-                              : W::c(C.dtsrc_m_d[md], C.dtsrc_m_df[md]));
-      // residual r = F(P, S) - T at the stored state (wide), cpu.cpp:305-306
+      const float dm1 = -dtphi * f, dm2 = -dtphi * gs;  // FP32 mass increments
+      // mass targets T = M + dm (wide), the rate source added exactly
+      const WT T1 = W::add(M1, W::f(dm1));
+      WT T2 = W::add(M2, W::f(dm2));
+      float srcf = 0.f;
+      if (j == 1 && i >= C.ri0 && i < C.ri0 + C.rn && k >= C.rk0 && k < C.rk0 + C.rn) {
+        const WT src = G.phi ? W::div_f(W::c(C.dtsrc_d, C.dtsrc_df), phi) : W::c(C.dtsrc_m_d[md], C.dtsrc_m_df[md]);
+        T2 = W::add(T2, src);
+        srcf = W::tof(src);
+      }
+      // residual r = F(P, S) - T at the stored state, cpu.cpp:305-306, split
+      // into its large part rho0 (1 - S) - M (wide; the products of FP32
+      // numbers are exact) and small FP32 parts rho0 beta P' (..) and dm:
+      //   r1 = (rho01 - M1 - rho01 S) + rho01 beta1 P' (1 - S) - dm1
+      //   r2 = (rho02 S - M2) + rho02 beta2 (P' + P_k) S - dm2 - src
       float dPk0;
       const float Pk0 = split_Pk(C, md, S0, dPk0);
-      const WT pp = W::add(W::f(dPc), W::mul(W::f((float)j), H));
-      const WT a1w = W::add(ONE, W::mul(B1, pp));
-      const float r1 = W::tof(W::sub(W::mul(W::mul(R01, a1w), W::sub(ONE, W::f(S0))), T1));
-      const WT a2w = W::add(ONE, W::mul(B2, W::add(pp, W::f(Pk0))));
-      const float r2 = W::tof(W::sub(W::mul(W::mul(R02, a2w), W::f(S0)), T2));
+      const float r1 = W::tof(W::sub(W::sub(R01, M1), W::mulf(R01, S0))) +
+                       C.ro01 * C.beta1 * Pp * (1.f - S0) - dm1;
+      const float r2 = W::tof(W::sub(W::mulf(R02, S0), M2)) + C.ro02 * C.beta2 * (Pp + Pk0) * S0 - dm2 - srcf;
       // FP32 Newton on d = (dp, ds): r + [F(x + d) - F(x)] = 0, the bracket
-      // written in increments (no large terms cancel)
+      // written in increments so that no large terms cancel; the increment
+      // equations are nearly linear, so two iterations reach FP32 round-off.
       const float a0 = fmaf(C.beta1, Pp, 1.f);
       const float b0 = fmaf(C.beta2, Pp + Pk0, 1.f);
-      float dp = 0.f, ds = 0.f, Pk = Pk0, dPk = dPk0;
-#pragma unroll 1
-      for (int it = 0; it < 4; it++) {
+      float dp, ds, Pk, dPk;
+      {
+        const float J11 = C.ro01 * C.beta1 * (1.f - S0), J12 = -C.ro01 * a0;
+        const float J21 = C.ro02 * C.beta2 * S0, J22 = C.ro02 * fmaf(C.beta2 * dPk0, S0, b0);
+        const float inv = 1.f / (J11 * J22 - J12 * J21);
+        dp = -inv * (J22 * r1 - J12 * r2);
+        ds = -inv * (J11 * r2 - J21 * r1);
+      }
+      {
+        float dPk1;
+        const float Pk1 = split_Pk(C, md, S0 + ds, dPk1);
         const float S1 = S0 + ds;
         const float G1 = r1 + C.ro01 * (C.beta1 * dp * (1.f - S1) - a0 * ds);
-        const float G2 = r2 + C.ro02 * (b0 * ds + C.beta2 * (dp + (Pk - Pk0)) * S1);
+        const float G2 = r2 + C.ro02 * (b0 * ds + C.beta2 * (dp + (Pk1 - Pk0)) * S1);
         const float J11 = C.ro01 * C.beta1 * (1.f - S1);
         const float J12 = -C.ro01 * (a0 + C.beta1 * dp);
         const float J21 = C.ro02 * C.beta2 * S1;
-        const float J22 = C.ro02 * (b0 + C.beta2 * (dp + (Pk - Pk0)) + C.beta2 * dPk * S1);
+        const float J22 = C.ro02 * (b0 + C.beta2 * (dp + (Pk1 - Pk0)) + C.beta2 * dPk1 * S1);
         const float inv = 1.f / (J11 * J22 - J12 * J21);
         const float ep = inv * (J22 * G1 - J12 * G2);
         const float es = inv * (J11 * G2 - J21 * G1);
         dp -= ep;
         ds -= es;
-        Pk = split_Pk(C, md, S0 + ds, dPk);
-        if (fabsf(es) <= 1e-7f * fmaxf(fabsf(ds), 1e-6f) && fabsf(ep) <= 1e-7f * fmaxf(fabsf(dp), 1e-2f)) break;
+        Pk = fmaf(-dPk1, es, Pk1);  // P_k at the final S, to first order in the last correction
+        dPk = dPk1;
       }
+      (void)dPk;
       const float dPn = dPc + dp, Sn = S0 + ds;
       G.dPn[c] = dPn;
       G.Sn[c] = Sn;
