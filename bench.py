@@ -1,28 +1,33 @@
 """Benchmark of the GB300 hot path: cell-steps/s of the two-phase flow step.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload NAME] [--cube N]
+                    [--workload NAME] [--cube N] [--no-compare] [--no-cpu-baseline]
+
+Workloads are <config>_<precision>: config0..config4 (the benchmark
+configurations as seeded synthetic inputs, see workloads.py) and f64, split
+(FP64 masses), splitdf (FP32-pair masses). The default, config4_splitdf, is
+the combined precision + batching form on the 256-member ensemble; the same
+line also reports plain FP64 and FP64-mass split on the same members.
 
 One JSON line on rank 0. `value` is device-resident throughput (inputs in
-HBM, CUDA events on the stream the kernels run on); `e2e` is the same metric
-through the public C ABI with host buffers (pinned host -> device copy of the
-state, the step, device -> host copy of P and S, every step). `--impl
-reference` times the reference CPU algorithm (the oracle: a bit-exact
-restatement of the reference's cpu.cpp) on the host cores instead.
+HBM, CUDA events on the stream the kernels run on, CUDA graphs for
+ensembles); `e2e` is the same metric through the public C ABI with host
+buffers (pinned host -> device state, the step, device -> host P and S,
+every step). `--impl reference` times the reference CPU algorithm (the
+oracle: a bit-exact restatement of the reference's cpu.cpp) on the host
+cores instead.
 """
 from __future__ import annotations
 
 import argparse
-import ctypes
 import json
 import os
+import pathlib
 import statistics
 import subprocess
 import sys
 import tempfile
-import threading
 import time
-import pathlib
 
 import numpy as np
 
@@ -59,12 +64,14 @@ class ClockSampler:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
                                           "--format=csv,noheader,nounits", "-lms", "200"],
                                          stdout=self.f, stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
         except (OSError, FileNotFoundError):
             self.proc = None
         return self
 
     def __exit__(self, *a):
         if self.proc:
+            time.sleep(0.25)
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
@@ -97,10 +104,9 @@ def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if world > 1:
-        import torch.distributed as dist
         import torch
-        backend = "nccl" if torch.cuda.is_available() else "gloo"
-        dist.init_process_group(backend)
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
         if torch.cuda.is_available():
             torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     return rank, world
@@ -124,46 +130,98 @@ def barrier(world):
 
 # ------------------------------------------------------------------ workloads
 
-PRECISIONS = {"f64": ("GBF_PREC_F64", "plain FP64"),
-              "split": ("GBF_PREC_SPLIT", "FP32 state and fluxes, FP64 masses and residual"),
-              "splitdf": ("GBF_PREC_SPLIT_DF", "FP32 state and fluxes, FP32-pair masses and residual")}
+PRECISIONS = {"f64": ("GBF_PREC_F64", "plain FP64", "f64"),
+              "split": ("GBF_PREC_SPLIT", "FP32 state and fluxes, FP64 masses and residual", "f32+f64"),
+              "splitdf": ("GBF_PREC_SPLIT_DF", "FP32 state and fluxes, FP32-pair masses and residual",
+                          "f32+f32x2")}
 
 
-def make_workload(pkg, lib, name, cube):
+def make_members(pkg, lib, cfg, cube):
     from importlib import import_module
     wl = import_module(pkg.__name__ + ".workloads")
-    cfg, _, p = name.partition("_")
-    if p not in PRECISIONS:
-        raise SystemExit(f"unknown workload {name}")
-    prec = getattr(pkg.abi, PRECISIONS[p][0])
+    if cfg == "config0":
+        return [wl.config0(lib)], "config 0: 40^3 homogeneous single grid", False
     if cfg == "config1":
         mem = wl.config1(lib, n=cube or 256)
-        desc = f"config 1: {mem.model.nx}^3 heterogeneous single grid"
-    elif cfg == "config0":
-        mem = wl.config0(lib)
-        desc = "config 0: 40^3 homogeneous"
-    elif cfg == "config2":
-        mem = wl.config2(lib)
-        desc = "config 2: 512x512x256 heterogeneous single grid (sigma_lnK 1.5)"
-    else:
-        raise SystemExit(f"unknown workload {name}")
-    return {"members": [mem], "precision": prec, "desc": f"{desc}, {PRECISIONS[p][1]}"}
+        return [mem], f"config 1: {mem.model.nx}^3 heterogeneous single grid", False
+    if cfg == "config2":
+        return [wl.config2(lib)], "config 2: 512x512x256 heterogeneous single grid (sigma_lnK 1.5)", False
+    if cfg == "config3":
+        return wl.config3(lib), "config 3: 96 realizations, edges in {64,96,128,160}", True
+    if cfg == "config4":
+        return wl.config4(lib), "config 4: 256 realizations, edges 48..128 step 16, anisotropic", True
+    raise SystemExit(f"unknown configuration {cfg}")
 
 
-# Algorithmic bytes per cell of each kernel (compulsory DRAM traffic of its
-# inputs and outputs).
+class Runner:
+    """One domain or one ensemble behind the same calls."""
+
+    def __init__(self, pkg, members, precision, ensemble, mass_cap):
+        from importlib import import_module
+        self.abi = pkg.abi
+        self.members = members
+        self.ensemble = ensemble
+        if ensemble:
+            E = import_module(pkg.__name__ + ".ensemble").Ensemble
+            self.obj = E(members, precision=precision)
+        else:
+            D = import_module(pkg.__name__ + ".domain").Domain
+            m = members[0]
+            self.obj = D(m.model, m.media, m.K, m.phi, precision=precision)
+        self.obj.set_outputs(self.abi.GBF_OUT_MASS, mass_cap)
+
+    def upload_initial(self):
+        if self.ensemble:
+            self.obj.upload_initial()
+        else:
+            self.obj.upload(*self.members[0].initial_state())
+
+    def upload(self, r, P, S):
+        if self.ensemble:
+            self.obj.upload(r, P, S)
+        else:
+            self.obj.upload(P, S)
+
+    def download(self, r, field, out=None):
+        return self.obj.download(r, field, out) if self.ensemble else self.obj.download(field, out)
+
+    def __getattr__(self, name):
+        return getattr(self.obj, name)
+
+    @property
+    def cells(self):
+        return sum(m.ncells for m in self.members)
+
+    @property
+    def interior_cells(self):
+        return sum((m.model.nx - 2) * (m.model.ny - 2) * (m.model.nz - 2) for m in self.members)
+
+
+# Algorithmic bytes per interior (or every) cell of each kernel: the
+# compulsory DRAM traffic of its inputs and outputs.
 ALGO_BYTES = {
-    "f64_props": 60.0,        # read P, S (16), K (4) = 20; write L1, L2, ro1, ro2, lnSe (40)
-    "f64_flux_newton": 76.0,  # read P, S, L1, L2, ro1, ro2, lnSe (56), phi (4); write P, S (16)
-    "split_step": 56.0,       # read dP, S, K, phi (16), M1, M2 (16); write dP, S (8), M1, M2 (16)
+    "f64_props": (60.0, "all"),             # read P, S, K (20); write L1, L2, ro1, ro2, lnSe (40)
+    "ensemble_f64_props": (60.0, "all"),
+    "f64_flux_newton": (76.0, "interior"),  # read P, S, L1, L2, ro1, ro2, lnSe (56), phi (4); write P, S (16)
+    "ensemble_f64_flux_newton": (76.0, "interior"),
+    "split_step": (56.0, "interior"),       # read dP, S, K, phi (16), M1, M2 (16); write dP, S (8), M1, M2 (16)
+    "ensemble_step": (56.0, "interior"),
 }
-KERNEL_CELLS = {"f64_props": "all", "f64_flux_newton": "interior", "split_step": "interior"}
 
 
-def cells_of(m, which):
-    if which == "all":
-        return m.nx * m.ny * m.nz
-    return (m.nx - 2) * (m.ny - 2) * (m.nz - 2)
+def timed(runner, steps, stream, world, clocks=None):
+    """Device time of `steps` steps on the runner's stream (CUDA events)."""
+    import torch
+    barrier(world)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    runner.step(steps)
+    e1.record(stream)
+    e1.synchronize()
+    torch.cuda.synchronize()
+    barrier(world)
+    return dist_max(e0.elapsed_time(e1), world)
 
 
 def cpu_baseline(O, abi, members, budget_s=12.0, threads=None):
@@ -173,7 +231,6 @@ def cpu_baseline(O, abi, members, budget_s=12.0, threads=None):
     threads = threads or os.cpu_count()
     os.environ["OMP_NUM_THREADS"] = str(threads)
     done_cells = 0
-    steps = 0
     t0 = time.perf_counter()
     sample = []
     for mem in sorted(members, key=lambda x: -x.ncells):
@@ -188,14 +245,13 @@ def cpu_baseline(O, abi, members, budget_s=12.0, threads=None):
             n += 1
             if n >= 1000:
                 break
-        steps += n
         sample.append(f"{mem.model.nx}x{mem.model.ny}x{mem.model.nz} x {n} steps")
         if time.perf_counter() - t0 >= budget_s:
             break
     dt = time.perf_counter() - t0
     return {"value": done_cells / dt, "unit": "cell-steps/s", "cores": threads, "kind": "port",
-            "sample": "; ".join(sample) + f" ({dt:.1f} s, oracle = bit-exact restatement of cpu.cpp, "
-                                          f"OpenMP over i, 7 Newton iterations)"}
+            "sample": "; ".join(sample) + f" ({dt:.1f} s; oracle = bit-exact restatement of the reference "
+                                          f"cpu.cpp, OpenMP over i, 7 Newton iterations)"}
 
 
 def run_ours(args, rank, world):
@@ -203,96 +259,114 @@ def run_ours(args, rank, world):
     pkg = ge.load_package()
     lib = pkg.load_library()
     abi = pkg.abi
-    from importlib import import_module
-    Domain = import_module(pkg.__name__ + ".domain").Domain
     torch.cuda.init()
-    wl = make_workload(pkg, lib, args.workload, args.cube)
-    mems = wl["members"]
-    assert len(mems) == 1, "single-grid workloads only in this version"
-    mem = mems[0]
-    m = mem.model
-    dom = Domain(m, mem.media, mem.K, mem.phi, precision=wl["precision"])
-    dom.set_outputs(abi.GBF_OUT_MASS, args.warmup + args.steps + 8)
-    P0, S0 = mem.initial_state()
-    dom.upload(P0, S0)
+    cfg, _, p = args.workload.partition("_")
+    if p not in PRECISIONS:
+        raise SystemExit(f"unknown precision in {args.workload}")
+    members, desc, ensemble = make_members(pkg, lib, cfg, args.cube)
+    prec = getattr(abi, PRECISIONS[p][0])
     stream = torch.cuda.Stream()
-    dom.set_stream(stream.cuda_stream)
-    dom.step(args.warmup)
-    dom.sync()
-    barrier(world)
-    torch.cuda.synchronize()
-    dom.set_timing(True)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    cap = args.warmup + 2 * args.steps + 8
+    run = Runner(pkg, members, prec, ensemble, cap)
+    run.set_stream(stream.cuda_stream)
+    tuning = None
+    if ensemble and prec != abi.GBF_PREC_F64 and not args.no_autotune:
+        run.upload_initial()
+        tuning = run.autotune(2)
+    run.upload_initial()
+    run.step(args.warmup)
+    run.sync()
+    cells = run.cells
     with ClockSampler(torch.cuda.current_device()) as clk:
-        e0.record(stream)
-        dom.step(args.steps)
-        e1.record(stream)
-        e1.synchronize()
-    torch.cuda.synchronize()
-    barrier(world)
-    ms = e0.elapsed_time(e1)
-    ktimes = dom.kernel_times()
-    dom.set_timing(False)
-    status = dom.status()
-    ms_max = dist_max(ms, world)
-    cells = mem.ncells
-    value = world * cells * args.steps / (ms_max / 1e3)
-
-    # e2e through the C ABI with pinned host buffers: H2D state, step, D2H P and S
-    Ph = torch.empty(m.shape, dtype=torch.float64, pin_memory=True).numpy()
-    Sh = torch.empty(m.shape, dtype=torch.float64, pin_memory=True).numpy()
-    Ph[...] = dom.download("P1")
-    Sh[...] = dom.download("S2")
-    e2e_steps = max(3, min(args.steps, 20))
-    dom.upload(Ph, Sh)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        dom.upload(Ph, Sh)
-        dom.step(1)
-        dom.download("P1", Ph)
-        dom.download("S2", Sh)
-    e2e_s = dist_max(time.perf_counter() - t0, world)
-    e2e = {"value": world * cells * e2e_steps / e2e_s, "unit": "cell-steps/s",
-           "h2d_bytes_per_step": 2 * cells * 8, "d2h_bytes_per_step": 2 * cells * 8,
-           "api": "gbf_domain_upload + gbf_domain_step(1) + gbf_domain_download(P1, S2)"}
+        ms = timed(run, args.steps, stream, world)            # value: graphs, no per-kernel events
+        run.set_timing(True)                                   # roofline: the same steps with kernel events
+        ms_k = timed(run, args.steps, stream, world)
+    ktimes = run.kernel_times()
+    run.set_timing(False)
+    status = run.status()
+    value = world * cells * args.steps / (ms / 1e3)
 
     # roofline of the dominant kernel
     hbm, peak_kind = peaks()
-    dom_k = max(ktimes.items(), key=lambda kv: kv[1][0])
-    kname, (kms, klaunch) = dom_k
+    kname, (kms, klaunch) = max(ktimes.items(), key=lambda kv: kv[1][0])
     per_launch_s = kms / 1e3 / max(klaunch, 1)
-    algo = ALGO_BYTES.get(kname, 0.0) * cells_of(m, KERNEL_CELLS.get(kname, "all"))
+    bpc, which = ALGO_BYTES.get(kname, (0.0, "all"))
+    algo = bpc * (run.interior_cells if which == "interior" else cells)
     achieved = algo / per_launch_s / 1e9 if per_launch_s > 0 else 0.0
     traffic = None
     tfile = ROOT / "profiles" / "traffic.json"
     if tfile.exists():
-        tj = json.loads(tfile.read_text())
-        ent = tj.get(args.workload, {}).get(kname)
+        ent = json.loads(tfile.read_text()).get(args.workload, {}).get(kname)
         if ent:
             traffic = ent["bytes_per_launch"]
     roof = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": hbm, "unit": "GB/s",
             "frac": achieved / hbm, "peak_source": peak_kind, "traffic": traffic,
-            "algorithmic_bytes_per_launch": algo, "ms_per_launch": per_launch_s * 1e3,
-            "kernel_times_ms": {k: {"total_ms": v[0], "launches": v[1]} for k, v in ktimes.items()}}
-    mass = dom.mass_history(args.warmup + args.steps)
+            "algorithmic_bytes_per_launch": algo, "bytes_per_cell": bpc, "ms_per_launch": per_launch_s * 1e3,
+            "kernel_times_ms": {k: {"total_ms": v[0], "launches": v[1]} for k, v in ktimes.items()},
+            "ms_per_step_with_kernel_events": ms_k / args.steps}
+
+    # e2e through the C ABI with pinned host buffers: H2D state, one step, D2H P and S
+    hostP = [torch.empty(m.model.shape, dtype=torch.float64, pin_memory=True).numpy() for m in members]
+    hostS = [torch.empty(m.model.shape, dtype=torch.float64, pin_memory=True).numpy() for m in members]
+    for r in range(len(members)):
+        run.download(r, "P1", hostP[r])
+        run.download(r, "S2", hostS[r])
+    e2e_steps = max(2, min(args.steps, 5 if ensemble else 20))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        for r in range(len(members)):
+            run.upload(r, hostP[r], hostS[r])
+        run.step(1)
+        for r in range(len(members)):
+            run.download(r, "P1", hostP[r])
+            run.download(r, "S2", hostS[r])
+    e2e_s = dist_max(time.perf_counter() - t0, world)
+    api = ("gbf_ensemble_upload (every member) + gbf_ensemble_step(1) + gbf_ensemble_download(P1, S2)"
+           if ensemble else "gbf_domain_upload + gbf_domain_step(1) + gbf_domain_download(P1, S2)")
+    e2e = {"value": world * cells * e2e_steps / e2e_s, "unit": "cell-steps/s",
+           "h2d_bytes_per_step": 2 * cells * 8, "d2h_bytes_per_step": 2 * cells * 8, "api": api}
+
     out = {"metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": world, "steps": args.steps,
-           "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None,
-           "dtype": {abi.GBF_PREC_F64: "f64", abi.GBF_PREC_SPLIT: "f32+f64",
-                     abi.GBF_PREC_SPLIT_DF: "f32+f32x2"}[wl["precision"]],
+           "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": PRECISIONS[p][2],
            "data": "synthetic (seeded fields with the configuration's shapes and statistics)",
-           "config": {"workload": args.workload, "desc": wl["desc"], "cells": cells,
-                      "grid": [m.nx, m.ny, m.nz], "dt_used": m.dt,
-                      "l2": "inputs larger than L2 (state+fields %.1f GB > 129 MB)" % (cells * 100 / 1e9),
-                      "newton_tol": m.newton_tol},
-           "clocks": clk.summary(), "e2e": e2e, "gpu_launches": dom.launches_per_step * args.steps,
-           "roofline": roof, "status": lib.gbf_status_string(status).decode(),
-           "phase_mass_last": mass[-1].tolist() if len(mass) else None}
+           "config": {"workload": args.workload, "desc": f"{desc}, {PRECISIONS[p][1]}", "cells": cells,
+                      "members": len(members), "dt_used_range": [min(m.model.dt for m in members),
+                                                                 max(m.model.dt for m in members)],
+                      "l2": f"inputs larger than L2 (state and fields {cells * 40 / 1e9:.1f} GB > 129 MB)",
+                      "newton": "FP64: converge-and-exit (tol 1e-11, max 7); split: 2 increment iterations",
+                      "tuning": tuning, "graphs": ensemble},
+           "clocks": clk.summary(), "e2e": e2e, "gpu_launches": run.launches_per_step * args.steps,
+           "roofline": roof, "status": lib.gbf_status_string(status).decode()}
+    run.close()
+    del run
+
+    if ensemble and not args.no_compare and rank == 0:
+        comp = {}
+        for q in ("f64", "split", "splitdf"):
+            if q == p:
+                continue
+            r2 = Runner(pkg, members, getattr(abi, PRECISIONS[q][0]), True, cap)
+            r2.set_stream(stream.cuda_stream)
+            if q != "f64" and not args.no_autotune:
+                r2.upload_initial()
+                r2.autotune(2)
+            r2.upload_initial()
+            r2.step(args.warmup)
+            r2.sync()
+            nst = min(args.steps, 10) if q == "f64" else args.steps
+            ms2 = timed(r2, nst, stream, 1)
+            comp[q] = {"value": cells * nst / (ms2 / 1e3), "steps": nst, "ms_per_step": ms2 / nst,
+                       "dtype": PRECISIONS[q][2]}
+            r2.close()
+            del r2
+        out["same_members"] = comp
+        if "f64" in comp:
+            out["split_batched_over_fp64_batched"] = value / comp["f64"]["value"]
     if rank == 0 and not args.no_cpu_baseline:
         O = ge.load_oracle_module()
-        out["cpu_baseline"] = cpu_baseline(O, abi, mems, budget_s=args.cpu_budget)
-    dom.close()
+        out["cpu_baseline"] = cpu_baseline(O, abi, members, budget_s=args.cpu_budget)
     return out
 
 
@@ -303,30 +377,35 @@ def run_reference(args, rank, world):
     pkg = ge.load_package()
     lib = pkg.load_library()
     O = ge.load_oracle_module()
-    wl = make_workload(pkg, lib, args.workload, args.cube)
-    mems = wl["members"]
+    cfg, _, p = args.workload.partition("_")
+    members, desc, _ = make_members(pkg, lib, cfg, args.cube)
     threads = os.cpu_count()
     os.environ["OMP_NUM_THREADS"] = str(threads)
     orc = O.Oracle(pkg.abi)
+    # bounded sample per step: whole members, largest first, until ~budget
+    budget = max(1.0, 120.0 / max(1, args.steps + args.warmup))
     states = []
-    for mem in mems:
+
+    def state(mem):
         st = O.State(mem.model, mem.media, mem.K, mem.phi)
         P, S = mem.initial_state()
         st["P1"][...] = P
         st["S2"][...] = S
-        states.append(st)
-    # bounded sample per step: whole members until ~budget per step
-    budget = max(1.0, 120.0 / max(1, args.steps + args.warmup))
+        return st
+
+    order = sorted(members, key=lambda x: -x.ncells)
 
     def one_step():
         t0 = time.perf_counter()
-        cells = 0
-        for st in states:
-            orc.step(st, 1)
-            cells += st.model.nx * st.model.ny * st.model.nz
+        c = 0
+        for q, mem in enumerate(order):
+            if q >= len(states):
+                states.append(state(mem))
+            orc.step(states[q], 1)
+            c += mem.ncells
             if time.perf_counter() - t0 > budget:
                 break
-        return cells, time.perf_counter() - t0
+        return c, time.perf_counter() - t0
 
     for _ in range(args.warmup):
         one_step()
@@ -336,13 +415,13 @@ def run_reference(args, rank, world):
         tot_c += c
         tot_t += t
     v = tot_c / tot_t
-    sample = f"{len(states)} member(s), whole steps bounded to ~{budget:.1f} s each"
+    sample = f"{len(states)} of {len(members)} member(s) per step, each step bounded to ~{budget:.1f} s"
     return {"metric": METRIC, "impl": "reference", "value": v, "unit": "cell-steps/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded fields with the configuration's shapes and statistics)",
-            "config": {"workload": args.workload, "desc": wl["desc"] + " (CPU oracle)",
-                       "cells": sum(s.model.nx * s.model.ny * s.model.nz for s in states)},
+            "config": {"workload": args.workload, "desc": desc + " (reference CPU algorithm, FP64)",
+                       "cells": sum(m.ncells for m in members)},
             "e2e": {"value": v, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "cpu_baseline": {"value": v, "unit": "cell-steps/s", "cores": threads, "kind": "port",
                              "sample": sample + "; oracle = bit-exact restatement of the reference cpu.cpp "
@@ -352,13 +431,15 @@ def run_reference(args, rank, world):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="config1_f64")
-    ap.add_argument("--cube", type=int, default=0, help="override the grid edge (profiling runs)")
+    ap.add_argument("--workload", default="config4_splitdf")
+    ap.add_argument("--cube", type=int, default=0, help="override the grid edge of config1 (profiling runs)")
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-compare", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours" and not args.cube:
         args.warmup = 3

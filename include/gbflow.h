@@ -178,6 +178,44 @@ int gbf_domain_kernel_times(gbf_domain* d, double* ms, int* launches, int nkinds
 int gbf_kernel_kinds(void);
 const char* gbf_kernel_name(int kind);
 
+/* ----------------------------------------------------------- ensembles ----
+ * Independent realizations of uneven sizes and parameters, advanced
+ * together: every gbf_ensemble_step moves every member by one of its own
+ * time steps. Split precisions run one persistent kernel over a packed tile
+ * work list of all members; FP64 runs its two passes over packed chunk
+ * lists. Each step is a CUDA graph. `host_cells` may be NULL or an array of
+ * n entries. Uploads and downloads are per member (FP64 host or device
+ * arrays of nx*ny*nz doubles).
+ */
+typedef struct gbf_ensemble gbf_ensemble;
+int gbf_ensemble_create(int n, const gbf_model* models, const gbf_cells* host_cells, int precision,
+                        gbf_ensemble** out);
+int gbf_ensemble_destroy(gbf_ensemble* e);
+int gbf_ensemble_size(gbf_ensemble* e);
+long long gbf_ensemble_cells(gbf_ensemble* e);
+long long gbf_ensemble_interior_cells(gbf_ensemble* e);
+int gbf_ensemble_set_stream(gbf_ensemble* e, void* stream);
+/* GBF_OUT_MASS only: per-member phase masses every step. */
+int gbf_ensemble_set_outputs(gbf_ensemble* e, int out_flags, int mass_history_capacity);
+int gbf_ensemble_upload(gbf_ensemble* e, int member, const double* P1, const double* S2);
+int gbf_ensemble_step(gbf_ensemble* e, int nsteps);
+int gbf_ensemble_download(gbf_ensemble* e, int member, int field, double* host);
+/* [step][member][2] since the last upload. */
+int gbf_ensemble_mass_history(gbf_ensemble* e, double* host, int max_steps, int* nsteps_out);
+int gbf_ensemble_status(gbf_ensemble* e);
+int gbf_ensemble_sync(gbf_ensemble* e);
+int gbf_ensemble_set_timing(gbf_ensemble* e, int on);
+int gbf_ensemble_kernel_times(gbf_ensemble* e, double* ms, int* launches, int nkinds);
+int gbf_ensemble_launches_per_step(gbf_ensemble* e);
+/* Tuning: tile shape (0: 32x8, 1: 64x4, 2: 32x4; -1 keeps it) and the k planes
+   per tile pass ("fusion depth") of members whose nx == edge (0: whole column).
+   gbf_ensemble_autotune times `trial_steps` steps per candidate and keeps the
+   fastest; it advances the state, so upload the initial state afterwards. */
+int gbf_ensemble_set_tuning(gbf_ensemble* e, int shape, int edge, int kchunk);
+int gbf_ensemble_get_tuning(gbf_ensemble* e, int* shape, int* edges, int* kchunks, int max_entries);
+const char* gbf_ensemble_shape_name(int shape);
+int gbf_ensemble_autotune(gbf_ensemble* e, int trial_steps);
+
 #ifdef __cplusplus
 }
 #endif

@@ -148,6 +148,26 @@ def _declare(lib) -> None:
         "gbf_domain_kernel_times": (c_int, [c_void_p, c_void_p, c_void_p, c_int]),
         "gbf_kernel_kinds": (c_int, []),
         "gbf_kernel_name": (ctypes.c_char_p, [c_int]),
+        "gbf_ensemble_create": (c_int, [c_int, PM, PC, c_int, ctypes.POINTER(c_void_p)]),
+        "gbf_ensemble_destroy": (c_int, [c_void_p]),
+        "gbf_ensemble_size": (c_int, [c_void_p]),
+        "gbf_ensemble_cells": (ctypes.c_longlong, [c_void_p]),
+        "gbf_ensemble_interior_cells": (ctypes.c_longlong, [c_void_p]),
+        "gbf_ensemble_set_stream": (c_int, [c_void_p, c_void_p]),
+        "gbf_ensemble_set_outputs": (c_int, [c_void_p, c_int, c_int]),
+        "gbf_ensemble_upload": (c_int, [c_void_p, c_int, c_void_p, c_void_p]),
+        "gbf_ensemble_step": (c_int, [c_void_p, c_int]),
+        "gbf_ensemble_download": (c_int, [c_void_p, c_int, c_int, c_void_p]),
+        "gbf_ensemble_mass_history": (c_int, [c_void_p, c_void_p, c_int, ctypes.POINTER(c_int)]),
+        "gbf_ensemble_status": (c_int, [c_void_p]),
+        "gbf_ensemble_sync": (c_int, [c_void_p]),
+        "gbf_ensemble_set_timing": (c_int, [c_void_p, c_int]),
+        "gbf_ensemble_kernel_times": (c_int, [c_void_p, c_void_p, c_void_p, c_int]),
+        "gbf_ensemble_launches_per_step": (c_int, [c_void_p]),
+        "gbf_ensemble_set_tuning": (c_int, [c_void_p, c_int, c_int, c_int]),
+        "gbf_ensemble_get_tuning": (c_int, [c_void_p, ctypes.POINTER(c_int), c_void_p, c_void_p, c_int]),
+        "gbf_ensemble_shape_name": (ctypes.c_char_p, [c_int]),
+        "gbf_ensemble_autotune": (c_int, [c_void_p, c_int]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

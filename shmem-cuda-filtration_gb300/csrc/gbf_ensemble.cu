@@ -1,0 +1,717 @@
+// gbf_ensemble.cu — batched ensembles: independent realizations of uneven
+// grid sizes advanced together, one time step of every member per step.
+//
+// Split precision: one persistent kernel over a packed tile work list
+// (member, x-tile, y-tile, k-range) of all members; CTAs take tiles from an
+// atomic counter (dynamic balance of uneven members) and run the z-marching
+// tile of gbf_split_tile.cuh with the member's constants copied to shared
+// memory. Plain FP64: the two passes of gbf_f64_cell.cuh over packed chunk
+// lists of all members' cells. Then one face pass over all members'
+// boundary cells and one per-member phase-mass reduction. A step is a CUDA
+// graph (counter reset, step, faces, masses), captured once per buffer parity.
+//
+// Tuning: the tile shape (one of three compiled shapes) and the k-range per
+// CTA ("fusion depth": planes marched per tile pass) per member edge are
+// picked by gbf_ensemble_autotune from timed trial steps.
+#include <string.h>
+
+#include <algorithm>
+#include <map>
+#include <vector>
+
+#include "gbf_f64_cell.cuh"
+#include "gbf_split_tile.cuh"
+
+namespace {
+
+struct EnsMember {
+  gbf_model m;
+  GbfDerived d;
+  GbfSplitConsts C;
+  gbf_cells cells;
+  double* P[2];
+  double* S[2];
+  float* dPf[2];
+  float* Sf[2];
+  double *M1, *M2;
+  double *L1, *L2, *ro1, *ro2, *lnSe;
+  int part_begin, part_end;  // this member's slots in the partial-sum array
+};
+
+struct EnsChunk {
+  int member;
+  unsigned begin, end;
+};
+
+enum { kShape32x8 = 0, kShape64x4 = 1, kShape32x4 = 2, kShapes = 3 };
+const int kShapeTX[kShapes] = {32, 64, 32}, kShapeTY[kShapes] = {8, 4, 4};
+constexpr int kChunkCells = 16384, kBoundaryChunk = 4096, kThreads = 256;
+
+// ------------------------------------------------------------ split kernels
+
+template <bool DF, int TX, int TY>
+__global__ void __launch_bounds__(TX * TY, 1024 / (TX * TY)) k_ens_split_step(const EnsMember* __restrict__ mem,
+                                                                             const int4* __restrict__ tiles,
+                                                                             int ntiles, int cur,
+                                                                             unsigned* counter, double* partials,
+                                                                             unsigned* status) {
+  __shared__ GbfSplitPlaneT<TX, TY> pl[2];
+  __shared__ GbfSplitConsts Cs;
+  __shared__ GbfSplitGrid Gs;
+  __shared__ int s_tile;
+  constexpr int NT = TX * TY;
+  for (;;) {
+    if (threadIdx.x == 0) s_tile = (int)atomicAdd(counter, 1u);
+    __syncthreads();
+    const int t = s_tile;
+    if (t >= ntiles) break;
+    const int4 tl = tiles[t];
+    const EnsMember* me = mem + tl.x;
+    {  // member constants to shared memory
+      const int* src = reinterpret_cast<const int*>(&me->C);
+      int* dst = reinterpret_cast<int*>(&Cs);
+      for (int q = threadIdx.x; q < (int)(sizeof(GbfSplitConsts) / sizeof(int)); q += NT) dst[q] = src[q];
+    }
+    if (threadIdx.x == 0) {
+      Gs.dP = me->dPf[cur];
+      Gs.S = me->Sf[cur];
+      Gs.dPn = me->dPf[cur ^ 1];
+      Gs.Sn = me->Sf[cur ^ 1];
+      Gs.K = me->cells.K;
+      Gs.phi = me->cells.phi;
+      Gs.media = me->cells.media;
+      Gs.M1 = me->M1;
+      Gs.M2 = me->M2;
+      Gs.mass_partials = partials;
+      Gs.status = status;
+    }
+    __syncthreads();
+    GbfSplitAcc<DF> acc;
+    split_tile<DF, TX, TY>(Cs, Gs, tl.y, tl.z, tl.w & 0xffff, tl.w >> 16, pl, acc);
+    if (acc.bad) atomicOr(status, GBF_DEV_NONFINITE);
+    if (partials) split_block_mass<DF, NT>(acc, Cs.V, partials + 2 * t);
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_ens_split_boundary(const EnsMember* __restrict__ mem,
+                                                                 const EnsChunk* __restrict__ chunks, int cur) {
+  const EnsChunk ch = chunks[blockIdx.x];
+  const EnsMember* me = mem + ch.member;
+  const gbf_model& m = me->m;
+  const GbfGeo g = gbf_geo(m);
+  const float* dP = me->dPf[cur];
+  const float* S = me->Sf[cur];
+  float* dPn = me->dPf[cur ^ 1];
+  float* Sn = me->Sf[cur ^ 1];
+  const float H = me->C.H;
+  for (unsigned t = ch.begin + threadIdx.x; t < ch.end; t += blockDim.x) {
+    int i, j, k;
+    gbf_boundary_cell(g, t, i, j, k);
+    const size_t c = gbf_idx(g, i, j, k);
+    Sn[c] = gbf_sweep_S<float>(m, g, Sn, S, i, j, k);
+    dPn[c] = gbf_split_sweep_dP(m, g, dPn, dP, i, j, k, H);
+  }
+}
+
+// ------------------------------------------------------------- FP64 kernels
+
+__device__ __forceinline__ GbfF64Step ens_f64_step(const EnsMember& me, int cur) {
+  GbfF64Step s = {};
+  s.P = me.P[cur];
+  s.S = me.S[cur];
+  s.Pn = me.P[cur ^ 1];
+  s.Sn = me.S[cur ^ 1];
+  s.L1 = me.L1; s.L2 = me.L2; s.ro1 = me.ro1; s.ro2 = me.ro2; s.lnSe = me.lnSe;
+  return s;
+}
+
+__global__ void __launch_bounds__(kThreads) k_ens_f64_props(const EnsMember* __restrict__ mem,
+                                                            const EnsChunk* __restrict__ chunks, int cur) {
+  __shared__ EnsMember me;
+  const EnsChunk ch = chunks[blockIdx.x];
+  {
+    const int* src = reinterpret_cast<const int*>(mem + ch.member);
+    int* dst = reinterpret_cast<int*>(&me);
+    for (int q = threadIdx.x; q < (int)(sizeof(EnsMember) / sizeof(int)); q += blockDim.x) dst[q] = src[q];
+  }
+  __syncthreads();
+  const GbfGeo g = gbf_geo(me.m);
+  const GbfF64Step s = ens_f64_step(me, cur);
+  for (unsigned c = ch.begin + threadIdx.x; c < ch.end; c += blockDim.x) gbf_f64_props_cell(me.m, me.d, me.cells, s, 0, g, c);
+}
+
+__global__ void __launch_bounds__(kThreads) k_ens_f64_flux_newton(const EnsMember* __restrict__ mem,
+                                                                  const EnsChunk* __restrict__ chunks, int cur,
+                                                                  double* partials, unsigned* status) {
+  __shared__ EnsMember me;
+  const EnsChunk ch = chunks[blockIdx.x];
+  {
+    const int* src = reinterpret_cast<const int*>(mem + ch.member);
+    int* dst = reinterpret_cast<int*>(&me);
+    for (int q = threadIdx.x; q < (int)(sizeof(EnsMember) / sizeof(int)); q += blockDim.x) dst[q] = src[q];
+  }
+  __syncthreads();
+  const GbfGeo g = gbf_geo(me.m);
+  const GbfF64Step s = ens_f64_step(me, cur);
+  const unsigned ix = g.nx - 2, iy = g.ny - 2;
+  double m1 = 0., m2 = 0.;
+  unsigned bad = 0;
+  for (unsigned t = ch.begin + threadIdx.x; t < ch.end; t += blockDim.x) {
+    const int i = 1 + (int)(t % ix), j = 1 + (int)((t / ix) % iy), k = 1 + (int)(t / (ix * iy));
+    gbf_f64_flux_newton_cell(me.m, me.d, me.cells, s, g, i, j, k, m1, m2, bad);
+  }
+  if (bad) atomicOr(status, GBF_DEV_NONFINITE);
+  if (partials) gbf_block_sum2<kThreads>(m1, m2, me.d.V, partials + 2 * blockIdx.x);
+}
+
+__global__ void __launch_bounds__(kThreads) k_ens_f64_boundary(const EnsMember* __restrict__ mem,
+                                                               const EnsChunk* __restrict__ chunks, int cur) {
+  const EnsChunk ch = chunks[blockIdx.x];
+  const EnsMember& me = mem[ch.member];
+  const GbfGeo g = gbf_geo(me.m);
+  const GbfF64Step s = ens_f64_step(me, cur);
+  for (unsigned t = ch.begin + threadIdx.x; t < ch.end; t += blockDim.x) gbf_f64_boundary_cell(me.m, s, g, t);
+}
+
+// Per-member phase masses of this step: one block per member sums its
+// partials in a fixed order into hist[step][member][2] (step from *count).
+__global__ void k_ens_mass_tail(const EnsMember* __restrict__ mem, const double* partials, double* hist,
+                                unsigned* count, int nmem, int cap) {
+  __shared__ double red[2][256];
+  const EnsMember& me = mem[blockIdx.x];
+  double a = 0., b = 0.;
+  for (int q = me.part_begin + threadIdx.x; q < me.part_end; q += blockDim.x) {
+    a += partials[2 * q];
+    b += partials[2 * q + 1];
+  }
+  red[0][threadIdx.x] = a;
+  red[1][threadIdx.x] = b;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) { red[0][threadIdx.x] += red[0][threadIdx.x + o]; red[1][threadIdx.x] += red[1][threadIdx.x + o]; }
+    __syncthreads();
+  }
+  const unsigned step = *count;
+  if (threadIdx.x == 0 && step < (unsigned)cap) {
+    hist[2 * ((size_t)step * nmem + blockIdx.x)] = red[0][0];
+    hist[2 * ((size_t)step * nmem + blockIdx.x) + 1] = red[1][0];
+  }
+}
+__global__ void k_ens_count(unsigned* count) { atomicAdd(count, 1u); }
+
+__global__ void k_ens_split_to_f64(const gbf_model m, const float* dPf, const float* Sf, double* P, double* S) {
+  const GbfGeo g = gbf_geo(m);
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < g.n; c += (size_t)gridDim.x * blockDim.x) {
+    const int j = (int)((c / g.nx) % g.ny);
+    if (P) P[c] = gbf_p_hydrostatic(m, j) + (double)dPf[c];
+    if (S) S[c] = (double)Sf[c];
+  }
+}
+
+}  // namespace
+
+// ----------------------------------------------------------------- object
+
+struct gbf_ensemble {
+  int n = 0;
+  int precision = GBF_PREC_SPLIT_DF;
+  std::vector<gbf_model> models;
+  std::vector<EnsMember> h_mem;
+  EnsMember* d_mem = nullptr;
+  std::vector<int4> tiles;
+  int4* d_tiles = nullptr;
+  std::vector<EnsChunk> props, flux, bnd;
+  EnsChunk *d_props = nullptr, *d_flux = nullptr, *d_bnd = nullptr;
+  int nparts = 0;
+  double* d_partials = nullptr;
+  unsigned *d_counter = nullptr, *d_status = nullptr, *d_mass_count = nullptr;
+  double* d_mass_hist = nullptr;
+  int mass_cap = 0;
+  int out_flags = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int cur = 0;
+  int shape = kShape32x8;
+  std::map<int, int> kchunk_by_edge;  // fusion depth per member edge (0 = default rule)
+  int persistent_blocks = 0;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  GbfTimer timer;
+  std::vector<void*> owned;
+  long long steps = 0, cells = 0;
+  bool uploaded_all = false;
+};
+
+namespace {
+
+int ens_alloc(gbf_ensemble* e, void** p, size_t bytes) {
+  cudaError_t r = cudaMalloc(p, bytes ? bytes : 16);
+  if (r != cudaSuccess) {
+    *p = nullptr;
+    return gbf_cuda_check(r, "gbf_ensemble alloc");
+  }
+  e->owned.push_back(*p);
+  return GBF_OK;
+}
+
+void drop_graphs(gbf_ensemble* e) {
+  for (auto& g : e->graph)
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
+}
+
+int default_kchunk(const gbf_model& m) { return std::max(1, m.nz - 2); }
+
+int kchunk_for(const gbf_ensemble* e, const gbf_model& m) {
+  auto it = e->kchunk_by_edge.find(m.nx);
+  int kc = (it != e->kchunk_by_edge.end() && it->second > 0) ? it->second : default_kchunk(m);
+  return std::min(kc, m.nz - 2);
+}
+
+// Packed work lists of the current tuning.
+int build_lists(gbf_ensemble* e) {
+  e->tiles.clear();
+  e->props.clear();
+  e->flux.clear();
+  e->bnd.clear();
+  const bool split = e->precision != GBF_PREC_F64;
+  const int TX = kShapeTX[e->shape], TY = kShapeTY[e->shape];
+  for (int r = 0; r < e->n; r++) {
+    const gbf_model& m = e->models[r];
+    const GbfGeo g = gbf_geo(m);
+    EnsMember& me = e->h_mem[r];
+    if (split) {
+      me.part_begin = (int)e->tiles.size();
+      const int kc = kchunk_for(e, m);
+      for (int k0 = 1; k0 < m.nz - 1; k0 += kc)
+        for (int j0 = 1; j0 < m.ny - 1; j0 += TY)
+          for (int i0 = 1; i0 < m.nx - 1; i0 += TX) {
+            const int k1 = std::min(k0 + kc, m.nz - 1);
+            e->tiles.push_back(make_int4(r, i0, j0, k0 | (k1 << 16)));
+          }
+      me.part_end = (int)e->tiles.size();
+    } else {
+      for (unsigned b = 0; b < g.n; b += kChunkCells) e->props.push_back({r, b, (unsigned)std::min<size_t>(g.n, b + kChunkCells)});
+      const size_t nint = (size_t)(m.nx - 2) * (m.ny - 2) * (m.nz - 2);
+      me.part_begin = (int)e->flux.size();
+      for (unsigned b = 0; b < nint; b += kChunkCells) e->flux.push_back({r, b, (unsigned)std::min<size_t>(nint, b + kChunkCells)});
+      me.part_end = (int)e->flux.size();
+    }
+    const size_t nb = gbf_boundary_count(g);
+    for (unsigned b = 0; b < nb; b += kBoundaryChunk) e->bnd.push_back({r, b, (unsigned)std::min<size_t>(nb, b + kBoundaryChunk)});
+  }
+  // device copies (reallocated when they grow)
+  auto upload = [&](void** dptr, const void* src, size_t bytes) -> int {
+    if (*dptr) {
+      auto it = std::find(e->owned.begin(), e->owned.end(), *dptr);
+      if (it != e->owned.end()) e->owned.erase(it);
+      cudaFree(*dptr);
+      *dptr = nullptr;
+    }
+    if (int s = ens_alloc(e, dptr, bytes)) return s;
+    GBF_CUDA(cudaMemcpy(*dptr, src, bytes, cudaMemcpyHostToDevice));
+    return GBF_OK;
+  };
+  int s = GBF_OK;
+  if (split) {
+    s |= upload((void**)&e->d_tiles, e->tiles.data(), e->tiles.size() * sizeof(int4));
+    e->nparts = (int)e->tiles.size();
+  } else {
+    s |= upload((void**)&e->d_props, e->props.data(), e->props.size() * sizeof(EnsChunk));
+    s |= upload((void**)&e->d_flux, e->flux.data(), e->flux.size() * sizeof(EnsChunk));
+    e->nparts = (int)e->flux.size();
+  }
+  s |= upload((void**)&e->d_bnd, e->bnd.data(), e->bnd.size() * sizeof(EnsChunk));
+  s |= upload((void**)&e->d_partials, std::vector<double>(2 * (size_t)std::max(1, e->nparts), 0.0).data(),
+              2 * sizeof(double) * std::max(1, e->nparts));
+  s |= upload((void**)&e->d_mem, e->h_mem.data(), e->h_mem.size() * sizeof(EnsMember));
+  drop_graphs(e);
+  return s ? GBF_ERR_CUDA : GBF_OK;
+}
+
+template <bool DF, int TX, int TY>
+int launch_split_step_t(gbf_ensemble* e, double* partials, cudaStream_t st) {
+  auto kern = k_ens_split_step<DF, TX, TY>;
+  int per_sm = 0;
+  GBF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TX * TY, 0));
+  const int blocks = std::max(1, std::min((int)e->tiles.size(), per_sm * gbf_num_sms()));
+  e->persistent_blocks = blocks;
+  kern<<<blocks, TX * TY, 0, st>>>(e->d_mem, e->d_tiles, (int)e->tiles.size(), e->cur, e->d_counter, partials,
+                                    e->d_status);
+  return GBF_OK;
+}
+
+int launch_split_step(gbf_ensemble* e, double* partials, cudaStream_t st) {
+  const bool df = e->precision == GBF_PREC_SPLIT_DF;
+  switch (e->shape) {
+    case kShape64x4: return df ? launch_split_step_t<true, 64, 4>(e, partials, st) : launch_split_step_t<false, 64, 4>(e, partials, st);
+    case kShape32x4: return df ? launch_split_step_t<true, 32, 4>(e, partials, st) : launch_split_step_t<false, 32, 4>(e, partials, st);
+    default: return df ? launch_split_step_t<true, 32, 8>(e, partials, st) : launch_split_step_t<false, 32, 8>(e, partials, st);
+  }
+}
+
+// Enqueue one step on `st` (also used under stream capture).
+int enqueue_step(gbf_ensemble* e, cudaStream_t st) {
+  const bool mass = (e->out_flags & GBF_OUT_MASS) && e->d_mass_hist;
+  double* partials = mass ? e->d_partials : nullptr;
+  GbfTimer* tm = &e->timer;
+  cudaEvent_t ev;
+  if (e->precision != GBF_PREC_F64) {
+    GBF_CUDA(cudaMemsetAsync(e->d_counter, 0, sizeof(unsigned), st));
+    ev = gbf_timer_begin(tm, st);
+    if (int s = launch_split_step(e, partials, st)) return s;
+    gbf_timer_end(tm, GBF_K_ENS_STEP, ev, st);
+    ev = gbf_timer_begin(tm, st);
+    k_ens_split_boundary<<<(unsigned)e->bnd.size(), kThreads, 0, st>>>(e->d_mem, e->d_bnd, e->cur);
+    gbf_timer_end(tm, GBF_K_ENS_BOUNDARY, ev, st);
+  } else {
+    ev = gbf_timer_begin(tm, st);
+    k_ens_f64_props<<<(unsigned)e->props.size(), kThreads, 0, st>>>(e->d_mem, e->d_props, e->cur);
+    gbf_timer_end(tm, GBF_K_ENS_PROPS, ev, st);
+    ev = gbf_timer_begin(tm, st);
+    k_ens_f64_flux_newton<<<(unsigned)e->flux.size(), kThreads, 0, st>>>(e->d_mem, e->d_flux, e->cur, partials,
+                                                                         e->d_status);
+    gbf_timer_end(tm, GBF_K_ENS_FLUX_NEWTON, ev, st);
+    ev = gbf_timer_begin(tm, st);
+    k_ens_f64_boundary<<<(unsigned)e->bnd.size(), kThreads, 0, st>>>(e->d_mem, e->d_bnd, e->cur);
+    gbf_timer_end(tm, GBF_K_ENS_BOUNDARY, ev, st);
+  }
+  if (mass) {
+    ev = gbf_timer_begin(tm, st);
+    k_ens_mass_tail<<<e->n, 256, 0, st>>>(e->d_mem, e->d_partials, e->d_mass_hist, e->d_mass_count, e->n, e->mass_cap);
+    k_ens_count<<<1, 1, 0, st>>>(e->d_mass_count);
+    gbf_timer_end(tm, GBF_K_MASS_TAIL, ev, st);
+  }
+  cudaError_t err = cudaGetLastError();
+  return err == cudaSuccess ? GBF_OK : gbf_cuda_check(err, "gbf_ensemble step");
+}
+
+int capture_graph(gbf_ensemble* e, int parity) {
+  const int saved = e->cur;
+  e->cur = parity;
+  cudaGraph_t g = nullptr;
+  GBF_CUDA(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+  int s = enqueue_step(e, e->stream);
+  cudaError_t r = cudaStreamEndCapture(e->stream, &g);
+  e->cur = saved;
+  if (s) return s;
+  if (r != cudaSuccess) return gbf_cuda_check(r, "end capture");
+  r = cudaGraphInstantiate(&e->graph[parity], g, 0);
+  cudaGraphDestroy(g);
+  return r == cudaSuccess ? GBF_OK : gbf_cuda_check(r, "graph instantiate");
+}
+
+int ens_step(gbf_ensemble* e, int nsteps, bool use_graph) {
+  for (int q = 0; q < nsteps; q++) {
+    if (use_graph && !e->timer.on) {
+      if (!e->graph[e->cur])
+        if (int s = capture_graph(e, e->cur)) return s;
+      GBF_CUDA(cudaGraphLaunch(e->graph[e->cur], e->stream));
+    } else {
+      if (int s = enqueue_step(e, e->stream)) return s;
+    }
+    e->cur ^= 1;
+    e->steps++;
+  }
+  return GBF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gbf_ensemble_create(int n, const gbf_model* models, const gbf_cells* host_cells, int precision,
+                        gbf_ensemble** out) {
+  if (!out || n < 1 || !models) return gbf_fail(GBF_ERR_ARG, "gbf_ensemble_create");
+  *out = nullptr;
+  if (precision != GBF_PREC_F64 && precision != GBF_PREC_SPLIT && precision != GBF_PREC_SPLIT_DF)
+    return gbf_fail(GBF_ERR_ARG, "precision");
+  for (int r = 0; r < n; r++)
+    if (int s = gbf_model_validate(&models[r], host_cells ? &host_cells[r] : nullptr, 0)) return s;
+  gbf_ensemble* e = new gbf_ensemble();
+  e->n = n;
+  e->precision = precision;
+  e->models.assign(models, models + n);
+  e->h_mem.resize(n);
+  int s = GBF_OK;
+  if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess) s = gbf_fail(GBF_ERR_CUDA, "stream");
+  e->own_stream = true;
+  const bool split = precision != GBF_PREC_F64;
+  for (int r = 0; r < n && !s; r++) {
+    const gbf_model& m = models[r];
+    const size_t nc = gbf_geo(m).n;
+    e->cells += (long long)nc;
+    EnsMember& me = e->h_mem[r];
+    memset(&me, 0, sizeof(me));
+    me.m = m;
+    me.d = gbf_derive(m);
+    me.C = gbf_split_consts(m);
+    if (host_cells) {
+      const gbf_cells& hc = host_cells[r];
+      if (hc.media && !(s |= ens_alloc(e, (void**)&me.cells.media, nc * sizeof(int))))
+        cudaMemcpy((void*)me.cells.media, hc.media, nc * sizeof(int), cudaMemcpyHostToDevice);
+      if (hc.K && !(s |= ens_alloc(e, (void**)&me.cells.K, nc * sizeof(float))))
+        cudaMemcpy((void*)me.cells.K, hc.K, nc * sizeof(float), cudaMemcpyHostToDevice);
+      if (hc.phi && !(s |= ens_alloc(e, (void**)&me.cells.phi, nc * sizeof(float))))
+        cudaMemcpy((void*)me.cells.phi, hc.phi, nc * sizeof(float), cudaMemcpyHostToDevice);
+    }
+    if (split) {
+      for (int b = 0; b < 2; b++) {
+        s |= ens_alloc(e, (void**)&me.dPf[b], nc * sizeof(float));
+        s |= ens_alloc(e, (void**)&me.Sf[b], nc * sizeof(float));
+      }
+      s |= ens_alloc(e, (void**)&me.M1, nc * sizeof(double));
+      s |= ens_alloc(e, (void**)&me.M2, nc * sizeof(double));
+    } else {
+      for (int b = 0; b < 2; b++) {
+        s |= ens_alloc(e, (void**)&me.P[b], nc * sizeof(double));
+        s |= ens_alloc(e, (void**)&me.S[b], nc * sizeof(double));
+      }
+      double** w[] = {&me.L1, &me.L2, &me.ro1, &me.ro2, &me.lnSe};
+      for (double** p : w) s |= ens_alloc(e, (void**)p, nc * sizeof(double));
+    }
+  }
+  if (!s) s |= ens_alloc(e, (void**)&e->d_counter, sizeof(unsigned));
+  if (!s) s |= ens_alloc(e, (void**)&e->d_status, sizeof(unsigned));
+  if (!s) s |= ens_alloc(e, (void**)&e->d_mass_count, sizeof(unsigned));
+  if (!s) {
+    cudaMemset(e->d_status, 0, sizeof(unsigned));
+    cudaMemset(e->d_mass_count, 0, sizeof(unsigned));
+    s = build_lists(e);
+  }
+  if (s) {
+    gbf_ensemble_destroy(e);
+    return gbf_fail(s ? s : GBF_ERR_CUDA, "gbf_ensemble_create");
+  }
+  *out = e;
+  return GBF_OK;
+}
+
+int gbf_ensemble_destroy(gbf_ensemble* e) {
+  if (!e) return GBF_OK;
+  if (e->stream) cudaStreamSynchronize(e->stream);
+  drop_graphs(e);
+  gbf_timer_free(&e->timer);
+  for (void* p : e->owned) cudaFree(p);
+  if (e->own_stream && e->stream) cudaStreamDestroy(e->stream);
+  delete e;
+  return GBF_OK;
+}
+
+int gbf_ensemble_size(gbf_ensemble* e) { return e ? e->n : 0; }
+long long gbf_ensemble_cells(gbf_ensemble* e) { return e ? e->cells : 0; }
+long long gbf_ensemble_interior_cells(gbf_ensemble* e) {
+  if (!e) return 0;
+  long long s = 0;
+  for (auto& m : e->models) s += (long long)(m.nx - 2) * (m.ny - 2) * (m.nz - 2);
+  return s;
+}
+
+int gbf_ensemble_set_stream(gbf_ensemble* e, void* stream) {
+  if (!e) return gbf_fail(GBF_ERR_ARG, "gbf_ensemble_set_stream");
+  GBF_CUDA(cudaStreamSynchronize(e->stream));
+  if (e->own_stream) cudaStreamDestroy(e->stream);
+  e->stream = (cudaStream_t)stream;
+  e->own_stream = false;
+  drop_graphs(e);
+  return GBF_OK;
+}
+
+int gbf_ensemble_set_outputs(gbf_ensemble* e, int flags, int mass_cap) {
+  if (!e || mass_cap < 0 || (flags & ~GBF_OUT_MASS)) return gbf_fail(GBF_ERR_ARG, "gbf_ensemble_set_outputs");
+  if ((flags & GBF_OUT_MASS) && mass_cap > e->mass_cap) {
+    if (int s = ens_alloc(e, (void**)&e->d_mass_hist, 2 * sizeof(double) * (size_t)mass_cap * e->n)) return s;
+    e->mass_cap = mass_cap;
+  }
+  e->out_flags = flags;
+  GBF_CUDA(cudaMemsetAsync(e->d_mass_count, 0, sizeof(unsigned), e->stream));
+  drop_graphs(e);
+  return GBF_OK;
+}
+
+int gbf_ensemble_upload(gbf_ensemble* e, int r, const double* P1, const double* S2) {
+  if (!e || r < 0 || r >= e->n || !P1 || !S2) return gbf_fail(GBF_ERR_ARG, "gbf_ensemble_upload");
+  EnsMember& me = e->h_mem[r];
+  const gbf_model& m = e->models[r];
+  const size_t nc = gbf_geo(m).n, b = nc * sizeof(double);
+  // all members share one buffer parity: write the member's current buffer
+  const int c = e->cur;
+  if (e->precision == GBF_PREC_F64) {
+    GBF_CUDA(cudaMemcpyAsync(me.P[c], P1, b, cudaMemcpyDefault, e->stream));
+    GBF_CUDA(cudaMemcpyAsync(me.S[c], S2, b, cudaMemcpyDefault, e->stream));
+  } else {
+    double* tmp = nullptr;
+    GBF_CUDA(cudaMallocAsync((void**)&tmp, 2 * b, e->stream));
+    GBF_CUDA(cudaMemcpyAsync(tmp, P1, b, cudaMemcpyDefault, e->stream));
+    GBF_CUDA(cudaMemcpyAsync(tmp + nc, S2, b, cudaMemcpyDefault, e->stream));
+    if (int s = gbf_split_init_state(m, tmp, tmp + nc, me.dPf[c], me.Sf[c], me.M1, me.M2,
+                                     e->precision == GBF_PREC_SPLIT_DF, e->stream))
+      return s;
+    // the next-state buffer's faces are rewritten every step; start them equal
+    GBF_CUDA(cudaMemcpyAsync(me.dPf[c ^ 1], me.dPf[c], nc * sizeof(float), cudaMemcpyDeviceToDevice, e->stream));
+    GBF_CUDA(cudaMemcpyAsync(me.Sf[c ^ 1], me.Sf[c], nc * sizeof(float), cudaMemcpyDeviceToDevice, e->stream));
+    GBF_CUDA(cudaFreeAsync(tmp, e->stream));
+  }
+  e->steps = 0;
+  GBF_CUDA(cudaMemsetAsync(e->d_status, 0, sizeof(unsigned), e->stream));
+  GBF_CUDA(cudaMemsetAsync(e->d_mass_count, 0, sizeof(unsigned), e->stream));
+  return GBF_OK;
+}
+
+int gbf_ensemble_step(gbf_ensemble* e, int nsteps) {
+  if (!e || nsteps < 0) return gbf_fail(GBF_ERR_ARG, "gbf_ensemble_step");
+  return ens_step(e, nsteps, true);
+}
+
+int gbf_ensemble_sync(gbf_ensemble* e) {
+  if (!e) return gbf_fail(GBF_ERR_ARG, "gbf_ensemble_sync");
+  GBF_CUDA(cudaStreamSynchronize(e->stream));
+  return GBF_OK;
+}
+
+int gbf_ensemble_status(gbf_ensemble* e) {
+  if (!e) return gbf_fail(GBF_ERR_ARG, "gbf_ensemble_status");
+  unsigned h = 0;
+  GBF_CUDA(cudaMemcpyAsync(&h, e->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost, e->stream));
+  GBF_CUDA(cudaStreamSynchronize(e->stream));
+  if (h & GBF_DEV_TIMEOUT) return gbf_fail(GBF_ERR_TIMEOUT, "device wait timed out");
+  if (h & GBF_DEV_NONFINITE) return gbf_fail(GBF_ERR_NONFINITE, "non-finite P or S");
+  return GBF_OK;
+}
+
+int gbf_ensemble_download(gbf_ensemble* e, int r, int field, double* host) {
+  if (!e || r < 0 || r >= e->n || !host || (field != GBF_FIELD_P1 && field != GBF_FIELD_S2))
+    return gbf_fail(GBF_ERR_ARG, "gbf_ensemble_download");
+  const EnsMember& me = e->h_mem[r];
+  const gbf_model& m = e->models[r];
+  const size_t nc = gbf_geo(m).n, b = nc * sizeof(double);
+  if (e->precision == GBF_PREC_F64) {
+    GBF_CUDA(cudaMemcpyAsync(host, field == GBF_FIELD_P1 ? me.P[e->cur] : me.S[e->cur], b, cudaMemcpyDefault, e->stream));
+  } else {
+    double* tmp = nullptr;
+    GBF_CUDA(cudaMallocAsync((void**)&tmp, b, e->stream));
+    k_ens_split_to_f64<<<gbf_grid_for(nc, kThreads, 4), kThreads, 0, e->stream>>>(
+        m, me.dPf[e->cur], me.Sf[e->cur], field == GBF_FIELD_P1 ? tmp : nullptr, field == GBF_FIELD_S2 ? tmp : nullptr);
+    GBF_CUDA(cudaGetLastError());
+    GBF_CUDA(cudaMemcpyAsync(host, tmp, b, cudaMemcpyDefault, e->stream));
+    GBF_CUDA(cudaFreeAsync(tmp, e->stream));
+  }
+  GBF_CUDA(cudaStreamSynchronize(e->stream));
+  return GBF_OK;
+}
+
+int gbf_ensemble_mass_history(gbf_ensemble* e, double* host, int max_steps, int* nsteps_out) {
+  if (!e || !host || max_steps < 0) return gbf_fail(GBF_ERR_ARG, "gbf_ensemble_mass_history");
+  unsigned cnt = 0;
+  GBF_CUDA(cudaMemcpyAsync(&cnt, e->d_mass_count, sizeof(unsigned), cudaMemcpyDeviceToHost, e->stream));
+  GBF_CUDA(cudaStreamSynchronize(e->stream));
+  int n = (int)std::min<unsigned>(cnt, (unsigned)std::min(max_steps, e->mass_cap));
+  if (n > 0)
+    GBF_CUDA(cudaMemcpy(host, e->d_mass_hist, 2 * sizeof(double) * (size_t)n * e->n, cudaMemcpyDeviceToHost));
+  if (nsteps_out) *nsteps_out = n;
+  return GBF_OK;
+}
+
+int gbf_ensemble_set_timing(gbf_ensemble* e, int on) {
+  if (!e) return gbf_fail(GBF_ERR_ARG, "gbf_ensemble_set_timing");
+  e->timer.on = on != 0;
+  return GBF_OK;
+}
+
+int gbf_ensemble_kernel_times(gbf_ensemble* e, double* ms, int* launches, int nkinds) {
+  if (!e || !ms || !launches) return gbf_fail(GBF_ERR_ARG, "gbf_ensemble_kernel_times");
+  return gbf_timer_collect(&e->timer, ms, launches, nkinds);
+}
+
+int gbf_ensemble_launches_per_step(gbf_ensemble* e) {
+  if (!e) return 0;
+  const int mass = (e->out_flags & GBF_OUT_MASS) ? 2 : 0;
+  return (e->precision == GBF_PREC_F64 ? 3 : 2) + mass;
+}
+
+int gbf_ensemble_set_tuning(gbf_ensemble* e, int shape, int edge, int kchunk) {
+  if (!e || shape < -1 || shape >= kShapes || kchunk < 0) return gbf_fail(GBF_ERR_ARG, "gbf_ensemble_set_tuning");
+  GBF_CUDA(cudaStreamSynchronize(e->stream));
+  if (shape >= 0) e->shape = shape;
+  if (edge > 0) e->kchunk_by_edge[edge] = kchunk;
+  return build_lists(e);
+}
+
+int gbf_ensemble_get_tuning(gbf_ensemble* e, int* shape, int* edges, int* kchunks, int max_entries) {
+  if (!e || !shape) return gbf_fail(GBF_ERR_ARG, "gbf_ensemble_get_tuning");
+  *shape = e->shape;
+  int q = 0;
+  for (auto& kv : e->kchunk_by_edge) {
+    if (q >= max_entries) break;
+    if (edges) edges[q] = kv.first;
+    if (kchunks) kchunks[q] = kv.second;
+    q++;
+  }
+  return q;
+}
+
+const char* gbf_ensemble_shape_name(int shape) {
+  static const char* names[kShapes] = {"32x8", "64x4", "32x4"};
+  return (shape >= 0 && shape < kShapes) ? names[shape] : "";
+}
+
+// Pick the tile shape, then the fusion depth of every member edge, each by
+// timing `trial_steps` steps per candidate (CUDA events on the ensemble's
+// stream). Advances the state: upload the initial state after tuning.
+int gbf_ensemble_autotune(gbf_ensemble* e, int trial_steps) {
+  if (!e || trial_steps < 1) return gbf_fail(GBF_ERR_ARG, "gbf_ensemble_autotune");
+  if (e->precision == GBF_PREC_F64) return GBF_OK;  // FP64 kernels: chunked, nothing to tune
+  const bool timing = e->timer.on;
+  e->timer.on = false;
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  auto trial = [&](float& ms) -> int {
+    if (int s = ens_step(e, 1, false)) return s;  // warm
+    cudaEventRecord(a, e->stream);
+    if (int s = ens_step(e, trial_steps, false)) return s;
+    cudaEventRecord(b, e->stream);
+    GBF_CUDA(cudaEventSynchronize(b));
+    cudaEventElapsedTime(&ms, a, b);
+    return GBF_OK;
+  };
+  int st = GBF_OK;
+  // 1. tile shape, with the default fusion depth
+  float best = 1e30f;
+  int best_shape = e->shape;
+  for (int sh = 0; sh < kShapes && !st; sh++) {
+    e->shape = sh;
+    if ((st = build_lists(e))) break;
+    float ms = 0;
+    if ((st = trial(ms))) break;
+    if (ms < best) { best = ms; best_shape = sh; }
+  }
+  e->shape = best_shape;
+  // 2. fusion depth per member edge (k planes per tile pass)
+  std::vector<int> edges;
+  for (auto& m : e->models)
+    if (std::find(edges.begin(), edges.end(), m.nx) == edges.end()) edges.push_back(m.nx);
+  const int cands[] = {16, 32, 64, 0};
+  for (int edge : edges) {
+    if (st) break;
+    int best_kc = 0;
+    float bt = 1e30f;
+    for (int kc : cands) {
+      e->kchunk_by_edge[edge] = kc;
+      if ((st = build_lists(e))) break;
+      float ms = 0;
+      if ((st = trial(ms))) break;
+      if (ms < bt) { bt = ms; best_kc = kc; }
+    }
+    e->kchunk_by_edge[edge] = best_kc;
+  }
+  if (!st) st = build_lists(e);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  e->timer.on = timing;
+  return st;
+}
+
+}  // extern "C"

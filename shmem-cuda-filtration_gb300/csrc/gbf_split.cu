@@ -93,47 +93,6 @@ __global__ void __launch_bounds__(kSplitThreads, 4) k_split_step(const GbfSplitC
   if (G.mass_partials) split_block_mass<DF>(acc, C.V, G.mass_partials + 2 * blockIdx.x);
 }
 
-// Value the reference's boundary sweep leaves in P1 (cpu.cpp:366-403), in
-// the dP = P - P_hs(j) representation: copies within a row keep dP, the top
-// (P_atm) and the hydrostatic sides (P_hs) are dP = 0, and the bottom rule
-// P(ny-1) = P(ny-2) + ro1(i,1,0) g h2 becomes dP(ny-2) + (ro1(i,1,0) - rho01) g h2.
-__device__ float sweep_dP(const gbf_model& m, const GbfGeo& g, const float* cur, const float* old, int i, int j,
-                          int k, float H) {
-  bool has_add = false;
-  float add = 0.f, base = NAN;
-  for (int hop = 0; hop < 6; ++hop) {
-    if (m.bc_mode == GBF_BC_HYDROSTATIC_SIDES && (i == 0 || i == g.nx - 1 || k == 0 || k == g.nz - 1)) {
-      base = 0.f;
-      break;
-    }
-    if (i == 0) { base = gbf_later(g, cur, old, 1, j, k); break; }
-    if (i == g.nx - 1) {
-      i = g.nx - 2;
-      if (!gbf_is_boundary(g, i, j, k)) { base = cur[gbf_idx(g, i, j, k)]; break; }
-      continue;
-    }
-    if (j == g.ny - 1) {
-      // start-of-step water density at (i, 1, 0): P - P_atm = dP_old + H
-      const float pp = old[(size_t)i + (size_t)g.nx] + H;
-      add = (float)(m.ro01 * m.beta1 * m.g * m.h2) * pp;
-      has_add = true;
-      j = g.ny - 2;
-      if (!gbf_is_boundary(g, i, j, k)) { base = cur[gbf_idx(g, i, j, k)]; break; }
-      continue;
-    }
-    if (j == 0) { base = 0.f; break; }
-    if (k == 0) { base = gbf_later(g, cur, old, i, j, 1); break; }
-    if (k == g.nz - 1) {
-      k = g.nz - 2;
-      if (!gbf_is_boundary(g, i, j, k)) { base = cur[gbf_idx(g, i, j, k)]; break; }
-      continue;
-    }
-    base = cur[gbf_idx(g, i, j, k)];
-    break;
-  }
-  return has_add ? base + add : base;
-}
-
 __global__ void __launch_bounds__(kThreads) k_split_boundary(const gbf_model m, const GbfSplitGrid G, float H) {
   const GbfGeo g = gbf_geo(m);
   const size_t nb = gbf_boundary_count(g);
@@ -142,7 +101,7 @@ __global__ void __launch_bounds__(kThreads) k_split_boundary(const gbf_model m, 
     gbf_boundary_cell(g, t, i, j, k);
     const size_t c = gbf_idx(g, i, j, k);
     G.Sn[c] = gbf_sweep_S<float>(m, g, G.Sn, G.S, i, j, k);
-    G.dPn[c] = sweep_dP(m, g, G.dPn, G.dP, i, j, k, H);
+    G.dPn[c] = gbf_split_sweep_dP(m, g, G.dPn, G.dP, i, j, k, H);
   }
 }
 
@@ -248,6 +207,14 @@ int gbf_split_alloc(gbf_domain* d) {
   // per-block mass partials of the split step kernel
   if (!s) s |= gbf_domain_alloc(d, (void**)&d->split_partials, 2 * sizeof(double) * gbf_split_blocks(d->m));
   return s ? GBF_ERR_NOMEM : GBF_OK;
+}
+
+int gbf_split_init_state(const gbf_model& m, const double* P_dev, const double* S_dev, float* dPf, float* Sf,
+                         double* M1, double* M2, bool df, cudaStream_t st) {
+  const size_t n = gbf_geo(m).n;
+  k_split_init<<<gbf_grid_for(n, kThreads, 4), kThreads, 0, st>>>(m, P_dev, S_dev, dPf, Sf, M1, M2, df ? 1 : 0);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? GBF_OK : gbf_cuda_check(e, "gbf_split_init_state");
 }
 
 int gbf_split_upload(gbf_domain* d, const double* P1, const double* S2, cudaMemcpyKind kind) {

@@ -87,15 +87,24 @@ template <> struct Wide<true> {
 };
 
 // ------------------------------------------------------------- tile shape
+// A CTA of TX x TY threads owns a TX x TY column tile (one column per thread).
+template <int TX, int TY>
+struct GbfSplitShape {
+  static constexpr int threads = TX * TY;
+  static constexpr int HX = TX + 2, HY = TY + 2, HN = HX * HY;  // plane with its 1-cell halo
+  static constexpr int slots = (HN + threads - 1) / threads;    // halo elements per thread
+};
+// Default shape of the single-domain kernel.
 constexpr int kSplitTX = 32, kSplitTY = 8;
 constexpr int kSplitThreads = kSplitTX * kSplitTY;
-constexpr int kSplitHX = kSplitTX + 2, kSplitHY = kSplitTY + 2, kSplitHN = kSplitHX * kSplitHY;
-constexpr int kSplitSlots = (kSplitHN + kSplitThreads - 1) / kSplitThreads;  // halo elements per thread
 
 // One x-y plane of the tile with its 1-cell halo.
-struct GbfSplitPlane {
-  float dP[kSplitHN], S[kSplitHN], L1[kSplitHN], L2[kSplitHN];
+template <int TX, int TY>
+struct GbfSplitPlaneT {
+  static constexpr int HN = GbfSplitShape<TX, TY>::HN;
+  float dP[HN], S[HN], L1[HN], L2[HN];
 };
+using GbfSplitPlane = GbfSplitPlaneT<kSplitTX, kSplitTY>;
 
 // Mobility x density of both phases at one cell (FP32): Brooks-Corey kr
 // (cpu.cpp:60-62) from one log2 and two exp2, Xi = -K kr / mu, densities at
@@ -139,11 +148,15 @@ struct GbfSplitAcc {
 
 // One CTA: interior cells [i0, i0+TX) x [j0, j0+TY) of planes [k0, k1); i0,
 // j0, k0 >= 1. `pl` points to two planes of shared memory.
-template <bool DF>
+template <bool DF, int TX = kSplitTX, int TY = kSplitTY>
 __device__ void split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i0, int j0, int k0, int k1,
-                           GbfSplitPlane* pl, GbfSplitAcc<DF>& acc) {
+                           GbfSplitPlaneT<TX, TY>* pl, GbfSplitAcc<DF>& acc) {
   using W = Wide<DF>;
   using WT = typename W::T;
+  using Sh = GbfSplitShape<TX, TY>;
+  constexpr int kSplitTX = TX, kSplitThreads = Sh::threads, kSplitHX = Sh::HX, kSplitHN = Sh::HN,
+                kSplitSlots = Sh::slots;
+  using GbfSplitPlane = GbfSplitPlaneT<TX, TY>;
   const int nx = C.nx, ny = C.ny, nz = C.nz;
   const unsigned pln = (unsigned)nx * (unsigned)ny;  // grids hold < 2^32 cells (checked on the host)
   const int tx = threadIdx.x % kSplitTX, ty = threadIdx.x / kSplitTX;
@@ -317,10 +330,51 @@ __device__ void split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i
   }
 }
 
+// Value the reference's boundary sweep leaves in P1 (cpu.cpp:366-403), in
+// the dP = P - P_hs(j) representation: copies within a row keep dP, the top
+// (P_atm) and the hydrostatic sides (P_hs) are dP = 0, and the bottom rule
+// P(ny-1) = P(ny-2) + ro1(i,1,0) g h2 becomes dP(ny-2) + (ro1(i,1,0) - rho01) g h2.
+__device__ __forceinline__ float gbf_split_sweep_dP(const gbf_model& m, const GbfGeo& g, const float* cur,
+                                                    const float* old, int i, int j, int k, float H) {
+  bool has_add = false;
+  float add = 0.f, base = NAN;
+  for (int hop = 0; hop < 6; ++hop) {
+    if (m.bc_mode == GBF_BC_HYDROSTATIC_SIDES && (i == 0 || i == g.nx - 1 || k == 0 || k == g.nz - 1)) {
+      base = 0.f;
+      break;
+    }
+    if (i == 0) { base = gbf_later(g, cur, old, 1, j, k); break; }
+    if (i == g.nx - 1) {
+      i = g.nx - 2;
+      if (!gbf_is_boundary(g, i, j, k)) { base = cur[gbf_idx(g, i, j, k)]; break; }
+      continue;
+    }
+    if (j == g.ny - 1) {
+      // start-of-step water density at (i, 1, 0): P - P_atm = dP_old + H
+      const float pp = old[(size_t)i + (size_t)g.nx] + H;
+      add = (float)(m.ro01 * m.beta1 * m.g * m.h2) * pp;
+      has_add = true;
+      j = g.ny - 2;
+      if (!gbf_is_boundary(g, i, j, k)) { base = cur[gbf_idx(g, i, j, k)]; break; }
+      continue;
+    }
+    if (j == 0) { base = 0.f; break; }
+    if (k == 0) { base = gbf_later(g, cur, old, i, j, 1); break; }
+    if (k == g.nz - 1) {
+      k = g.nz - 2;
+      if (!gbf_is_boundary(g, i, j, k)) { base = cur[gbf_idx(g, i, j, k)]; break; }
+      continue;
+    }
+    base = cur[gbf_idx(g, i, j, k)];
+    break;
+  }
+  return has_add ? base + add : base;
+}
+
 // Deterministic block reduction of the phase-mass partial sums (FP64).
-template <bool DF>
+template <bool DF, int NT = kSplitThreads>
 __device__ __forceinline__ void split_block_mass(const GbfSplitAcc<DF>& acc, double V, double* out2) {
-  __shared__ double red[2][kSplitThreads / 32];
+  __shared__ double red[2][NT / 32];
   double a = Wide<DF>::tod(acc.m1), b = Wide<DF>::tod(acc.m2);
   for (int o = 16; o > 0; o >>= 1) {
     a += __shfl_down_sync(0xffffffffu, a, o);
@@ -331,7 +385,7 @@ __device__ __forceinline__ void split_block_mass(const GbfSplitAcc<DF>& acc, dou
   __syncthreads();
   if (threadIdx.x == 0) {
     double x = 0., y = 0.;
-    for (int q = 0; q < kSplitThreads / 32; q++) { x += red[0][q]; y += red[1][q]; }
+    for (int q = 0; q < NT / 32; q++) { x += red[0][q]; y += red[1][q]; }
     out2[0] = x * V;
     out2[1] = y * V;
   }

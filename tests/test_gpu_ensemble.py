@@ -1,0 +1,153 @@
+"""Batched ensembles: every member must equal a single-domain run of the same
+model bit for bit (tiling and batching do not change any cell's arithmetic),
+for every tile shape and fusion depth, and must match the FP64 oracle to the
+precision form's tolerances."""
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+import pytest
+
+from gpu_util import p_tol
+
+pytestmark = pytest.mark.gpu
+
+
+@dataclass
+class Mem:
+    model: object
+    K: np.ndarray = None
+    phi: np.ndarray = None
+    media: np.ndarray = None
+
+    def initial_state(self):
+        m = self.model
+        j = np.arange(m.ny, dtype=np.float64)[None, :, None]
+        P = np.broadcast_to(m.P_atm + j * m.ro01 * m.g * m.h2, m.shape).copy()
+        S = np.zeros(m.shape, np.float64)
+        if m.source_mode == 0:
+            i, k = np.arange(m.nx), np.arange(m.nz)
+            pi = (i >= m.nx // 2 - m.source) & (i <= m.nx // 2 + m.source)
+            pk = (k >= m.nz // 2 - m.source) & (k <= m.nz // 2 + m.source)
+            S[:, 0, :] = np.where(pk[:, None] & pi[None, :], m.S2_gr, 0.0)
+        return P, S
+
+
+def members(abi, lib):
+    """Uneven members: sizes, fields, closures, anisotropy, sources, BCs."""
+    out = []
+    rng = np.random.default_rng(21)
+    for r, (nx, ny, nz) in enumerate([(24, 20, 18), (36, 16, 22), (16, 16, 16), (40, 24, 12)]):
+        m = abi.reference_model(nx, ny, nz, 1.0)
+        m.h1 = m.h2 = m.h3 = 0.05
+        m.S_wr[:] = [0.1, 0.1]
+        lam = float(rng.uniform(2.0, 3.5))
+        m.lam[:] = [lam, lam]
+        pd = float(rng.uniform(500, 1500))
+        m.P_d[:] = [pd, pd]
+        m.kv = float(rng.uniform(0.1, 1.0))
+        if r % 2 == 0:
+            m.source_mode, m.rate_cells, m.rate = abi.GBF_SOURCE_RATE, 4, float(rng.uniform(1e-3, 1e-2))
+            m.bc_mode = abi.GBF_BC_HYDROSTATIC_SIDES
+        else:
+            m.source = 2
+        K = np.empty(m.shape, np.float32)
+        phi = np.empty(m.shape, np.float32)
+        lib.gbf_fill_lognormal_K(nx, ny, nz, 500 + r, 6.64e-11, float(rng.uniform(0.5, 2.0)), 3.0, K.ctypes.data)
+        lib.gbf_fill_porosity(nx, ny, nz, 600 + r, 0.35, 0.05, phi.ctypes.data)
+        cells = abi.GbfCells()
+        cells.K = K.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+        cells.phi = phi.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+        m.dt = 0.5 * lib.gbf_stable_dt(ctypes.byref(m), ctypes.byref(cells), 1.0)
+        m.newton_tol = 1e-11
+        out.append(Mem(m, K, phi))
+    return out
+
+
+def mods(pkg):
+    from importlib import import_module
+    return import_module(pkg.__name__ + ".ensemble"), import_module(pkg.__name__ + ".domain")
+
+
+PRECS = ["f64", "split", "split_df"]
+
+
+def prec(abi, name):
+    return {"split": abi.GBF_PREC_SPLIT, "split_df": abi.GBF_PREC_SPLIT_DF, "f64": abi.GBF_PREC_F64}[name]
+
+
+@pytest.mark.parametrize("p", PRECS)
+def test_ensemble_members_equal_single_domains(gpu_lib, abi, pkg, p):
+    E, D = mods(pkg)
+    mems = members(abi, gpu_lib)
+    steps = 25
+    single = []
+    for mem in mems:
+        d = D.Domain(mem.model, None, mem.K, mem.phi, precision=prec(abi, p))
+        d.set_outputs(abi.GBF_OUT_MASS, steps)
+        d.upload(*mem.initial_state())
+        d.step(steps)
+        single.append((d.download("P1"), d.download("S2"), d.mass_history(steps)))
+        d.close()
+    shapes = [0] if p == "f64" else [0, 1, 2]
+    for shape in shapes:
+        ens = E.Ensemble(mems, precision=prec(abi, p))
+        if p != "f64":
+            ens.set_tuning(shape, 0, 0)
+            ens.set_tuning(-1, 24, 7)  # a member edge with a short k range (several passes per column)
+        ens.set_outputs(abi.GBF_OUT_MASS, steps)
+        ens.upload_initial()
+        ens.step(steps)
+        assert ens.status() == abi.GBF_OK
+        mass = ens.mass_history(steps)
+        assert mass.shape == (steps, len(mems), 2)
+        for r, (P, S, mh) in enumerate(single):
+            assert np.array_equal(ens.download(r, "S2"), S), (shape, r)
+            assert np.array_equal(ens.download(r, "P1"), P), (shape, r)
+            np.testing.assert_allclose(mass[:, r, :], mh, rtol=1e-12, atol=0)
+        ens.close()
+
+
+@pytest.mark.parametrize("p", PRECS)
+def test_ensemble_members_match_oracle(gpu_lib, abi, pkg, O, oracle, p):
+    E, _ = mods(pkg)
+    mems = members(abi, gpu_lib)
+    steps = 30
+    ens = E.Ensemble(mems, precision=prec(abi, p))
+    ens.upload_initial()
+    ens.step(steps)
+    assert ens.status() == abi.GBF_OK
+    for r, mem in enumerate(mems):
+        st = O.State(mem.model, None, mem.K, mem.phi)
+        P0, S0 = mem.initial_state()
+        st["P1"][...] = P0
+        st["S2"][...] = S0
+        oracle.step(st, steps)
+        S, P = ens.download(r, "S2"), ens.download(r, "P1")
+        if p == "f64":
+            assert np.abs(S - st["S2"]).max() <= 1e-12
+            assert np.abs(P - st["P1"]).max() / np.abs(st["P1"]).max() <= p_tol(mem.model)
+        else:
+            assert np.abs(S - st["S2"]).max() <= 1e-5
+            assert np.linalg.norm(P - st["P1"]) / np.linalg.norm(st["P1"]) <= 1e-6
+    ens.close()
+
+
+def test_ensemble_autotune(gpu_lib, abi, pkg):
+    E, _ = mods(pkg)
+    mems = members(abi, gpu_lib)
+    ens = E.Ensemble(mems, precision=abi.GBF_PREC_SPLIT_DF)
+    ens.upload_initial()
+    tuning = ens.autotune(2)
+    assert tuning["tile"] in ("32x8", "64x4", "32x4")
+    assert set(tuning["kchunk_by_edge"]) == {m.model.nx for m in mems}
+    # after tuning, a fresh run still equals the default-tuned one
+    ens.upload_initial()
+    ens.step(10)
+    ref = E.Ensemble(mems, precision=abi.GBF_PREC_SPLIT_DF)
+    ref.upload_initial()
+    ref.step(10)
+    for r in range(len(mems)):
+        assert np.array_equal(ens.download(r, "S2"), ref.download(r, "S2"))
+    ens.close()
+    ref.close()
