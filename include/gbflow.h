@@ -136,6 +136,18 @@ int gbf_newton_f64(const gbf_model* m, gbf_arrays d_arrays, gbf_cells d_cells, v
 /* a5; `d_scratch` must hold gbf_boundary_scratch_doubles(m) doubles (device). */
 int gbf_boundary_f64(const gbf_model* m, gbf_arrays d_arrays, double* d_scratch, void* stream);
 size_t gbf_boundary_scratch_doubles(const gbf_model* m);
+/* a5 for callers that cannot allocate device memory where they apply the
+   boundary conditions: code being captured into a CUDA graph (cudaMalloc is
+   not allowed during capture), callers whose memory belongs to another
+   allocator or is budgeted up front, drivers that bring their own arrays.
+   No counterpart in the reference. Same results as gbf_boundary_f64; its
+   scratch is a fixed 8 MiB array of the library in device memory that every
+   GPU loading the library keeps until exit, so it serves grids with at most
+   524288 boundary cells (cubes up to 295^3) and returns GBF_ERR_ARG beyond.
+   Allocates nothing. Its first call on a device looks up the array's device
+   address, so make it before any stream capture. All calls share the array:
+   calls that overlap on the GPU race. */
+int gbf_boundary_f64_noalloc(const gbf_model* m, gbf_arrays d_arrays, void* stream);
 
 /* ------------------------------------------------------- single domain ----
  * One grid whose state lives in HBM between steps. `precision` is

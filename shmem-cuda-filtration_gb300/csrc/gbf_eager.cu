@@ -18,6 +18,8 @@
 // bit between CUDA and the host libm.
 #include <math.h>
 
+#include <mutex>
+
 #include "gbf_internal.h"
 
 namespace {
@@ -219,6 +221,37 @@ __global__ void __launch_bounds__(kThreads) k_boundary_scatter(const gbf_model m
   }
 }
 
+// Scratch of gbf_boundary_f64_noalloc: a fixed array of this library in
+// device memory, 8 MiB, held by every GPU that loads the library until the
+// process exits. In host code the name is only a stand-in for the array, not
+// its device address: host code passes the address that
+// cudaGetSymbolAddress returns for the current device (noalloc_scratch).
+constexpr size_t kNoAllocScratchDoubles = (size_t)1 << 20;
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocScratchDoubles];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+double* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+// Device address of g_noalloc_scratch on the current device, looked up once
+// per device (with that device current) and cached.
+int noalloc_scratch(double** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return gbf_cuda_check(e, "gbf_boundary_f64_noalloc: cudaGetDevice");
+  if (dev < 0 || dev >= kNoAllocMaxDevices) return gbf_fail(GBF_ERR_ARG, "gbf_boundary_f64_noalloc: device index");
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) return gbf_cuda_check(e != cudaSuccess ? e : cudaErrorInvalidSymbol,
+                                                      "gbf_boundary_f64_noalloc: cudaGetSymbolAddress");
+    g_noalloc_ptr[dev] = (double*)p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return GBF_OK;
+}
+
 int check_model(const gbf_model* m, const char* where) {
   if (!m || m->nx < 3 || m->ny < 3 || m->nz < 3) return gbf_fail(GBF_ERR_ARG, where);
   return GBF_OK;
@@ -272,6 +305,30 @@ int gbf_boundary_f64(const gbf_model* m, gbf_arrays a, double* scratch, void* st
   k_boundary_gather<<<grid, kThreads, 0, (cudaStream_t)stream>>>(*m, a, scratch);
   k_boundary_scatter<<<grid, kThreads, 0, (cudaStream_t)stream>>>(*m, a, scratch);
   return launched("gbf_boundary_f64");
+}
+
+// The boundary pass for callers that cannot allocate device memory when they
+// apply the boundary conditions. Same kernels and results as
+// gbf_boundary_f64; the gather scratch is the library's fixed device array
+// g_noalloc_scratch instead of a caller buffer. Allocates nothing: no
+// cudaMalloc, cudaFree or allocating library routine. The first call on a
+// device looks up the array's address there (cudaGetSymbolAddress), so make
+// that first call before any stream capture. Every call on a device uses the
+// same array, which keeps the last call's contents: the gather fills every
+// slot the scatter reads, so nothing needs clearing, and calls that overlap
+// on the same GPU (from several streams or host threads) race on it.
+int gbf_boundary_f64_noalloc(const gbf_model* m, gbf_arrays a, void* stream) {
+  if (int s = check_model(m, "gbf_boundary_f64_noalloc")) return s;
+  const size_t nb = gbf_boundary_count(gbf_geo(*m));
+  if (2 * nb > kNoAllocScratchDoubles)
+    return gbf_fail(GBF_ERR_ARG, "gbf_boundary_f64_noalloc: more than 524288 boundary cells (its fixed 8 MiB "
+                                 "scratch holds 2 doubles per boundary cell); use gbf_boundary_f64");
+  double* scratch = nullptr;
+  if (int s = noalloc_scratch(&scratch)) return s;
+  const unsigned grid = gbf_grid_for(nb, kThreads);
+  k_boundary_gather<<<grid, kThreads, 0, (cudaStream_t)stream>>>(*m, a, scratch);
+  k_boundary_scatter<<<grid, kThreads, 0, (cudaStream_t)stream>>>(*m, a, scratch);
+  return launched("gbf_boundary_f64_noalloc");
 }
 
 }  // extern "C"
