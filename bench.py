@@ -264,6 +264,9 @@ def run_ours(args, rank, world):
     if p not in PRECISIONS:
         raise SystemExit(f"unknown precision in {args.workload}")
     members, desc, ensemble = make_members(pkg, lib, cfg, args.cube)
+    if args.members:
+        members = members[: args.members]
+        desc += f" (first {len(members)} members)"
     prec = getattr(abi, PRECISIONS[p][0])
     stream = torch.cuda.Stream()
     cap = args.warmup + 2 * args.steps + 8
@@ -295,10 +298,10 @@ def run_ours(args, rank, world):
     achieved = algo / per_launch_s / 1e9 if per_launch_s > 0 else 0.0
     traffic = None
     tfile = ROOT / "profiles" / "traffic.json"
-    if tfile.exists():
+    if tfile.exists():  # ncu DRAM bytes per cell of a smaller capture, scaled to this launch's cells
         ent = json.loads(tfile.read_text()).get(args.workload, {}).get(kname)
         if ent:
-            traffic = ent["bytes_per_launch"]
+            traffic = ent["bytes_per_cell"] * (run.interior_cells if ent["cells"] == "interior" else cells)
     roof = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": hbm, "unit": "GB/s",
             "frac": achieved / hbm, "peak_source": peak_kind, "traffic": traffic,
             "algorithmic_bytes_per_launch": algo, "bytes_per_cell": bpc, "ms_per_launch": per_launch_s * 1e3,
@@ -436,6 +439,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="config4_splitdf")
     ap.add_argument("--cube", type=int, default=0, help="override the grid edge of config1 (profiling runs)")
+    ap.add_argument("--members", type=int, default=0, help="first N members of an ensemble (profiling runs)")
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-compare", action="store_true")
