@@ -41,12 +41,18 @@ GbfSplitConsts gbf_split_consts(const gbf_model& m) {
   C.g_dro = (float)(m.g * (m.ro02 - m.ro01));
   C.neg_inv_mu1 = (float)(-1.0 / m.mu1);
   C.neg_inv_mu2 = (float)(-1.0 / m.mu2);
+  C.nmr1 = (float)(-m.ro01 / m.mu1);
+  C.nmr2 = (float)(-m.ro02 / m.mu2);
+  C.ro01b1 = (float)(m.ro01 * m.beta1);
+  C.ro02b2 = (float)(m.ro02 * m.beta2);
   for (int md = 0; md < 2; md++) {
     const double lam = m.lambda[md], swr = m.S_wr[md];
     C.K[md] = (float)m.K[md];
     C.m[md] = (float)m.m[md];
     C.swr[md] = (float)swr;
     C.inv_1mswr[md] = (float)(1.0 / (1.0 - swr));
+    C.se_a[md] = 1.0f;  // (1 - S_wr) / (1 - S_wr)
+    C.se_b[md] = (float)(-1.0 / (1.0 - swr));
     C.e1[md] = (float)((2. + 3. * lam) / lam);
     C.e2[md] = (float)((2. + lam) / lam);
     C.m_inv_lam[md] = (float)(-1. / lam);

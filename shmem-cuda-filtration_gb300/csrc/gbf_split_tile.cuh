@@ -106,21 +106,33 @@ struct GbfSplitPlaneT {
 };
 using GbfSplitPlane = GbfSplitPlaneT<kSplitTX, kSplitTY>;
 
+// FP32 base-2 logarithm and exponential: the hardware approximations
+// (PTX lg2.approx / ex2.approx, flush-to-zero; about 2^-22 relative error),
+// ample for FP32 mobilities and capillary pressures.
+__device__ __forceinline__ float split_lg2(float x) {
+  float y;
+  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float split_ex2(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
 // Mobility x density of both phases at one cell (FP32): Brooks-Corey kr
 // (cpu.cpp:60-62) from one log2 and two exp2, Xi = -K kr / mu, densities at
 // P2 = P1 (cpu.cpp:63, 72-73).
 __device__ __forceinline__ void split_props(const GbfSplitConsts& C, int md, float K, float dP, float S, int j,
                                             float& L1, float& L2) {
   const float Pp = fmaf((float)j, C.H, dP);  // P - P_atm
-  const float Se = (1.f - S - C.swr[md]) * C.inv_1mswr[md];
-  const float l2 = __log2f(Se);
-  const float kr1 = exp2f(C.e1[md] * l2);
+  const float Se = fmaf(S, C.se_b[md], C.se_a[md]);  // (1 - S - S_wr) / (1 - S_wr)
+  const float l2 = split_lg2(Se);
+  const float kr1 = split_ex2(C.e1[md] * l2);
   const float om = 1.f - Se;
-  const float kr2 = om * om * (1.f - exp2f(C.e2[md] * l2));
-  const float ro1 = C.ro01 * fmaf(C.beta1, Pp, 1.f);
-  const float ro2 = C.ro02 * fmaf(C.beta2, Pp, 1.f);
-  L1 = K * kr1 * C.neg_inv_mu1 * ro1;
-  L2 = K * kr2 * C.neg_inv_mu2 * ro2;
+  const float kr2 = om * om * (1.f - split_ex2(C.e2[md] * l2));
+  L1 = K * kr1 * C.nmr1 * fmaf(C.beta1, Pp, 1.f);  // nmr = -rho0 / mu
+  L2 = K * kr2 * C.nmr2 * fmaf(C.beta2, Pp, 1.f);
 }
 
 // Donor-cell flux difference of one direction (see gbf_f64.cu): max/min
@@ -133,9 +145,9 @@ __device__ __forceinline__ float split_donor(float x1, float x2, float Lc, float
 
 // Brooks-Corey capillary pressure P_d S_e^(-1/lambda) and its S-derivative (cpu.cpp:303-308).
 __device__ __forceinline__ float split_Pk(const GbfSplitConsts& C, int md, float S, float& dPk_dS) {
-  const float Se = (1.f - S - C.swr[md]) * C.inv_1mswr[md];
-  const float Pk = C.P_d[md] * exp2f(C.m_inv_lam[md] * __log2f(Se));
-  dPk_dS = Pk * C.inv_lam_1mswr[md] / Se;
+  const float Se = fmaf(S, C.se_b[md], C.se_a[md]);
+  const float Pk = C.P_d[md] * split_ex2(C.m_inv_lam[md] * split_lg2(Se));
+  dPk_dS = __fdividef(Pk * C.inv_lam_1mswr[md], Se);
   return Pk;
 }
 
@@ -256,7 +268,7 @@ __device__ void split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i
       const float gs = split_donor(x1, x2, L2c, Pc.L2[hc - 1], Pc.L2[hc + 1]) * C.inv_h1 +
                        C.kv * split_donor(y12, y22, L2c, Pc.L2[hc - kSplitHX], Pc.L2[hc + kSplitHX]) * C.inv_h2 +
                        split_donor(z1, z2, L2c, L2m, L2p) * C.inv_h3;
-      const float dtphi = C.dt / phi;
+      const float dtphi = __fdividef(C.dt, phi);
       const float dm1 = -dtphi * f, dm2 = -dtphi * gs;  // FP32 mass increments
       // mass targets T = M + dm (wide), the rate source added exactly
       const WT T1 = W::add(M1, W::f(dm1));
@@ -274,51 +286,58 @@ __device__ void split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i
       //   r2 = (rho02 S - M2) + rho02 beta2 (P' + P_k) S - dm2 - src
       float dPk0;
       const float Pk0 = split_Pk(C, md, S0, dPk0);
-      const float r1 = W::tof(W::sub(W::sub(R01, M1), W::mulf(R01, S0))) +
-                       C.ro01 * C.beta1 * Pp * (1.f - S0) - dm1;
-      const float r2 = W::tof(W::sub(W::mulf(R02, S0), M2)) + C.ro02 * C.beta2 * (Pp + Pk0) * S0 - dm2 - srcf;
+      const float r1 = W::tof(W::sub(W::sub(R01, M1), W::mulf(R01, S0))) + C.ro01b1 * Pp * (1.f - S0) - dm1;
+      const float r2 = W::tof(W::sub(W::mulf(R02, S0), M2)) + C.ro02b2 * (Pp + Pk0) * S0 - dm2 - srcf;
       // FP32 Newton on d = (dp, ds): r + [F(x + d) - F(x)] = 0, the bracket
-      // written in increments so that no large terms cancel; the increment
-      // equations are nearly linear, so two iterations reach FP32 round-off.
+      // written in increments so that no large terms cancel. The equations
+      // are linear up to terms beta (dp ds, P_k'' ds^2): after the first
+      // (linear) iteration the residual is about rho0 beta |dp ds|; a second
+      // iteration runs when that could move S by more than 1e-9.
       const float a0 = fmaf(C.beta1, Pp, 1.f);
       const float b0 = fmaf(C.beta2, Pp + Pk0, 1.f);
-      float dp, ds, Pk, dPk;
+      float dp, ds, Pk;
       {
-        const float J11 = C.ro01 * C.beta1 * (1.f - S0), J12 = -C.ro01 * a0;
-        const float J21 = C.ro02 * C.beta2 * S0, J22 = C.ro02 * fmaf(C.beta2 * dPk0, S0, b0);
-        const float inv = 1.f / (J11 * J22 - J12 * J21);
+        const float J11 = C.ro01b1 * (1.f - S0), J12 = -C.ro01 * a0;
+        const float J21 = C.ro02b2 * S0, J22 = C.ro02 * fmaf(C.beta2 * dPk0, S0, b0);
+        const float inv = __fdividef(1.f, J11 * J22 - J12 * J21);
         dp = -inv * (J22 * r1 - J12 * r2);
         ds = -inv * (J11 * r2 - J21 * r1);
       }
-      {
+      const float nl = fmaxf(C.beta1, C.beta2) * fabsf(ds) * (fabsf(dp) + 4.f * fabsf(dPk0 * ds) + 1.f);
+      if (nl > 1e-9f) {
         float dPk1;
         const float Pk1 = split_Pk(C, md, S0 + ds, dPk1);
         const float S1 = S0 + ds;
         const float G1 = r1 + C.ro01 * (C.beta1 * dp * (1.f - S1) - a0 * ds);
         const float G2 = r2 + C.ro02 * (b0 * ds + C.beta2 * (dp + (Pk1 - Pk0)) * S1);
-        const float J11 = C.ro01 * C.beta1 * (1.f - S1);
+        const float J11 = C.ro01b1 * (1.f - S1);
         const float J12 = -C.ro01 * (a0 + C.beta1 * dp);
-        const float J21 = C.ro02 * C.beta2 * S1;
+        const float J21 = C.ro02b2 * S1;
         const float J22 = C.ro02 * (b0 + C.beta2 * (dp + (Pk1 - Pk0)) + C.beta2 * dPk1 * S1);
-        const float inv = 1.f / (J11 * J22 - J12 * J21);
+        const float inv = __fdividef(1.f, J11 * J22 - J12 * J21);
         const float ep = inv * (J22 * G1 - J12 * G2);
         const float es = inv * (J11 * G2 - J21 * G1);
         dp -= ep;
         ds -= es;
         Pk = fmaf(-dPk1, es, Pk1);  // P_k at the final S, to first order in the last correction
-        dPk = dPk1;
+      } else {
+        Pk = fmaf(dPk0, ds, Pk0);
       }
-      (void)dPk;
       const float dPn = dPc + dp, Sn = S0 + ds;
       G.dPn[c] = dPn;
       G.Sn[c] = Sn;
       W::store(G.M1, c, T1);
       // next step's ro2 S2 is taken at P2 = P1, without P_k (cpu.cpp:63 vs :306)
       W::store(G.M2, c, W::sub(T2, W::f(C.ro02 * C.beta2 * Pk * Sn)));
-      if (G.mass_partials) {
-        const WT phw = G.phi ? W::f(phi) : W::c(C.m_d[md], C.m_df[md]);
-        acc.m1 = W::add(acc.m1, W::mul(phw, T1));
-        acc.m2 = W::add(acc.m2, W::mul(phw, T2));
+      if (G.mass_partials) {  // phi T in the wide type (phi exact: an FP32 input or a wide table value)
+        if (G.phi) {
+          acc.m1 = W::add(acc.m1, W::mulf(T1, phi));
+          acc.m2 = W::add(acc.m2, W::mulf(T2, phi));
+        } else {
+          const WT phw = W::c(C.m_d[md], C.m_df[md]);
+          acc.m1 = W::add(acc.m1, W::mul(phw, T1));
+          acc.m2 = W::add(acc.m2, W::mul(phw, T2));
+        }
       }
       if (!isfinite(dPn) || !isfinite(Sn)) acc.bad = 1;
       dPm = dPc;
