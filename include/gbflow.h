@@ -210,6 +210,11 @@ int gbf_ensemble_set_stream(gbf_ensemble* e, void* stream);
 /* GBF_OUT_MASS only: per-member phase masses every step. */
 int gbf_ensemble_set_outputs(gbf_ensemble* e, int out_flags, int mass_history_capacity);
 int gbf_ensemble_upload(gbf_ensemble* e, int member, const double* P1, const double* S2);
+/* Every member at once: P_all and S_all hold all members' nx*ny*nz doubles
+   back to back in member order (host or device memory; pinned host memory
+   moves at full link speed). Both return after the transfer completed. */
+int gbf_ensemble_upload_all(gbf_ensemble* e, const double* P_all, const double* S_all);
+int gbf_ensemble_download_all(gbf_ensemble* e, double* P_all, double* S_all);
 int gbf_ensemble_step(gbf_ensemble* e, int nsteps);
 int gbf_ensemble_download(gbf_ensemble* e, int member, int field, double* host);
 /* [step][member][2] since the last upload. */

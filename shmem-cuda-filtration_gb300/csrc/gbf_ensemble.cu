@@ -36,6 +36,7 @@ struct EnsMember {
   double *M1, *M2;
   double *L1, *L2, *ro1, *ro2, *lnSe;
   int part_begin, part_end;  // this member's slots in the partial-sum array
+  unsigned long long off;    // first cell of this member in the packed all-members layout
 };
 
 struct EnsChunk {
@@ -200,6 +201,53 @@ __global__ void k_ens_mass_tail(const EnsMember* __restrict__ mem, const double*
 }
 __global__ void k_ens_count(unsigned* count) { atomicAdd(count, 1u); }
 
+// Packed all-members FP64 state (staging) -> every member's current buffer
+// (and the next buffer's faces, which the next step rewrites), one chunk
+// (member, cell range) per block.
+__global__ void __launch_bounds__(kThreads) k_ens_load(const EnsMember* __restrict__ mem,
+                                                       const EnsChunk* __restrict__ chunks, int cur,
+                                                       const double* __restrict__ P_all,
+                                                       const double* __restrict__ S_all, int precision) {
+  const EnsChunk ch = chunks[blockIdx.x];
+  const EnsMember& me = mem[ch.member];
+  const gbf_model& m = me.m;
+  for (unsigned c = ch.begin + threadIdx.x; c < ch.end; c += blockDim.x) {
+    const double p = P_all[me.off + c], s = S_all[me.off + c];
+    if (precision == GBF_PREC_F64) {
+      me.P[cur][c] = p;
+      me.S[cur][c] = s;
+    } else {
+      const int j = (int)((c / (unsigned)m.nx) % (unsigned)m.ny);
+      float dPf, Sf;
+      gbf_split_init_cell(m, p, s, j, dPf, Sf, me.M1, me.M2, c, precision == GBF_PREC_SPLIT_DF);
+      me.dPf[cur][c] = dPf;
+      me.Sf[cur][c] = Sf;
+      me.dPf[cur ^ 1][c] = dPf;
+      me.Sf[cur ^ 1][c] = Sf;
+    }
+  }
+}
+
+// Every member's current state -> packed all-members FP64 arrays.
+__global__ void __launch_bounds__(kThreads) k_ens_store(const EnsMember* __restrict__ mem,
+                                                        const EnsChunk* __restrict__ chunks, int cur,
+                                                        double* __restrict__ P_all, double* __restrict__ S_all,
+                                                        int precision) {
+  const EnsChunk ch = chunks[blockIdx.x];
+  const EnsMember& me = mem[ch.member];
+  const gbf_model& m = me.m;
+  for (unsigned c = ch.begin + threadIdx.x; c < ch.end; c += blockDim.x) {
+    if (precision == GBF_PREC_F64) {
+      P_all[me.off + c] = me.P[cur][c];
+      S_all[me.off + c] = me.S[cur][c];
+    } else {
+      const int j = (int)((c / (unsigned)m.nx) % (unsigned)m.ny);
+      P_all[me.off + c] = gbf_p_hydrostatic(m, j) + (double)me.dPf[cur][c];
+      S_all[me.off + c] = (double)me.Sf[cur][c];
+    }
+  }
+}
+
 __global__ void k_ens_split_to_f64(const gbf_model m, const float* dPf, const float* Sf, double* P, double* S) {
   const GbfGeo g = gbf_geo(m);
   for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < g.n; c += (size_t)gridDim.x * blockDim.x) {
@@ -221,8 +269,9 @@ struct gbf_ensemble {
   EnsMember* d_mem = nullptr;
   std::vector<int4> tiles;
   int4* d_tiles = nullptr;
-  std::vector<EnsChunk> props, flux, bnd;
-  EnsChunk *d_props = nullptr, *d_flux = nullptr, *d_bnd = nullptr;
+  std::vector<EnsChunk> props, flux, bnd, all;
+  EnsChunk *d_props = nullptr, *d_flux = nullptr, *d_bnd = nullptr, *d_all = nullptr;
+  double* d_stage = nullptr;  // packed FP64 P, S of all members (whole-ensemble transfers)
   int nparts = 0;
   double* d_partials = nullptr;
   unsigned *d_counter = nullptr, *d_status = nullptr, *d_mass_count = nullptr;
@@ -276,6 +325,7 @@ int build_lists(gbf_ensemble* e) {
   e->props.clear();
   e->flux.clear();
   e->bnd.clear();
+  e->all.clear();
   const bool split = e->precision != GBF_PREC_F64;
   const int TX = kShapeTX[e->shape], TY = kShapeTY[e->shape];
   for (int r = 0; r < e->n; r++) {
@@ -301,6 +351,7 @@ int build_lists(gbf_ensemble* e) {
     }
     const size_t nb = gbf_boundary_count(g);
     for (unsigned b = 0; b < nb; b += kBoundaryChunk) e->bnd.push_back({r, b, (unsigned)std::min<size_t>(nb, b + kBoundaryChunk)});
+    for (unsigned b = 0; b < g.n; b += kChunkCells) e->all.push_back({r, b, (unsigned)std::min<size_t>(g.n, b + kChunkCells)});
   }
   // device copies (reallocated when they grow)
   auto upload = [&](void** dptr, const void* src, size_t bytes) -> int {
@@ -324,6 +375,7 @@ int build_lists(gbf_ensemble* e) {
     e->nparts = (int)e->flux.size();
   }
   s |= upload((void**)&e->d_bnd, e->bnd.data(), e->bnd.size() * sizeof(EnsChunk));
+  s |= upload((void**)&e->d_all, e->all.data(), e->all.size() * sizeof(EnsChunk));
   s |= upload((void**)&e->d_partials, std::vector<double>(2 * (size_t)std::max(1, e->nparts), 0.0).data(),
               2 * sizeof(double) * std::max(1, e->nparts));
   s |= upload((void**)&e->d_mem, e->h_mem.data(), e->h_mem.size() * sizeof(EnsMember));
@@ -445,6 +497,7 @@ int gbf_ensemble_create(int n, const gbf_model* models, const gbf_cells* host_ce
     e->cells += (long long)nc;
     EnsMember& me = e->h_mem[r];
     memset(&me, 0, sizeof(me));
+    me.off = (unsigned long long)(e->cells - (long long)nc);
     me.m = m;
     me.d = gbf_derive(m);
     me.C = gbf_split_consts(m);
@@ -557,6 +610,44 @@ int gbf_ensemble_upload(gbf_ensemble* e, int r, const double* P1, const double* 
   e->steps = 0;
   GBF_CUDA(cudaMemsetAsync(e->d_status, 0, sizeof(unsigned), e->stream));
   GBF_CUDA(cudaMemsetAsync(e->d_mass_count, 0, sizeof(unsigned), e->stream));
+  return GBF_OK;
+}
+
+// Whole-ensemble transfers through one staging buffer of 2 x cells doubles
+// (allocated on first use): one copy each way for all members and one
+// conversion kernel, instead of per-member copies.
+static int ensure_stage(gbf_ensemble* e) {
+  if (e->d_stage) return GBF_OK;
+  return ens_alloc(e, (void**)&e->d_stage, 2 * sizeof(double) * (size_t)e->cells);
+}
+
+int gbf_ensemble_upload_all(gbf_ensemble* e, const double* P_all, const double* S_all) {
+  if (!e || !P_all || !S_all) return gbf_fail(GBF_ERR_ARG, "gbf_ensemble_upload_all");
+  if (int s = ensure_stage(e)) return s;
+  const size_t b = sizeof(double) * (size_t)e->cells;
+  GBF_CUDA(cudaMemcpyAsync(e->d_stage, P_all, b, cudaMemcpyDefault, e->stream));
+  GBF_CUDA(cudaMemcpyAsync(e->d_stage + e->cells, S_all, b, cudaMemcpyDefault, e->stream));
+  k_ens_load<<<(unsigned)e->all.size(), kThreads, 0, e->stream>>>(e->d_mem, e->d_all, e->cur, e->d_stage,
+                                                                  e->d_stage + e->cells, e->precision);
+  GBF_CUDA(cudaGetLastError());
+  e->steps = 0;
+  GBF_CUDA(cudaMemsetAsync(e->d_status, 0, sizeof(unsigned), e->stream));
+  GBF_CUDA(cudaMemsetAsync(e->d_mass_count, 0, sizeof(unsigned), e->stream));
+  // the host arrays may be reused as soon as this returns
+  GBF_CUDA(cudaStreamSynchronize(e->stream));
+  return GBF_OK;
+}
+
+int gbf_ensemble_download_all(gbf_ensemble* e, double* P_all, double* S_all) {
+  if (!e || !P_all || !S_all) return gbf_fail(GBF_ERR_ARG, "gbf_ensemble_download_all");
+  if (int s = ensure_stage(e)) return s;
+  const size_t b = sizeof(double) * (size_t)e->cells;
+  k_ens_store<<<(unsigned)e->all.size(), kThreads, 0, e->stream>>>(e->d_mem, e->d_all, e->cur, e->d_stage,
+                                                                   e->d_stage + e->cells, e->precision);
+  GBF_CUDA(cudaGetLastError());
+  GBF_CUDA(cudaMemcpyAsync(P_all, e->d_stage, b, cudaMemcpyDefault, e->stream));
+  GBF_CUDA(cudaMemcpyAsync(S_all, e->d_stage + e->cells, b, cudaMemcpyDefault, e->stream));
+  GBF_CUDA(cudaStreamSynchronize(e->stream));
   return GBF_OK;
 }
 

@@ -130,19 +130,7 @@ __global__ void k_split_init(const gbf_model m, const double* P, const double* S
   const GbfGeo g = gbf_geo(m);
   for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < g.n; c += (size_t)gridDim.x * blockDim.x) {
     const int j = (int)((c / g.nx) % g.ny);
-    const double p = P[c], s = S[c];
-    dPf[c] = (float)(p - gbf_p_hydrostatic(m, j));
-    Sf[c] = (float)s;
-    // ro1 (1 - S2), ro2 S2 with P2 = P1 (cpu.cpp:72-73, 224-225)
-    const double m1 = m.ro01 * (1. + m.beta1 * (p - m.P_atm)) * (1. - s);
-    const double m2 = m.ro02 * (1. + m.beta2 * (p - m.P_atm)) * s;
-    if (df) {
-      reinterpret_cast<float2*>(M1)[c] = gbf_df_from_double(m1);
-      reinterpret_cast<float2*>(M2)[c] = gbf_df_from_double(m2);
-    } else {
-      M1[c] = m1;
-      M2[c] = m2;
-    }
+    gbf_split_init_cell(m, P[c], S[c], j, dPf[c], Sf[c], M1, M2, c, df != 0);
   }
 }
 

@@ -349,6 +349,24 @@ __device__ void split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i
   }
 }
 
+// Split state of one cell from FP64 P, S: dP = P - P_hs(j), S in FP32 and
+// the phase masses ro1 (1 - S2), ro2 S2 with P2 = P1 (cpu.cpp:72-73, 224-225)
+// in the wide type of `df`.
+__device__ __forceinline__ void gbf_split_init_cell(const gbf_model& m, double p, double s, int j, float& dPf,
+                                                    float& Sf, double* M1, double* M2, size_t c, bool df) {
+  dPf = (float)(p - gbf_p_hydrostatic(m, j));
+  Sf = (float)s;
+  const double m1 = m.ro01 * (1. + m.beta1 * (p - m.P_atm)) * (1. - s);
+  const double m2 = m.ro02 * (1. + m.beta2 * (p - m.P_atm)) * s;
+  if (df) {
+    reinterpret_cast<float2*>(M1)[c] = gbf_df_from_double(m1);
+    reinterpret_cast<float2*>(M2)[c] = gbf_df_from_double(m2);
+  } else {
+    M1[c] = m1;
+    M2[c] = m2;
+  }
+}
+
 // Value the reference's boundary sweep leaves in P1 (cpu.cpp:366-403), in
 // the dP = P - P_hs(j) representation: copies within a row keep dP, the top
 // (P_atm) and the hydrostatic sides (P_hs) are dP = 0, and the bottom rule

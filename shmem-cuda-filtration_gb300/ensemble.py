@@ -73,6 +73,19 @@ class Ensemble:
             self.upload(r, P, S)
         self.sync()
 
+    def offsets(self):
+        """Start of each member in the packed all-members layout."""
+        return np.concatenate([[0], np.cumsum([m.model.ncells for m in self.members])])
+
+    def upload_all(self, P_all: np.ndarray, S_all: np.ndarray):
+        assert P_all.dtype == np.float64 and S_all.dtype == np.float64
+        assert P_all.size == self.cells and S_all.size == self.cells
+        abi.check(self.lib.gbf_ensemble_upload_all(self.h, P_all.ctypes.data, S_all.ctypes.data), "upload_all")
+
+    def download_all(self, P_all: np.ndarray, S_all: np.ndarray):
+        assert P_all.size == self.cells and S_all.size == self.cells
+        abi.check(self.lib.gbf_ensemble_download_all(self.h, P_all.ctypes.data, S_all.ctypes.data), "download_all")
+
     def step(self, n: int = 1):
         abi.check(self.lib.gbf_ensemble_step(self.h, n), "step")
 

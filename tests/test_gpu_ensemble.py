@@ -133,6 +133,31 @@ def test_ensemble_members_match_oracle(gpu_lib, abi, pkg, O, oracle, p):
     ens.close()
 
 
+@pytest.mark.parametrize("p", PRECS)
+def test_ensemble_whole_transfers_equal_per_member(gpu_lib, abi, pkg, p):
+    """upload_all/download_all (one packed copy each way) equal the per-member
+    calls bit for bit, before and after stepping."""
+    E, _ = mods(pkg)
+    mems = members(abi, gpu_lib)
+    a = E.Ensemble(mems, precision=prec(abi, p))
+    b = E.Ensemble(mems, precision=prec(abi, p))
+    a.upload_initial()
+    off = b.offsets()
+    P_all = np.concatenate([m.initial_state()[0].ravel() for m in mems])
+    S_all = np.concatenate([m.initial_state()[1].ravel() for m in mems])
+    b.upload_all(P_all, S_all)
+    for ens in (a, b):
+        ens.step(7)
+    Pb, Sb = np.empty_like(P_all), np.empty_like(S_all)
+    b.download_all(Pb, Sb)
+    for r, mem in enumerate(mems):
+        sl = slice(off[r], off[r + 1])
+        assert np.array_equal(a.download(r, "P1").ravel(), Pb[sl])
+        assert np.array_equal(a.download(r, "S2").ravel(), Sb[sl])
+    a.close()
+    b.close()
+
+
 def test_ensemble_autotune(gpu_lib, abi, pkg):
     E, _ = mods(pkg)
     mems = members(abi, gpu_lib)
