@@ -60,6 +60,13 @@ template <> struct Wide<false> {
   static __device__ __forceinline__ double tod(T a) { return a; }
   static __device__ __forceinline__ T load(const double* p, size_t i) { return p[i]; }
   static __device__ __forceinline__ void store(double* p, size_t i, T v) { p[i] = v; }
+  // fused forms used by the tile (see the FP32-pair versions)
+  static __device__ __forceinline__ T add_f(T a, float b) { return a + (double)b; }
+  static __device__ __forceinline__ float rho_1mS_minus(T rho, T M, float S) {
+    return (float)((rho - M) - rho * (double)S);
+  }
+  static __device__ __forceinline__ float rhoS_minus(T rho, T M, float S) { return (float)(rho * (double)S - M); }
+  static __device__ __forceinline__ T acc_phi(T acc, float phi, T v) { return acc + (double)phi * v; }
 };
 template <> struct Wide<true> {
   using T = GbfDF;
@@ -83,6 +90,32 @@ template <> struct Wide<true> {
   }
   static __device__ __forceinline__ void store(double* p, size_t i, T v) {
     reinterpret_cast<float2*>(p)[i] = make_float2(v.hi, v.lo);
+  }
+  // pair + FP32: one TwoSum on the high parts, the rest folded into lo
+  static __device__ __forceinline__ T add_f(T a, float b) {
+    GbfDF s = df_two_sum(a.hi, b);
+    return df_fast_two_sum(s.hi, s.lo + a.lo);
+  }
+  // (rho - M) - rho S rounded to FP32, with rho S exact (TwoProduct of the
+  // high part plus the low part's product) and the large terms cancelled
+  // by TwoSum before any rounding: rho (1 - S) - M of cpu.cpp:305.
+  static __device__ __forceinline__ float rho_1mS_minus(T rho, T M, float S) {
+    const GbfDF a = df_two_sum(rho.hi, -M.hi);          // rho - M (high parts, exact)
+    const float p = rho.hi * S, pe = fmaf(rho.hi, S, -p);  // rho.hi S, exact
+    const GbfDF b = df_two_sum(a.hi, -p);
+    return b.hi + (b.lo + ((a.lo - pe) + (rho.lo - M.lo) - rho.lo * S));
+  }
+  // rho S - M rounded to FP32 (cpu.cpp:306 without the small beta terms).
+  static __device__ __forceinline__ float rhoS_minus(T rho, T M, float S) {
+    const float p = rho.hi * S, pe = fmaf(rho.hi, S, -p);
+    const GbfDF b = df_two_sum(p, -M.hi);
+    return b.hi + (b.lo + ((pe - M.lo) + rho.lo * S));
+  }
+  // acc + phi v, the product's rounding error kept
+  static __device__ __forceinline__ T acc_phi(T acc, float phi, T v) {
+    const float p = v.hi * phi, pe = fmaf(v.hi, phi, -p);
+    const GbfDF s = df_two_sum(acc.hi, p);
+    return {s.hi, acc.lo + (s.lo + fmaf(v.lo, phi, pe))};
   }
 };
 
@@ -271,8 +304,8 @@ __device__ void split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i
       const float dtphi = __fdividef(C.dt, phi);
       const float dm1 = -dtphi * f, dm2 = -dtphi * gs;  // FP32 mass increments
       // mass targets T = M + dm (wide), the rate source added exactly
-      const WT T1 = W::add(M1, W::f(dm1));
-      WT T2 = W::add(M2, W::f(dm2));
+      const WT T1 = W::add_f(M1, dm1);
+      WT T2 = W::add_f(M2, dm2);
       float srcf = 0.f;
       if (j == 1 && i >= C.ri0 && i < C.ri0 + C.rn && k >= C.rk0 && k < C.rk0 + C.rn) {
         const WT src = G.phi ? W::div_f(W::c(C.dtsrc_d, C.dtsrc_df), phi) : W::c(C.dtsrc_m_d[md], C.dtsrc_m_df[md]);
@@ -286,8 +319,8 @@ __device__ void split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i
       //   r2 = (rho02 S - M2) + rho02 beta2 (P' + P_k) S - dm2 - src
       float dPk0;
       const float Pk0 = split_Pk(C, md, S0, dPk0);
-      const float r1 = W::tof(W::sub(W::sub(R01, M1), W::mulf(R01, S0))) + C.ro01b1 * Pp * (1.f - S0) - dm1;
-      const float r2 = W::tof(W::sub(W::mulf(R02, S0), M2)) + C.ro02b2 * (Pp + Pk0) * S0 - dm2 - srcf;
+      const float r1 = W::rho_1mS_minus(R01, M1, S0) + C.ro01b1 * Pp * (1.f - S0) - dm1;
+      const float r2 = W::rhoS_minus(R02, M2, S0) + C.ro02b2 * (Pp + Pk0) * S0 - dm2 - srcf;
       // FP32 Newton on d = (dp, ds): r + [F(x + d) - F(x)] = 0, the bracket
       // written in increments so that no large terms cancel. The equations
       // are linear up to terms beta (dp ds, P_k'' ds^2): after the first
@@ -328,11 +361,11 @@ __device__ void split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i
       G.Sn[c] = Sn;
       W::store(G.M1, c, T1);
       // next step's ro2 S2 is taken at P2 = P1, without P_k (cpu.cpp:63 vs :306)
-      W::store(G.M2, c, W::sub(T2, W::f(C.ro02 * C.beta2 * Pk * Sn)));
+      W::store(G.M2, c, W::add_f(T2, -C.ro02b2 * Pk * Sn));
       if (G.mass_partials) {  // phi T in the wide type (phi exact: an FP32 input or a wide table value)
         if (G.phi) {
-          acc.m1 = W::add(acc.m1, W::mulf(T1, phi));
-          acc.m2 = W::add(acc.m2, W::mulf(T2, phi));
+          acc.m1 = W::acc_phi(acc.m1, phi, T1);
+          acc.m2 = W::acc_phi(acc.m2, phi, T2);
         } else {
           const WT phw = W::c(C.m_d[md], C.m_df[md]);
           acc.m1 = W::add(acc.m1, W::mul(phw, T1));
