@@ -193,6 +193,11 @@ class Runner:
         return sum(m.ncells for m in self.members)
 
     @property
+    def uses_tma(self):
+        lib = self.obj.lib
+        return bool(lib.gbf_ensemble_uses_tma(self.obj.h) if self.ensemble else lib.gbf_domain_uses_tma(self.obj.h))
+
+    @property
     def interior_cells(self):
         return sum((m.model.nx - 2) * (m.model.ny - 2) * (m.model.nz - 2) for m in self.members)
 
@@ -260,6 +265,8 @@ def run_ours(args, rank, world):
     lib = pkg.load_library()
     abi = pkg.abi
     torch.cuda.init()
+    if args.no_tma:
+        lib.gbf_set_tma(0)
     cfg, _, p = args.workload.partition("_")
     if p not in PRECISIONS:
         raise SystemExit(f"unknown precision in {args.workload}")
@@ -347,7 +354,8 @@ def run_ours(args, rank, world):
                                                                  max(m.model.dt for m in members)],
                       "l2": f"inputs larger than L2 (state and fields {cells * 40 / 1e9:.1f} GB > 129 MB)",
                       "newton": "FP64: converge-and-exit (tol 1e-11, max 7); split: 2 increment iterations",
-                      "tuning": tuning, "graphs": ensemble},
+                      "tuning": tuning, "graphs": ensemble,
+                      "plane_staging": "TMA" if run.uses_tma else "plain loads"},
            "clocks": clk.summary(), "e2e": e2e, "gpu_launches": run.launches_per_step * args.steps,
            "roofline": roof, "status": lib.gbf_status_string(status).decode()}
     run.close()
@@ -452,6 +460,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-compare", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--no-tma", action="store_true", help="stage split-step planes by plain loads, not TMA")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours" and not args.cube:
         args.warmup = 3

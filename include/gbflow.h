@@ -158,6 +158,7 @@ int gbf_boundary_f64_noalloc(const gbf_model* m, gbf_arrays d_arrays, void* stre
  * stream; gbf_domain_step only enqueues work.
  */
 typedef struct gbf_domain gbf_domain;
+typedef struct gbf_ensemble gbf_ensemble; /* batched grids, declared below */
 /* Per-step outputs that are off by default (the hot path writes P, S only). */
 enum { GBF_OUT_MASS = 1,        /* phase masses after the mass update, every step */
        GBF_OUT_VELOCITY = 2,    /* u1x..u2z of the reference's a2 (FP64 only)      */
@@ -189,6 +190,15 @@ int gbf_domain_set_timing(gbf_domain* d, int on);
 int gbf_domain_kernel_times(gbf_domain* d, double* ms, int* launches, int nkinds);
 int gbf_kernel_kinds(void);
 const char* gbf_kernel_name(int kind);
+/* Split kernels stage their x-y planes by TMA (cp.async.bulk.tensor) where a
+   grid qualifies (FP32 K field, no media table, nx % 4 == 0), else by plain
+   loads. 0 forces plain loads for domains and ensembles created afterwards
+   (and ensemble tile lists rebuilt afterwards); default 1. Negative `on`
+   leaves the setting as it is. Returns the setting in force before the call. */
+int gbf_set_tma(int on);
+/* 1 if the object's split step stages planes by TMA, 0 if by plain loads. */
+int gbf_domain_uses_tma(gbf_domain* d);
+int gbf_ensemble_uses_tma(gbf_ensemble* e);
 
 /* ----------------------------------------------------------- ensembles ----
  * Independent realizations of uneven sizes and parameters, advanced
@@ -199,7 +209,6 @@ const char* gbf_kernel_name(int kind);
  * n entries. Uploads and downloads are per member (FP64 host or device
  * arrays of nx*ny*nz doubles).
  */
-typedef struct gbf_ensemble gbf_ensemble;
 int gbf_ensemble_create(int n, const gbf_model* models, const gbf_cells* host_cells, int precision,
                         gbf_ensemble** out);
 int gbf_ensemble_destroy(gbf_ensemble* e);

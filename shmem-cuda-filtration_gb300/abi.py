@@ -148,6 +148,9 @@ def _declare(lib) -> None:
         "gbf_domain_kernel_times": (c_int, [c_void_p, c_void_p, c_void_p, c_int]),
         "gbf_kernel_kinds": (c_int, []),
         "gbf_kernel_name": (ctypes.c_char_p, [c_int]),
+        "gbf_set_tma": (c_int, [c_int]),
+        "gbf_domain_uses_tma": (c_int, [c_void_p]),
+        "gbf_ensemble_uses_tma": (c_int, [c_void_p]),
         "gbf_ensemble_create": (c_int, [c_int, PM, PC, c_int, ctypes.POINTER(c_void_p)]),
         "gbf_ensemble_destroy": (c_int, [c_void_p]),
         "gbf_ensemble_size": (c_int, [c_void_p]),

@@ -20,7 +20,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", str(INC
 # Per-file extra flags. The one-kernel-per-function path rounds every
 # multiply and add separately like the CPU reference.
 EXTRA = {"gbf_eager.cu": ["-fmad=false"]}
-SOURCES = ["gbf_host.cpp", "gbf_fields.cpp", "gbf_eager.cu", "gbf_f64.cu", "gbf_split.cu", "gbf_domain.cu", "gbf_dropin.cu",
+SOURCES = ["gbf_host.cpp", "gbf_fields.cpp", "gbf_tma.cpp", "gbf_eager.cu", "gbf_f64.cu", "gbf_split.cu", "gbf_domain.cu", "gbf_dropin.cu",
            "gbf_ensemble.cu"]
 
 
@@ -55,7 +55,8 @@ def build(verbose: bool = False) -> pathlib.Path:
         objs = list(ex.map(_compile, srcs))
     lib = BUILD / "libgbflow.so"
     if not lib.exists() or any(o.stat().st_mtime > lib.stat().st_mtime for o in objs):
-        cmd = [nvcc(), *ARCH, "-shared", "-o", str(lib), *map(str, objs), "-cudart", "static"]
+        cmd = [nvcc(), *ARCH, "-shared", "-o", str(lib), *map(str, objs), "-cudart", "static",
+               "-Xlinker", "--no-undefined", "-lpthread", "-ldl", "-lrt"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")

@@ -285,6 +285,7 @@ int gbf_domain_status(gbf_domain* d) {
 }
 
 long long gbf_domain_steps_done(gbf_domain* d) { return d ? d->steps : -1; }
+int gbf_domain_uses_tma(gbf_domain* d) { return d && d->tma ? 1 : 0; }
 
 int gbf_domain_set_timing(gbf_domain* d, int on) {
   if (!d) return gbf_fail(GBF_ERR_ARG, "gbf_domain_set_timing");

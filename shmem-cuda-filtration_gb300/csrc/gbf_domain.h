@@ -65,6 +65,7 @@ struct gbf_domain {
   float *Pf[2] = {nullptr, nullptr}, *Sf[2] = {nullptr, nullptr};
   double *M1 = nullptr, *M2 = nullptr;
   double* split_partials = nullptr;
+  void* tma = nullptr;  // device GbfTmaSet of the split state (NULL: plain loads)
   // mass tracking
   double* mass_partials = nullptr;
   double* mass_hist = nullptr;

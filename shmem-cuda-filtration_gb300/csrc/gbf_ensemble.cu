@@ -50,17 +50,29 @@ constexpr int kChunkCells = 16384, kBoundaryChunk = 4096, kThreads = 256;
 
 // ------------------------------------------------------------ split kernels
 
-template <bool DF, int TX, int TY>
+template <bool DF, int TX, int TY, bool TMA>
 __global__ void __launch_bounds__(TX * TY, 1024 / (TX * TY)) k_ens_split_step(const EnsMember* __restrict__ mem,
                                                                              const int4* __restrict__ tiles,
                                                                              int ntiles, int cur,
                                                                              unsigned* counter, double* partials,
-                                                                             unsigned* status) {
+                                                                             unsigned* status,
+                                                                             const GbfTmaSet* __restrict__ maps) {
   __shared__ GbfSplitPlaneT<TX, TY> pl[2];
   __shared__ GbfSplitConsts Cs;
   __shared__ GbfSplitGrid Gs;
   __shared__ int s_tile;
   constexpr int NT = TX * TY;
+  GbfRawRing<TX, TY>* raw = nullptr;
+  unsigned phases = 0;  // barrier parities of the stages, carried from tile to tile
+  if constexpr (TMA) {
+    __shared__ __align__(128) GbfRawRing<TX, TY> ring;
+    raw = &ring;
+    if (threadIdx.x == 0) {
+      for (int s = 0; s < kTmaStages; s++) gbf_mbar_init(&ring.bar[s], 1);
+      gbf_mbar_fence_init();
+    }
+    __syncthreads();
+  }
   for (;;) {
     if (threadIdx.x == 0) s_tile = (int)atomicAdd(counter, 1u);
     __syncthreads();
@@ -88,7 +100,9 @@ __global__ void __launch_bounds__(TX * TY, 1024 / (TX * TY)) k_ens_split_step(co
     }
     __syncthreads();
     GbfSplitAcc<DF> acc;
-    split_tile<DF, TX, TY>(Cs, Gs, tl.y, tl.z, tl.w & 0xffff, tl.w >> 16, pl, acc);
+    const bool ok = split_tile<DF, TX, TY, TMA>(Cs, Gs, tl.y, tl.z, tl.w & 0xffff, tl.w >> 16, pl, acc, raw,
+                                                TMA ? maps + tl.x : nullptr, cur, &phases);
+    if (!ok) break;  // a plane wait gave up (status set); the whole CTA stops
     if (acc.bad) atomicOr(status, GBF_DEV_NONFINITE);
     if (partials) split_block_mass<DF, NT>(acc, Cs.V, partials + 2 * t);
     __syncthreads();
@@ -272,6 +286,7 @@ struct gbf_ensemble {
   std::vector<EnsChunk> props, flux, bnd, all;
   EnsChunk *d_props = nullptr, *d_flux = nullptr, *d_bnd = nullptr, *d_all = nullptr;
   double* d_stage = nullptr;  // packed FP64 P, S of all members (whole-ensemble transfers)
+  GbfTmaSet* d_maps = nullptr;  // per-member TMA plane maps of the current tile shape (NULL: plain loads)
   int nparts = 0;
   double* d_partials = nullptr;
   unsigned *d_counter = nullptr, *d_status = nullptr, *d_mass_count = nullptr;
@@ -379,19 +394,50 @@ int build_lists(gbf_ensemble* e) {
   s |= upload((void**)&e->d_partials, std::vector<double>(2 * (size_t)std::max(1, e->nparts), 0.0).data(),
               2 * sizeof(double) * std::max(1, e->nparts));
   s |= upload((void**)&e->d_mem, e->h_mem.data(), e->h_mem.size() * sizeof(EnsMember));
+  // TMA plane maps for the tile shape, when every member qualifies (FP32 K
+  // field, no media table, rows of whole 16-byte units)
+  if (e->d_maps) {
+    auto it = std::find(e->owned.begin(), e->owned.end(), (void*)e->d_maps);
+    if (it != e->owned.end()) e->owned.erase(it);
+    cudaFree(e->d_maps);
+    e->d_maps = nullptr;
+  }
+  bool tma = split;
+  for (int r = 0; r < e->n && tma; r++) {
+    const EnsMember& me = e->h_mem[r];
+    tma = me.cells.K && !me.cells.media && gbf_tma_eligible(e->models[r].nx, TX);
+  }
+  if (tma && !s) {
+    std::vector<GbfTmaSet> maps(e->n);
+    int enc = GBF_OK;
+    for (int r = 0; r < e->n && !enc; r++) {
+      const EnsMember& me = e->h_mem[r];
+      const gbf_model& m = e->models[r];
+      for (int b = 0; b < 2; b++) {
+        enc |= gbf_tma_encode_plane(&maps[r].dP[b], me.dPf[b], m.nx, m.ny, m.nz, TX, TY);
+        enc |= gbf_tma_encode_plane(&maps[r].S[b], me.Sf[b], m.nx, m.ny, m.nz, TX, TY);
+      }
+      enc |= gbf_tma_encode_plane(&maps[r].K, me.cells.K, m.nx, m.ny, m.nz, TX, TY);
+    }
+    if (!enc)
+      s |= upload((void**)&e->d_maps, maps.data(), maps.size() * sizeof(GbfTmaSet));
+    else
+      gbf_clear_status();  // plain loads
+  }
   drop_graphs(e);
   return s ? GBF_ERR_CUDA : GBF_OK;
 }
 
 template <bool DF, int TX, int TY>
 int launch_split_step_t(gbf_ensemble* e, double* partials, cudaStream_t st) {
-  auto kern = k_ens_split_step<DF, TX, TY>;
+  const bool tma = e->d_maps != nullptr;
+  auto kern = tma ? k_ens_split_step<DF, TX, TY, true> : k_ens_split_step<DF, TX, TY, false>;
   int per_sm = 0;
   GBF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TX * TY, 0));
   const int blocks = std::max(1, std::min((int)e->tiles.size(), per_sm * gbf_num_sms()));
   e->persistent_blocks = blocks;
   kern<<<blocks, TX * TY, 0, st>>>(e->d_mem, e->d_tiles, (int)e->tiles.size(), e->cur, e->d_counter, partials,
-                                    e->d_status);
+                                    e->d_status, e->d_maps);
   return GBF_OK;
 }
 
@@ -729,6 +775,8 @@ int gbf_ensemble_set_tuning(gbf_ensemble* e, int shape, int edge, int kchunk) {
   if (edge > 0) e->kchunk_by_edge[edge] = kchunk;
   return build_lists(e);
 }
+
+int gbf_ensemble_uses_tma(gbf_ensemble* e) { return e && e->d_maps ? 1 : 0; }
 
 int gbf_ensemble_get_tuning(gbf_ensemble* e, int* shape, int* edges, int* kchunks, int max_entries) {
   if (!e || !shape) return gbf_fail(GBF_ERR_ARG, "gbf_ensemble_get_tuning");

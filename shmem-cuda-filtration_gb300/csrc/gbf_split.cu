@@ -84,9 +84,9 @@ constexpr int kThreads = 256;
 int tiles_x(const GbfSplitConsts& C) { return (C.nx - 2 + kSplitTX - 1) / kSplitTX; }
 int tiles_y(const GbfSplitConsts& C) { return (C.ny - 2 + kSplitTY - 1) / kSplitTY; }
 
-template <bool DF>
+template <bool DF, bool TMA>
 __global__ void __launch_bounds__(kSplitThreads, 4) k_split_step(const GbfSplitConsts C, const GbfSplitGrid G,
-                                                              const int kchunk) {
+                                                              const int kchunk, const GbfTmaSet* maps, int buf) {
   __shared__ GbfSplitPlane pl[2];
   const int ntx = (C.nx - 2 + kSplitTX - 1) / kSplitTX, nty = (C.ny - 2 + kSplitTY - 1) / kSplitTY;
   const int b = blockIdx.x;
@@ -94,7 +94,19 @@ __global__ void __launch_bounds__(kSplitThreads, 4) k_split_step(const GbfSplitC
   const int k0 = 1 + kc * kchunk;
   const int k1 = min(k0 + kchunk, C.nz - 1);
   GbfSplitAcc<DF> acc;
-  split_tile<DF>(C, G, 1 + tx * kSplitTX, 1 + ty * kSplitTY, k0, k1, pl, acc);
+  if constexpr (TMA) {
+    __shared__ __align__(128) GbfRawRing<kSplitTX, kSplitTY> raw;
+    if (threadIdx.x == 0) {
+      for (int s = 0; s < kTmaStages; s++) gbf_mbar_init(&raw.bar[s], 1);
+      gbf_mbar_fence_init();
+    }
+    __syncthreads();
+    unsigned phases = 0;
+    split_tile<DF, kSplitTX, kSplitTY, true>(C, G, 1 + tx * kSplitTX, 1 + ty * kSplitTY, k0, k1, pl, acc, &raw,
+                                             maps, buf, &phases);
+  } else {
+    split_tile<DF>(C, G, 1 + tx * kSplitTX, 1 + ty * kSplitTY, k0, k1, pl, acc);
+  }
   if (acc.bad) atomicOr(G.status, GBF_DEV_NONFINITE);
   if (G.mass_partials) split_block_mass<DF>(acc, C.V, G.mass_partials + 2 * blockIdx.x);
 }
@@ -158,15 +170,22 @@ int gbf_split_kchunk(const GbfSplitConsts& C) {
 }
 
 int gbf_split_launch_domain(const gbf_model& m, const GbfSplitConsts& C, const GbfSplitGrid& G, bool df,
-                            double* mass_out, cudaStream_t st, GbfTimer* tm) {
+                            double* mass_out, cudaStream_t st, GbfTimer* tm, const GbfTmaSet* maps, int buf) {
   const int kchunk = gbf_split_kchunk(C);
   const int nkc = (C.nz - 2 + kchunk - 1) / kchunk;
   const unsigned blocks = (unsigned)(tiles_x(C) * tiles_y(C) * nkc);
   cudaEvent_t e = gbf_timer_begin(tm, st);
-  if (df)
-    k_split_step<true><<<blocks, kSplitThreads, 0, st>>>(C, G, kchunk);
-  else
-    k_split_step<false><<<blocks, kSplitThreads, 0, st>>>(C, G, kchunk);
+  if (maps) {
+    if (df)
+      k_split_step<true, true><<<blocks, kSplitThreads, 0, st>>>(C, G, kchunk, maps, buf);
+    else
+      k_split_step<false, true><<<blocks, kSplitThreads, 0, st>>>(C, G, kchunk, maps, buf);
+  } else {
+    if (df)
+      k_split_step<true, false><<<blocks, kSplitThreads, 0, st>>>(C, G, kchunk, nullptr, 0);
+    else
+      k_split_step<false, false><<<blocks, kSplitThreads, 0, st>>>(C, G, kchunk, nullptr, 0);
+  }
   gbf_timer_end(tm, GBF_K_SPLIT_STEP, e, st);
   e = gbf_timer_begin(tm, st);
   k_split_boundary<<<gbf_grid_for(gbf_boundary_count(gbf_geo(m)), kThreads, 4), kThreads, 0, st>>>(m, G, C.H);
@@ -200,7 +219,25 @@ int gbf_split_alloc(gbf_domain* d) {
   if (!s) s |= gbf_domain_alloc(d, (void**)&d->M2, n * sizeof(double));
   // per-block mass partials of the split step kernel
   if (!s) s |= gbf_domain_alloc(d, (void**)&d->split_partials, 2 * sizeof(double) * gbf_split_blocks(d->m));
-  return s ? GBF_ERR_NOMEM : GBF_OK;
+  if (s) return GBF_ERR_NOMEM;
+  // TMA plane loads: FP32 K field, no media table, rows of whole 16-byte units
+  const gbf_model& m = d->m;
+  if (d->cells.K && !d->cells.media && gbf_tma_eligible(m.nx, kSplitTX)) {
+    GbfTmaSet h;
+    int e = GBF_OK;
+    for (int b = 0; b < 2 && !e; b++) {
+      e |= gbf_tma_encode_plane(&h.dP[b], d->Pf[b], m.nx, m.ny, m.nz, kSplitTX, kSplitTY);
+      e |= gbf_tma_encode_plane(&h.S[b], d->Sf[b], m.nx, m.ny, m.nz, kSplitTX, kSplitTY);
+    }
+    if (!e) e |= gbf_tma_encode_plane(&h.K, d->cells.K, m.nx, m.ny, m.nz, kSplitTX, kSplitTY);
+    if (!e && !gbf_domain_alloc(d, &d->tma, sizeof(GbfTmaSet))) {
+      GBF_CUDA(cudaMemcpy(d->tma, &h, sizeof(GbfTmaSet), cudaMemcpyHostToDevice));
+    } else {
+      d->tma = nullptr;  // plain loads
+      gbf_clear_status();
+    }
+  }
+  return GBF_OK;
 }
 
 int gbf_split_init_state(const gbf_model& m, const double* P_dev, const double* S_dev, float* dPf, float* Sf,
@@ -254,7 +291,8 @@ int gbf_split_step(gbf_domain* d) {
     d->mass_count++;
   }
   const GbfSplitConsts C = gbf_split_consts(d->m);
-  int s = gbf_split_launch_domain(d->m, C, G, d->precision == GBF_PREC_SPLIT_DF, mass_out, d->stream, &d->timer);
+  int s = gbf_split_launch_domain(d->m, C, G, d->precision == GBF_PREC_SPLIT_DF, mass_out, d->stream, &d->timer,
+                                  (const GbfTmaSet*)d->tma, d->cur);
   if (s) return s;
   d->cur = nxt;
   d->steps++;

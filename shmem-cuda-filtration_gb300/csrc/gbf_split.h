@@ -52,5 +52,7 @@ int gbf_split_launches_per_step(gbf_domain* d);
 // FP32 state and wide masses of one grid from FP64 device arrays.
 int gbf_split_init_state(const gbf_model& m, const double* P_dev, const double* S_dev, float* dPf, float* Sf,
                          double* M1, double* M2, bool df, cudaStream_t st);
+struct GbfTmaSet;
+// `maps` (device memory) selects the TMA plane loads for state buffer `buf`.
 int gbf_split_launch_domain(const gbf_model& m, const GbfSplitConsts& C, const GbfSplitGrid& G, bool df,
-                            double* mass_out, cudaStream_t st, GbfTimer* tm);
+                            double* mass_out, cudaStream_t st, GbfTimer* tm, const GbfTmaSet* maps, int buf);

@@ -5,6 +5,7 @@
 #include <math.h>
 
 #include "gbf_split.h"
+#include "gbf_tma.h"
 
 // ------------------------------------------------------------ FP32 pairs
 // Unevaluated sums hi + lo of two FP32 numbers ("double-float", about 48
@@ -139,6 +140,54 @@ struct GbfSplitPlaneT {
 };
 using GbfSplitPlane = GbfSplitPlaneT<kSplitTX, kSplitTY>;
 
+// ----------------------------------------------------- TMA plane staging
+// Ring of raw planes (dP, S, K of one x-y plane of the tile with its halo)
+// filled by cp.async.bulk.tensor; one mbarrier per stage, kStages planes in
+// flight ahead of the plane being built.
+constexpr int kTmaStages = 3;
+template <int TX, int TY>
+struct GbfRawRing {
+  static constexpr int BX = gbf_tma_box_x(TX), HY = TY + 2, N = BX * HY;
+  static constexpr int NP = (N + 31) / 32 * 32;  // each array starts on 128 bytes
+  float v[kTmaStages][3][NP];
+  unsigned long long bar[kTmaStages];
+};
+
+__device__ __forceinline__ unsigned gbf_smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void gbf_mbar_init(unsigned long long* b, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(gbf_smem_u32(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void gbf_mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void gbf_mbar_expect_tx(unsigned long long* b, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(gbf_smem_u32(b)), "r"(bytes) : "memory");
+}
+// Bounded wait for the completion of the barrier's phase `parity`.
+__device__ __forceinline__ bool gbf_mbar_wait(unsigned long long* b, unsigned parity, unsigned max_tries) {
+  for (unsigned it = 0; it < max_tries; ++it) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(gbf_smem_u32(b)), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+// One plane box of a 3-D FP32 tensor into shared memory; the barrier
+// receives the transferred bytes.
+__device__ __forceinline__ void gbf_tma_plane(float* dst, const GbfTensorMap* map, int x, int y, int z,
+                                              unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+      ::"r"(gbf_smem_u32(dst)), "l"(map), "r"(x), "r"(y), "r"(z), "r"(gbf_smem_u32(bar))
+      : "memory");
+}
+constexpr unsigned kTmaWaitTries = 1u << 22;   // a wait gives up after this many try_wait rounds
+constexpr unsigned kTmaDrainTries = 1u << 16;  // after a give-up, per outstanding copy
+
 // FP32 base-2 logarithm and exponential: the hardware approximations
 // (PTX lg2.approx / ex2.approx, flush-to-zero; about 2^-22 relative error),
 // ample for FP32 mobilities and capillary pressures.
@@ -193,9 +242,16 @@ struct GbfSplitAcc {
 
 // One CTA: interior cells [i0, i0+TX) x [j0, j0+TY) of planes [k0, k1); i0,
 // j0, k0 >= 1. `pl` points to two planes of shared memory.
-template <bool DF, int TX = kSplitTX, int TY = kSplitTY>
-__device__ void split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i0, int j0, int k0, int k1,
-                           GbfSplitPlaneT<TX, TY>* pl, GbfSplitAcc<DF>& acc) {
+//
+// TMA = true: the raw planes arrive by cp.async.bulk.tensor into `raw` (maps
+// of the state buffer `buf` and of K; a K field and no media table); the
+// call returns false if a bounded wait on a plane gave up (the status word
+// then carries GBF_DEV_TIMEOUT). `phases` holds the stages' barrier parities
+// across calls. TMA = false: plain loads, one plane prefetched in registers.
+template <bool DF, int TX = kSplitTX, int TY = kSplitTY, bool TMA = false>
+__device__ bool split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i0, int j0, int k0, int k1,
+                           GbfSplitPlaneT<TX, TY>* pl, GbfSplitAcc<DF>& acc, GbfRawRing<TX, TY>* raw = nullptr,
+                           const GbfTmaSet* maps = nullptr, int buf = 0, unsigned* phases = nullptr) {
   using W = Wide<DF>;
   using WT = typename W::T;
   using Sh = GbfSplitShape<TX, TY>;
@@ -256,7 +312,59 @@ __device__ void split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i
     }
   };
 
+  // TMA staging: plane p goes to stage (p - k0) % kTmaStages; thread 0 issues
+  using Ring = GbfRawRing<TX, TY>;
+  auto issue = [&](int p) {
+    if constexpr (TMA) {
+      const int s = (p - k0) % kTmaStages;
+      gbf_mbar_expect_tx(&raw->bar[s], 3u * Ring::N * (unsigned)sizeof(float));
+      gbf_tma_plane(raw->v[s][0], &maps->dP[buf], i0 - 1, j0 - 1, p, &raw->bar[s]);
+      gbf_tma_plane(raw->v[s][1], &maps->S[buf], i0 - 1, j0 - 1, p, &raw->bar[s]);
+      gbf_tma_plane(raw->v[s][2], &maps->K, i0 - 1, j0 - 1, p, &raw->bar[s]);
+    }
+  };
+  auto wait_plane = [&](int p) -> bool {  // every thread; false once the CTA gave up
+    if constexpr (TMA) {
+      const int s = (p - k0) % kTmaStages;
+      const bool ok = gbf_mbar_wait(&raw->bar[s], (*phases >> s) & 1u, kTmaWaitTries);
+      if (__syncthreads_or(!ok)) {
+        // give up: wait (bounded) for the copies in flight, planes p .. p + stages - 1
+        for (int q = p; q <= k1 && q < p + kTmaStages; q++) {
+          const int sq = (q - k0) % kTmaStages;
+          gbf_mbar_wait(&raw->bar[sq], (*phases >> sq) & 1u, kTmaDrainTries);
+          *phases ^= 1u << sq;
+        }
+        if (threadIdx.x == 0) atomicOr(G.status, GBF_DEV_TIMEOUT);
+        return false;
+      }
+      *phases ^= 1u << s;
+    }
+    return true;
+  };
+  auto build_tma = [&](GbfSplitPlane& P, int p) {
+    if constexpr (TMA) {
+      const int s = (p - k0) % kTmaStages;
+#pragma unroll
+      for (int q = 0; q < kSplitSlots; q++) {
+        if (hcol[q] >= 0) {
+          const int ri = (hq[q] / kSplitHX) * Ring::BX + hq[q] % kSplitHX;
+          float L1, L2;
+          const float rp = raw->v[s][0][ri], rs = raw->v[s][1][ri];
+          split_props(C, 0, raw->v[s][2][ri], rp, rs, hj[q], L1, L2);
+          P.dP[hq[q]] = rp;
+          P.S[hq[q]] = rs;
+          P.L1[hq[q]] = L1;
+          P.L2[hq[q]] = L2;
+        }
+      }
+    }
+  };
+
   // prologue: own column at k0 - 1 (registers), plane k0 (shared)
+  if constexpr (TMA) {
+    if (threadIdx.x == 0)
+      for (int q = 0; q < kTmaStages && k0 + q <= k1; q++) issue(k0 + q);
+  }
   float dPm = 0.f, L1m = 0.f, L2m = 0.f;
   if (active) {
     const unsigned c = (unsigned)(i + j * nx) + (unsigned)(k0 - 1) * pln;
@@ -265,18 +373,32 @@ __device__ void split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i
     dPm = G.dP[c];
     split_props(C, md, Kc, dPm, G.S[c], j, L1m, L2m);
   }
-  fetch(k0);
-  build(pl[0]);
-  fetch(k0 + 1);
-  __syncthreads();
+  if constexpr (TMA) {
+    if (!wait_plane(k0)) return false;
+    build_tma(pl[0], k0);
+    __syncthreads();
+    if (threadIdx.x == 0 && k0 + kTmaStages <= k1) issue(k0 + kTmaStages);
+  } else {
+    fetch(k0);
+    build(pl[0]);
+    fetch(k0 + 1);
+    __syncthreads();
+  }
   int cur = 0;
   const WT R01 = W::c(C.ro01_d, C.ro01_df), R02 = W::c(C.ro02_d, C.ro02_df);
   for (int k = k0; k < k1; k++) {
     GbfSplitPlane& Pc = pl[cur];
     GbfSplitPlane& Pn = pl[cur ^ 1];
-    build(Pn);     // plane k + 1 from the prefetched raw values
-    fetch(k + 2);  // prefetch plane k + 2
-    __syncthreads();
+    if constexpr (TMA) {
+      if (!wait_plane(k + 1)) return false;
+      build_tma(Pn, k + 1);  // plane k + 1 from its stage
+      __syncthreads();       // the stage is consumed: refill it with plane k + 1 + stages
+      if (threadIdx.x == 0 && k + 1 + kTmaStages <= k1) issue(k + 1 + kTmaStages);
+    } else {
+      build(Pn);     // plane k + 1 from the prefetched raw values
+      fetch(k + 2);  // prefetch plane k + 2
+      __syncthreads();
+    }
     if (active) {
       const unsigned c = (unsigned)(i + j * nx) + (unsigned)k * pln;
       const int md = G.media ? __ldg(G.media + c) : 0;
@@ -380,6 +502,7 @@ __device__ void split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i
     __syncthreads();
     cur ^= 1;
   }
+  return true;
 }
 
 // Split state of one cell from FP64 P, S: dP = P - P_hs(j), S in FP32 and

@@ -176,3 +176,33 @@ def test_ensemble_autotune(gpu_lib, abi, pkg):
         assert np.array_equal(ens.download(r, "S2"), ref.download(r, "S2"))
     ens.close()
     ref.close()
+
+
+@pytest.mark.parametrize("p", ["split", "split_df"])
+def test_ensemble_tma_staging_equals_plain_loads(gpu_lib, abi, pkg, p):
+    """Persistent ensemble kernel with TMA plane staging (barrier parities
+    carried from tile to tile) against plain loads, every tile shape, with a
+    short k range so that tiles hold fewer planes than the ring has stages."""
+    E, _ = mods(pkg)
+    mems = members(abi, gpu_lib)
+    steps = 12
+    prev = gpu_lib.gbf_set_tma(-1)
+    try:
+        for shape in (0, 1, 2):
+            res = {}
+            for tma in (1, 0):
+                gpu_lib.gbf_set_tma(tma)
+                ens = E.Ensemble(mems, precision=prec(abi, p))
+                ens.set_tuning(shape, 0, 0)
+                ens.set_tuning(-1, 36, 2)
+                assert gpu_lib.gbf_ensemble_uses_tma(ens.h) == tma
+                ens.upload_initial()
+                ens.step(steps)
+                assert ens.status() == abi.GBF_OK
+                res[tma] = [(ens.download(r, "P1"), ens.download(r, "S2")) for r in range(len(mems))]
+                ens.close()
+            for r in range(len(mems)):
+                assert np.array_equal(res[1][r][0], res[0][r][0]), (shape, r)
+                assert np.array_equal(res[1][r][1], res[0][r][1]), (shape, r)
+    finally:
+        gpu_lib.gbf_set_tma(prev)

@@ -114,3 +114,31 @@ def test_split_nonfinite_status(gpu_lib, abi, O, oracle, pkg):
     assert dom.status() == abi.GBF_ERR_NONFINITE
     gpu_lib.gbf_clear_status()
     dom.close()
+
+
+@pytest.mark.parametrize("form", SPLITS)
+def test_tma_staging_equals_plain_loads(gpu_lib, abi, O, oracle, pkg, form):
+    """The TMA-staged split step (planes by cp.async.bulk.tensor into an
+    mbarrier ring) computes every cell from the same inputs as the plain-load
+    step: the results are identical bit for bit."""
+    Domain = domain_cls(pkg)
+    m, st, steps = make_case(abi, O, gpu_lib, "heterogeneous_aniso_24x20x18")
+    assert st.K is not None and m.nx % 4 == 0
+    oracle.initial(st)
+    out = {}
+    prev = gpu_lib.gbf_set_tma(-1)
+    try:
+        for tma in (1, 0):
+            gpu_lib.gbf_set_tma(tma)
+            dom = Domain(m, None, st.K, st.phi, precision=prec(abi, form))  # no media table
+            assert gpu_lib.gbf_domain_uses_tma(dom.h) == tma
+            dom.set_outputs(abi.GBF_OUT_MASS, steps)
+            dom.upload(st["P1"], st["S2"])
+            dom.step(steps)
+            assert dom.status() == abi.GBF_OK
+            out[tma] = (dom.download("P1"), dom.download("S2"), dom.mass_history(steps))
+            dom.close()
+    finally:
+        gpu_lib.gbf_set_tma(prev)
+    for a, b in zip(out[1], out[0]):
+        assert np.array_equal(a, b)
