@@ -196,6 +196,13 @@ const char* gbf_kernel_name(int kind);
    (and ensemble tile lists rebuilt afterwards); default 1. Negative `on`
    leaves the setting as it is. Returns the setting in force before the call. */
 int gbf_set_tma(int on);
+/* Host arrays that are page-locked (cudaHostAlloc, cudaHostRegister) are read
+   and written in place by the FP64 <-> split conversion kernels of the upload
+   and download calls (split-precision domains and ensembles), over the
+   CPU-GPU link, instead of being staged through device memory by copies.
+   0 forces staging; negative leaves the setting as it is; default 1. Returns
+   the setting in force before the call. */
+int gbf_set_host_direct(int on);
 /* 1 if the object's split step stages planes by TMA, 0 if by plain loads. */
 int gbf_domain_uses_tma(gbf_domain* d);
 int gbf_ensemble_uses_tma(gbf_ensemble* e);

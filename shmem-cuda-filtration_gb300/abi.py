@@ -149,6 +149,7 @@ def _declare(lib) -> None:
         "gbf_kernel_kinds": (c_int, []),
         "gbf_kernel_name": (ctypes.c_char_p, [c_int]),
         "gbf_set_tma": (c_int, [c_int]),
+        "gbf_set_host_direct": (c_int, [c_int]),
         "gbf_domain_uses_tma": (c_int, [c_void_p]),
         "gbf_ensemble_uses_tma": (c_int, [c_void_p]),
         "gbf_ensemble_create": (c_int, [c_int, PM, PC, c_int, ctypes.POINTER(c_void_p)]),

@@ -669,12 +669,18 @@ static int ensure_stage(gbf_ensemble* e) {
 
 int gbf_ensemble_upload_all(gbf_ensemble* e, const double* P_all, const double* S_all) {
   if (!e || !P_all || !S_all) return gbf_fail(GBF_ERR_ARG, "gbf_ensemble_upload_all");
-  if (int s = ensure_stage(e)) return s;
-  const size_t b = sizeof(double) * (size_t)e->cells;
-  GBF_CUDA(cudaMemcpyAsync(e->d_stage, P_all, b, cudaMemcpyDefault, e->stream));
-  GBF_CUDA(cudaMemcpyAsync(e->d_stage + e->cells, S_all, b, cudaMemcpyDefault, e->stream));
-  k_ens_load<<<(unsigned)e->all.size(), kThreads, 0, e->stream>>>(e->d_mem, e->d_all, e->cur, e->d_stage,
-                                                                  e->d_stage + e->cells, e->precision);
+  // page-locked host arrays: the conversion kernel reads them in place
+  const double* P = (const double*)gbf_mapped_host(P_all);
+  const double* S = (const double*)gbf_mapped_host(S_all);
+  if (!P || !S) {
+    if (int s = ensure_stage(e)) return s;
+    const size_t b = sizeof(double) * (size_t)e->cells;
+    GBF_CUDA(cudaMemcpyAsync(e->d_stage, P_all, b, cudaMemcpyDefault, e->stream));
+    GBF_CUDA(cudaMemcpyAsync(e->d_stage + e->cells, S_all, b, cudaMemcpyDefault, e->stream));
+    P = e->d_stage;
+    S = e->d_stage + e->cells;
+  }
+  k_ens_load<<<(unsigned)e->all.size(), kThreads, 0, e->stream>>>(e->d_mem, e->d_all, e->cur, P, S, e->precision);
   GBF_CUDA(cudaGetLastError());
   e->steps = 0;
   GBF_CUDA(cudaMemsetAsync(e->d_status, 0, sizeof(unsigned), e->stream));
@@ -686,13 +692,21 @@ int gbf_ensemble_upload_all(gbf_ensemble* e, const double* P_all, const double* 
 
 int gbf_ensemble_download_all(gbf_ensemble* e, double* P_all, double* S_all) {
   if (!e || !P_all || !S_all) return gbf_fail(GBF_ERR_ARG, "gbf_ensemble_download_all");
-  if (int s = ensure_stage(e)) return s;
-  const size_t b = sizeof(double) * (size_t)e->cells;
-  k_ens_store<<<(unsigned)e->all.size(), kThreads, 0, e->stream>>>(e->d_mem, e->d_all, e->cur, e->d_stage,
-                                                                   e->d_stage + e->cells, e->precision);
-  GBF_CUDA(cudaGetLastError());
-  GBF_CUDA(cudaMemcpyAsync(P_all, e->d_stage, b, cudaMemcpyDefault, e->stream));
-  GBF_CUDA(cudaMemcpyAsync(S_all, e->d_stage + e->cells, b, cudaMemcpyDefault, e->stream));
+  // page-locked host arrays: the conversion kernel writes them in place
+  double* P = (double*)gbf_mapped_host(P_all);
+  double* S = (double*)gbf_mapped_host(S_all);
+  if (P && S) {
+    k_ens_store<<<(unsigned)e->all.size(), kThreads, 0, e->stream>>>(e->d_mem, e->d_all, e->cur, P, S, e->precision);
+    GBF_CUDA(cudaGetLastError());
+  } else {
+    if (int s = ensure_stage(e)) return s;
+    const size_t b = sizeof(double) * (size_t)e->cells;
+    k_ens_store<<<(unsigned)e->all.size(), kThreads, 0, e->stream>>>(e->d_mem, e->d_all, e->cur, e->d_stage,
+                                                                     e->d_stage + e->cells, e->precision);
+    GBF_CUDA(cudaGetLastError());
+    GBF_CUDA(cudaMemcpyAsync(P_all, e->d_stage, b, cudaMemcpyDefault, e->stream));
+    GBF_CUDA(cudaMemcpyAsync(S_all, e->d_stage + e->cells, b, cudaMemcpyDefault, e->stream));
+  }
   GBF_CUDA(cudaStreamSynchronize(e->stream));
   return GBF_OK;
 }

@@ -95,6 +95,20 @@ void gbf_timer_free(GbfTimer* t) {
   t->cap = t->used = t->nrec = t->rcap = 0;
 }
 
+// Page-locked host arrays are read and written in place by the conversion
+// kernels (over NVLink-C2C) instead of being staged by copy-engine copies.
+static std::atomic<int> g_host_direct{1};
+
+const void* gbf_mapped_host(const void* p) {
+  if (!p || !g_host_direct.load()) return nullptr;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();  // unregistered memory on older runtimes: not an error here
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 extern "C" {
 
 const char* gbf_kernel_name(int kind) {
@@ -107,6 +121,11 @@ int gbf_kernel_kinds(void) { return GBF_K_COUNT; }
 
 int gbf_last_status(void) { return g_status.load(); }
 void gbf_clear_status(void) { g_status.store(GBF_OK); }
+
+int gbf_set_host_direct(int on) {
+  if (on < 0) return g_host_direct.load();
+  return g_host_direct.exchange(on ? 1 : 0);
+}
 
 const char* gbf_status_string(int s) {
   switch (s) {

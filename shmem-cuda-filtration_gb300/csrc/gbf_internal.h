@@ -15,6 +15,10 @@
 // reference). Returns `s` so callers can `return gbf_fail(...)`.
 int gbf_fail(int s, const char* where);
 int gbf_cuda_check(cudaError_t e, const char* where);
+// Device address of a page-locked host array (cudaHostAlloc, cudaHostRegister)
+// that kernels may access in place; NULL for pageable memory or when direct
+// host access is switched off (gbf_set_host_direct).
+const void* gbf_mapped_host(const void* p);
 #define GBF_CUDA(call) do { cudaError_t e_ = (call); if (e_ != cudaSuccess) return gbf_cuda_check(e_, #call); } while (0)
 
 // ---------------------------------------------------------------- geometry

@@ -252,7 +252,12 @@ int gbf_split_upload(gbf_domain* d, const double* P1, const double* S2, cudaMemc
   const size_t n = gbf_geo(d->m).n, b = n * sizeof(double);
   const double *P = P1, *S = S2;
   double* tmp = nullptr;
-  if (kind == cudaMemcpyHostToDevice) {  // stage through device memory
+  const double* mP = (const double*)gbf_mapped_host(P1);
+  const double* mS = (const double*)gbf_mapped_host(S2);
+  if (kind == cudaMemcpyHostToDevice && mP && mS) {  // page-locked: read in place
+    P = mP;
+    S = mS;
+  } else if (kind == cudaMemcpyHostToDevice) {  // stage through device memory
     GBF_CUDA(cudaMallocAsync((void**)&tmp, 2 * b, d->stream));
     GBF_CUDA(cudaMemcpyAsync(tmp, P1, b, cudaMemcpyHostToDevice, d->stream));
     GBF_CUDA(cudaMemcpyAsync(tmp + n, S2, b, cudaMemcpyHostToDevice, d->stream));
@@ -303,13 +308,16 @@ int gbf_split_download(gbf_domain* d, int field, double* host) {
   const size_t n = gbf_geo(d->m).n, b = n * sizeof(double);
   if (field != GBF_FIELD_P1 && field != GBF_FIELD_S2)
     return gbf_fail(GBF_ERR_STATE, "split precision keeps P1 and S2 only");
-  double* tmp = nullptr;
-  GBF_CUDA(cudaMallocAsync((void**)&tmp, b, d->stream));
+  double* tmp = (double*)gbf_mapped_host(host);  // page-locked: written in place
+  const bool staged = tmp == nullptr;
+  if (staged) GBF_CUDA(cudaMallocAsync((void**)&tmp, b, d->stream));
   k_split_to_f64<<<gbf_grid_for(n, kThreads, 4), kThreads, 0, d->stream>>>(
       d->m, d->Pf[d->cur], d->Sf[d->cur], field == GBF_FIELD_P1 ? tmp : nullptr, field == GBF_FIELD_S2 ? tmp : nullptr);
   GBF_CUDA(cudaGetLastError());
-  GBF_CUDA(cudaMemcpyAsync(host, tmp, b, cudaMemcpyDeviceToHost, d->stream));
-  GBF_CUDA(cudaFreeAsync(tmp, d->stream));
+  if (staged) {
+    GBF_CUDA(cudaMemcpyAsync(host, tmp, b, cudaMemcpyDeviceToHost, d->stream));
+    GBF_CUDA(cudaFreeAsync(tmp, d->stream));
+  }
   GBF_CUDA(cudaStreamSynchronize(d->stream));
   return GBF_OK;
 }

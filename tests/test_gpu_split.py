@@ -142,3 +142,29 @@ def test_tma_staging_equals_plain_loads(gpu_lib, abi, O, oracle, pkg, form):
         gpu_lib.gbf_set_tma(prev)
     for a, b in zip(out[1], out[0]):
         assert np.array_equal(a, b)
+
+
+def test_pinned_transfers_equal_staged(gpu_lib, abi, O, oracle, pkg):
+    """Split-domain upload/download with page-locked host arrays (converted
+    in place by the kernels) against pageable arrays (staged by copies)."""
+    import torch
+    Domain = domain_cls(pkg)
+    m, st, steps = make_case(abi, O, gpu_lib, "c0_rate_hydrostatic_40")
+    oracle.initial(st)
+    res = []
+    for pinned in (True, False):
+        if pinned:
+            P = torch.empty(st["P1"].shape, dtype=torch.float64, pin_memory=True).numpy()
+            S = torch.empty(st["S2"].shape, dtype=torch.float64, pin_memory=True).numpy()
+            P[...], S[...] = st["P1"], st["S2"]
+        else:
+            P, S = st["P1"].copy(), st["S2"].copy()
+        dom = Domain(m, None, None, None, precision=abi.GBF_PREC_SPLIT_DF)
+        dom.upload(P, S)
+        dom.step(10)
+        dom.download("P1", P)
+        dom.download("S2", S)
+        assert dom.status() == abi.GBF_OK
+        res.append((P.copy(), S.copy()))
+        dom.close()
+    assert np.array_equal(res[0][0], res[1][0]) and np.array_equal(res[0][1], res[1][1])
