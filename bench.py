@@ -324,10 +324,9 @@ def run_ours(args, rank, world):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
-            run.upload_all(Pall, Sall)
-            run.step(1)
-            run.download_all(Pall, Sall)
-        api = "gbf_ensemble_upload_all + gbf_ensemble_step(1) + gbf_ensemble_download_all (P1, S2 of every member)"
+            run.advance_host(Pall, Sall, 1)
+        api = ("gbf_ensemble_advance_host(P, S, 1, P, S): every member's P1, S2 host->device, one step, "
+               "device->host, pipelined over member groups")
     else:
         hostP = torch.empty(members[0].model.shape, dtype=torch.float64, pin_memory=True).numpy()
         hostS = torch.empty(members[0].model.shape, dtype=torch.float64, pin_memory=True).numpy()

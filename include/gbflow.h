@@ -231,6 +231,18 @@ int gbf_ensemble_upload(gbf_ensemble* e, int member, const double* P1, const dou
    moves at full link speed). Both return after the transfer completed. */
 int gbf_ensemble_upload_all(gbf_ensemble* e, const double* P_all, const double* S_all);
 int gbf_ensemble_download_all(gbf_ensemble* e, double* P_all, double* S_all);
+/* Host-resident ensemble in one call: upload_all(P_in, S_in), `nsteps`
+   steps, download_all(P_out, S_out), pipelined over groups of members on
+   three streams (host-to-device copies, conversion and steps, device-to-host
+   copies) so that the two copy directions and the steps of different groups
+   overlap. The outputs may alias the inputs. Results equal the three calls
+   bit for bit; phase masses are not recorded (the mass history restarts
+   empty). Overlap needs page-locked host arrays. Returns after the last copy. */
+int gbf_ensemble_advance_host(gbf_ensemble* e, const double* P_in, const double* S_in, int nsteps, double* P_out,
+                              double* S_out);
+/* Member groups of gbf_ensemble_advance_host (1..16, at most one per member);
+   0 (default): about 4M cells per group. */
+int gbf_ensemble_set_pipeline_groups(gbf_ensemble* e, int groups);
 int gbf_ensemble_step(gbf_ensemble* e, int nsteps);
 int gbf_ensemble_download(gbf_ensemble* e, int member, int field, double* host);
 /* [step][member][2] since the last upload. */

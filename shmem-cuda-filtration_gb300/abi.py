@@ -162,6 +162,8 @@ def _declare(lib) -> None:
         "gbf_ensemble_upload": (c_int, [c_void_p, c_int, c_void_p, c_void_p]),
         "gbf_ensemble_upload_all": (c_int, [c_void_p, c_void_p, c_void_p]),
         "gbf_ensemble_download_all": (c_int, [c_void_p, c_void_p, c_void_p]),
+        "gbf_ensemble_advance_host": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_void_p]),
+        "gbf_ensemble_set_pipeline_groups": (c_int, [c_void_p, c_int]),
         "gbf_ensemble_step": (c_int, [c_void_p, c_int]),
         "gbf_ensemble_download": (c_int, [c_void_p, c_int, c_int, c_void_p]),
         "gbf_ensemble_mass_history": (c_int, [c_void_p, c_void_p, c_int, ctypes.POINTER(c_int)]),

@@ -304,6 +304,15 @@ struct gbf_ensemble {
   std::vector<void*> owned;
   long long steps = 0, cells = 0;
   bool uploaded_all = false;
+  // first entry of each member in the packed lists (n + 1 rows; row n = totals)
+  struct ListStarts { int tiles, props, flux, bnd, all; };
+  std::vector<ListStarts> starts;
+  // host-resident pipeline (gbf_ensemble_advance_host): copy streams, events,
+  // one tile counter per member group
+  cudaStream_t s_in = nullptr, s_out = nullptr;
+  std::vector<cudaEvent_t> ev;  // [0] start, [1] end, then 2 per group
+  unsigned* d_gcounter = nullptr;
+  int pipe_groups = 0;  // requested group count (0: automatic)
 };
 
 namespace {
@@ -343,10 +352,16 @@ int build_lists(gbf_ensemble* e) {
   e->all.clear();
   const bool split = e->precision != GBF_PREC_F64;
   const int TX = kShapeTX[e->shape], TY = kShapeTY[e->shape];
+  e->starts.assign(e->n + 1, {});
+  auto mark = [&](int r) {
+    e->starts[r] = {(int)e->tiles.size(), (int)e->props.size(), (int)e->flux.size(), (int)e->bnd.size(),
+                    (int)e->all.size()};
+  };
   for (int r = 0; r < e->n; r++) {
     const gbf_model& m = e->models[r];
     const GbfGeo g = gbf_geo(m);
     EnsMember& me = e->h_mem[r];
+    mark(r);
     if (split) {
       me.part_begin = (int)e->tiles.size();
       const int kc = kchunk_for(e, m);
@@ -368,6 +383,7 @@ int build_lists(gbf_ensemble* e) {
     for (unsigned b = 0; b < nb; b += kBoundaryChunk) e->bnd.push_back({r, b, (unsigned)std::min<size_t>(nb, b + kBoundaryChunk)});
     for (unsigned b = 0; b < g.n; b += kChunkCells) e->all.push_back({r, b, (unsigned)std::min<size_t>(g.n, b + kChunkCells)});
   }
+  mark(e->n);
   // device copies (reallocated when they grow)
   auto upload = [&](void** dptr, const void* src, size_t bytes) -> int {
     if (*dptr) {
@@ -428,25 +444,32 @@ int build_lists(gbf_ensemble* e) {
   return s ? GBF_ERR_CUDA : GBF_OK;
 }
 
+// Tiles [t0, t0 + nt) of the packed list, buffer parity `cur`; the CTAs
+// take tiles from `counter` (zeroed beforehand on the same stream).
+struct TileRange {
+  int t0, nt, cur;
+  unsigned* counter;
+};
+
 template <bool DF, int TX, int TY>
-int launch_split_step_t(gbf_ensemble* e, double* partials, cudaStream_t st) {
+int launch_split_step_t(gbf_ensemble* e, double* partials, cudaStream_t st, const TileRange& tr) {
   const bool tma = e->d_maps != nullptr;
   auto kern = tma ? k_ens_split_step<DF, TX, TY, true> : k_ens_split_step<DF, TX, TY, false>;
   int per_sm = 0;
   GBF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TX * TY, 0));
-  const int blocks = std::max(1, std::min((int)e->tiles.size(), per_sm * gbf_num_sms()));
+  const int blocks = std::max(1, std::min(tr.nt, per_sm * gbf_num_sms()));
   e->persistent_blocks = blocks;
-  kern<<<blocks, TX * TY, 0, st>>>(e->d_mem, e->d_tiles, (int)e->tiles.size(), e->cur, e->d_counter, partials,
-                                    e->d_status, e->d_maps);
+  kern<<<blocks, TX * TY, 0, st>>>(e->d_mem, e->d_tiles + tr.t0, tr.nt, tr.cur, tr.counter,
+                                    partials ? partials + 2 * (size_t)tr.t0 : nullptr, e->d_status, e->d_maps);
   return GBF_OK;
 }
 
-int launch_split_step(gbf_ensemble* e, double* partials, cudaStream_t st) {
+int launch_split_step(gbf_ensemble* e, double* partials, cudaStream_t st, const TileRange& tr) {
   const bool df = e->precision == GBF_PREC_SPLIT_DF;
   switch (e->shape) {
-    case kShape64x4: return df ? launch_split_step_t<true, 64, 4>(e, partials, st) : launch_split_step_t<false, 64, 4>(e, partials, st);
-    case kShape32x4: return df ? launch_split_step_t<true, 32, 4>(e, partials, st) : launch_split_step_t<false, 32, 4>(e, partials, st);
-    default: return df ? launch_split_step_t<true, 32, 8>(e, partials, st) : launch_split_step_t<false, 32, 8>(e, partials, st);
+    case kShape64x4: return df ? launch_split_step_t<true, 64, 4>(e, partials, st, tr) : launch_split_step_t<false, 64, 4>(e, partials, st, tr);
+    case kShape32x4: return df ? launch_split_step_t<true, 32, 4>(e, partials, st, tr) : launch_split_step_t<false, 32, 4>(e, partials, st, tr);
+    default: return df ? launch_split_step_t<true, 32, 8>(e, partials, st, tr) : launch_split_step_t<false, 32, 8>(e, partials, st, tr);
   }
 }
 
@@ -459,7 +482,7 @@ int enqueue_step(gbf_ensemble* e, cudaStream_t st) {
   if (e->precision != GBF_PREC_F64) {
     GBF_CUDA(cudaMemsetAsync(e->d_counter, 0, sizeof(unsigned), st));
     ev = gbf_timer_begin(tm, st);
-    if (int s = launch_split_step(e, partials, st)) return s;
+    if (int s = launch_split_step(e, partials, st, {0, (int)e->tiles.size(), e->cur, e->d_counter})) return s;
     gbf_timer_end(tm, GBF_K_ENS_STEP, ev, st);
     ev = gbf_timer_begin(tm, st);
     k_ens_split_boundary<<<(unsigned)e->bnd.size(), kThreads, 0, st>>>(e->d_mem, e->d_bnd, e->cur);
@@ -512,6 +535,56 @@ int ens_step(gbf_ensemble* e, int nsteps, bool use_graph) {
     }
     e->cur ^= 1;
     e->steps++;
+  }
+  return GBF_OK;
+}
+
+// One step of members [r0, r1) at buffer parity `cur` on `st`: their tiles
+// (or chunks) and faces only, no phase-mass reduction.
+int enqueue_group_step(gbf_ensemble* e, int r0, int r1, int cur, unsigned* counter, cudaStream_t st) {
+  const auto &a = e->starts[r0], &b = e->starts[r1];
+  if (e->precision != GBF_PREC_F64) {
+    GBF_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned), st));
+    if (int s = launch_split_step(e, nullptr, st, {a.tiles, b.tiles - a.tiles, cur, counter})) return s;
+    k_ens_split_boundary<<<(unsigned)(b.bnd - a.bnd), kThreads, 0, st>>>(e->d_mem, e->d_bnd + a.bnd, cur);
+  } else {
+    k_ens_f64_props<<<(unsigned)(b.props - a.props), kThreads, 0, st>>>(e->d_mem, e->d_props + a.props, cur);
+    k_ens_f64_flux_newton<<<(unsigned)(b.flux - a.flux), kThreads, 0, st>>>(e->d_mem, e->d_flux + a.flux, cur,
+                                                                           nullptr, e->d_status);
+    k_ens_f64_boundary<<<(unsigned)(b.bnd - a.bnd), kThreads, 0, st>>>(e->d_mem, e->d_bnd + a.bnd, cur);
+  }
+  cudaError_t err = cudaGetLastError();
+  return err == cudaSuccess ? GBF_OK : gbf_cuda_check(err, "gbf_ensemble group step");
+}
+
+// Member groups of the host-resident pipeline: contiguous ranges of about
+// equal cells, at least kPipeCells cells each, at most kPipeGroups groups.
+constexpr long long kPipeCells = 4ll << 20;
+constexpr int kPipeGroups = 16;
+std::vector<int> pipe_groups(const gbf_ensemble* e) {
+  const long long want = std::max(1ll, std::min<long long>({(long long)kPipeGroups, (long long)e->n,
+                                                              e->pipe_groups > 0 ? e->pipe_groups : e->cells / kPipeCells}));
+  std::vector<int> first = {0};
+  long long acc = 0;
+  for (int r = 0; r < e->n; r++) {
+    acc += (long long)gbf_geo(e->models[r]).n;
+    const long long g = (long long)first.size();  // groups closed so far
+    if (r + 1 < e->n && g < want && acc * want >= g * e->cells) first.push_back(r + 1);
+  }
+  first.push_back(e->n);
+  return first;
+}
+
+int ensure_pipe(gbf_ensemble* e, int groups) {
+  if (!e->s_in) {
+    GBF_CUDA(cudaStreamCreateWithFlags(&e->s_in, cudaStreamNonBlocking));
+    GBF_CUDA(cudaStreamCreateWithFlags(&e->s_out, cudaStreamNonBlocking));
+    if (int s = ens_alloc(e, (void**)&e->d_gcounter, sizeof(unsigned) * kPipeGroups)) return s;
+  }
+  while ((int)e->ev.size() < 2 + 2 * groups) {
+    cudaEvent_t v;
+    GBF_CUDA(cudaEventCreateWithFlags(&v, cudaEventDisableTiming));
+    e->ev.push_back(v);
   }
   return GBF_OK;
 }
@@ -591,8 +664,12 @@ int gbf_ensemble_create(int n, const gbf_model* models, const gbf_cells* host_ce
 int gbf_ensemble_destroy(gbf_ensemble* e) {
   if (!e) return GBF_OK;
   if (e->stream) cudaStreamSynchronize(e->stream);
+  if (e->s_out) cudaStreamSynchronize(e->s_out);
   drop_graphs(e);
   gbf_timer_free(&e->timer);
+  for (cudaEvent_t v : e->ev) cudaEventDestroy(v);
+  if (e->s_in) cudaStreamDestroy(e->s_in);
+  if (e->s_out) cudaStreamDestroy(e->s_out);
   for (void* p : e->owned) cudaFree(p);
   if (e->own_stream && e->stream) cudaStreamDestroy(e->stream);
   delete e;
@@ -708,6 +785,67 @@ int gbf_ensemble_download_all(gbf_ensemble* e, double* P_all, double* S_all) {
     GBF_CUDA(cudaMemcpyAsync(S_all, e->d_stage + e->cells, b, cudaMemcpyDefault, e->stream));
   }
   GBF_CUDA(cudaStreamSynchronize(e->stream));
+  return GBF_OK;
+}
+
+int gbf_ensemble_advance_host(gbf_ensemble* e, const double* P_in, const double* S_in, int nsteps, double* P_out,
+                              double* S_out) {
+  if (!e || !P_in || !S_in || !P_out || !S_out || nsteps < 0)
+    return gbf_fail(GBF_ERR_ARG, "gbf_ensemble_advance_host");
+  if (int s = ensure_stage(e)) return s;
+  const std::vector<int> first = pipe_groups(e);
+  const int G = (int)first.size() - 1;
+  if (int s = ensure_pipe(e, G)) return s;
+  double *stP = e->d_stage, *stS = e->d_stage + e->cells;
+  cudaStream_t cs = e->stream;
+  // everything earlier on the ensemble's stream comes first
+  GBF_CUDA(cudaMemsetAsync(e->d_status, 0, sizeof(unsigned), cs));
+  GBF_CUDA(cudaEventRecord(e->ev[0], cs));
+  GBF_CUDA(cudaStreamWaitEvent(e->s_in, e->ev[0], 0));
+  GBF_CUDA(cudaStreamWaitEvent(e->s_out, e->ev[0], 0));
+  auto span = [&](int g, size_t& off, size_t& bytes) {
+    off = (size_t)e->h_mem[first[g]].off;
+    const size_t end = first[g + 1] < e->n ? (size_t)e->h_mem[first[g + 1]].off : (size_t)e->cells;
+    bytes = (end - off) * sizeof(double);
+  };
+  // host -> device copies of every group, in order, on the input stream
+  for (int g = 0; g < G; g++) {
+    size_t off, bytes;
+    span(g, off, bytes);
+    GBF_CUDA(cudaMemcpyAsync(stP + off, P_in + off, bytes, cudaMemcpyDefault, e->s_in));
+    GBF_CUDA(cudaMemcpyAsync(stS + off, S_in + off, bytes, cudaMemcpyDefault, e->s_in));
+    GBF_CUDA(cudaEventRecord(e->ev[2 + 2 * g], e->s_in));
+  }
+  // per group: load, nsteps steps, store (compute stream); device -> host copy (output stream)
+  const int c0 = e->cur;
+  for (int g = 0; g < G; g++) {
+    const auto &a = e->starts[first[g]], &b = e->starts[first[g + 1]];
+    GBF_CUDA(cudaStreamWaitEvent(cs, e->ev[2 + 2 * g], 0));
+    k_ens_load<<<(unsigned)(b.all - a.all), kThreads, 0, cs>>>(e->d_mem, e->d_all + a.all, c0, stP, stS, e->precision);
+    for (int q = 0; q < nsteps; q++)
+      if (int s = enqueue_group_step(e, first[g], first[g + 1], c0 ^ (q & 1), e->d_gcounter + g, cs)) return s;
+    k_ens_store<<<(unsigned)(b.all - a.all), kThreads, 0, cs>>>(e->d_mem, e->d_all + a.all, c0 ^ (nsteps & 1), stP,
+                                                                 stS, e->precision);
+    GBF_CUDA(cudaGetLastError());
+    GBF_CUDA(cudaEventRecord(e->ev[3 + 2 * g], cs));
+    GBF_CUDA(cudaStreamWaitEvent(e->s_out, e->ev[3 + 2 * g], 0));
+    size_t off, bytes;
+    span(g, off, bytes);
+    GBF_CUDA(cudaMemcpyAsync(P_out + off, stP + off, bytes, cudaMemcpyDefault, e->s_out));
+    GBF_CUDA(cudaMemcpyAsync(S_out + off, stS + off, bytes, cudaMemcpyDefault, e->s_out));
+  }
+  GBF_CUDA(cudaEventRecord(e->ev[1], e->s_out));
+  GBF_CUDA(cudaStreamWaitEvent(cs, e->ev[1], 0));
+  e->cur = c0 ^ (nsteps & 1);
+  e->steps = nsteps;
+  GBF_CUDA(cudaMemsetAsync(e->d_mass_count, 0, sizeof(unsigned), cs));
+  GBF_CUDA(cudaStreamSynchronize(cs));
+  return GBF_OK;
+}
+
+int gbf_ensemble_set_pipeline_groups(gbf_ensemble* e, int groups) {
+  if (!e || groups < 0) return gbf_fail(GBF_ERR_ARG, "gbf_ensemble_set_pipeline_groups");
+  e->pipe_groups = groups;
   return GBF_OK;
 }
 

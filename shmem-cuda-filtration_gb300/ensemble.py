@@ -86,6 +86,17 @@ class Ensemble:
         assert P_all.size == self.cells and S_all.size == self.cells
         abi.check(self.lib.gbf_ensemble_download_all(self.h, P_all.ctypes.data, S_all.ctypes.data), "download_all")
 
+    def advance_host(self, P_in: np.ndarray, S_in: np.ndarray, nsteps: int,
+                     P_out: np.ndarray | None = None, S_out: np.ndarray | None = None):
+        """upload_all + nsteps steps + download_all, pipelined over member
+        groups (outputs default to the inputs, updated in place)."""
+        P_out = P_in if P_out is None else P_out
+        S_out = S_in if S_out is None else S_out
+        for a in (P_in, S_in, P_out, S_out):
+            assert a.dtype == np.float64 and a.size == self.cells and a.flags.c_contiguous
+        abi.check(self.lib.gbf_ensemble_advance_host(self.h, P_in.ctypes.data, S_in.ctypes.data, nsteps,
+                                                     P_out.ctypes.data, S_out.ctypes.data), "advance_host")
+
     def step(self, n: int = 1):
         abi.check(self.lib.gbf_ensemble_step(self.h, n), "step")
 

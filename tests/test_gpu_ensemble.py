@@ -238,3 +238,48 @@ def test_ensemble_pinned_transfers_equal_staged(gpu_lib, abi, pkg, p):
         gpu_lib.gbf_set_host_direct(prev)
     for a, b in zip(out[1], out[0]):
         assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("p", PRECS)
+def test_ensemble_advance_host_equals_three_calls(gpu_lib, abi, pkg, p):
+    """The pipelined host-resident call (member groups over three streams)
+    equals upload_all + step(n) + download_all bit for bit, with separate and
+    with aliased output arrays, and leaves the ensemble in the same state."""
+    import torch
+    E, _ = mods(pkg)
+    mems = members(abi, gpu_lib) * 3  # 12 members: several groups
+    cells = sum(m.model.nx * m.model.ny * m.model.nz for m in mems)
+    P0 = np.concatenate([m.initial_state()[0].ravel() for m in mems])
+    S0 = np.concatenate([m.initial_state()[1].ravel() for m in mems])
+
+    def pinned(a):
+        t = torch.empty(a.shape, dtype=torch.float64, pin_memory=True).numpy()
+        t[...] = a
+        return t
+
+    for nsteps in (1, 4):
+        ref = E.Ensemble(mems, precision=prec(abi, p))
+        ref.upload_all(P0, S0)
+        ref.step(nsteps)
+        Pr, Sr = np.empty_like(P0), np.empty_like(S0)
+        ref.download_all(Pr, Sr)
+        dut = E.Ensemble(mems, precision=prec(abi, p))
+        assert gpu_lib.gbf_ensemble_set_pipeline_groups(dut.h, 5) == abi.GBF_OK
+        Pi, Si = pinned(P0), pinned(S0)
+        Po, So = pinned(np.zeros_like(P0)), pinned(np.zeros_like(S0))
+        dut.advance_host(Pi, Si, nsteps, Po, So)
+        assert dut.status() == abi.GBF_OK
+        assert np.array_equal(Po, Pr) and np.array_equal(So, Sr)
+        assert np.array_equal(Pi, P0)  # inputs untouched
+        # aliased in/out, pageable arrays
+        Pa, Sa = P0.copy(), S0.copy()
+        dut.advance_host(Pa, Sa, nsteps)
+        assert np.array_equal(Pa, Pr) and np.array_equal(Sa, Sr)
+        # the state left behind steps on like the reference ensemble's
+        ref.step(2)
+        dut.step(2)
+        for r in (0, 5, 11):
+            assert np.array_equal(dut.download(r, "S2"), ref.download(r, "S2"))
+            assert np.array_equal(dut.download(r, "P1"), ref.download(r, "P1"))
+        ref.close()
+        dut.close()
