@@ -57,7 +57,7 @@ __global__ void __launch_bounds__(TX * TY, 1024 / (TX * TY)) k_ens_split_step(co
                                                                              unsigned* counter, double* partials,
                                                                              unsigned* status,
                                                                              const GbfTmaSet* __restrict__ maps) {
-  __shared__ GbfSplitPlaneT<TX, TY> pl[2];
+  __shared__ GbfSplitPlaneT<TX, TY> pl[TMA ? 3 : 2];
   __shared__ GbfSplitConsts Cs;
   __shared__ GbfSplitGrid Gs;
   __shared__ int s_tile;
@@ -69,6 +69,7 @@ __global__ void __launch_bounds__(TX * TY, 1024 / (TX * TY)) k_ens_split_step(co
     raw = &ring;
     if (threadIdx.x == 0) {
       for (int s = 0; s < kTmaStages; s++) gbf_mbar_init(&ring.bar[s], 1);
+      for (int s = 0; s < kRowStages; s++) gbf_mbar_init(&ring.mbar[s], 1);
       gbf_mbar_fence_init();
     }
     __syncthreads();
@@ -410,8 +411,8 @@ int build_lists(gbf_ensemble* e) {
   s |= upload((void**)&e->d_partials, std::vector<double>(2 * (size_t)std::max(1, e->nparts), 0.0).data(),
               2 * sizeof(double) * std::max(1, e->nparts));
   s |= upload((void**)&e->d_mem, e->h_mem.data(), e->h_mem.size() * sizeof(EnsMember));
-  // TMA plane maps for the tile shape, when every member qualifies (FP32 K
-  // field, no media table, rows of whole 16-byte units)
+  // TMA maps for the tile shape, when every member qualifies (FP32 K and phi
+  // fields, no media table, rows of whole 16-byte units)
   if (e->d_maps) {
     auto it = std::find(e->owned.begin(), e->owned.end(), (void*)e->d_maps);
     if (it != e->owned.end()) e->owned.erase(it);
@@ -421,7 +422,7 @@ int build_lists(gbf_ensemble* e) {
   bool tma = split;
   for (int r = 0; r < e->n && tma; r++) {
     const EnsMember& me = e->h_mem[r];
-    tma = me.cells.K && !me.cells.media && gbf_tma_eligible(e->models[r].nx, TX);
+    tma = me.cells.K && me.cells.phi && !me.cells.media && gbf_tma_eligible(e->models[r].nx, TX);
   }
   if (tma && !s) {
     std::vector<GbfTmaSet> maps(e->n);
@@ -434,6 +435,9 @@ int build_lists(gbf_ensemble* e) {
         enc |= gbf_tma_encode_plane(&maps[r].S[b], me.Sf[b], m.nx, m.ny, m.nz, TX, TY);
       }
       enc |= gbf_tma_encode_plane(&maps[r].K, me.cells.K, m.nx, m.ny, m.nz, TX, TY);
+      enc |= gbf_tma_encode_rows(&maps[r].M1, me.M1, 8, m.nx, m.ny, m.nz, TX, TY);
+      enc |= gbf_tma_encode_rows(&maps[r].M2, me.M2, 8, m.nx, m.ny, m.nz, TX, TY);
+      enc |= gbf_tma_encode_rows(&maps[r].phi, me.cells.phi, 4, m.nx, m.ny, m.nz, TX, TY);
     }
     if (!enc)
       s |= upload((void**)&e->d_maps, maps.data(), maps.size() * sizeof(GbfTmaSet));

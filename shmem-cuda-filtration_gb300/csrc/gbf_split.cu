@@ -87,7 +87,7 @@ int tiles_y(const GbfSplitConsts& C) { return (C.ny - 2 + kSplitTY - 1) / kSplit
 template <bool DF, bool TMA>
 __global__ void __launch_bounds__(kSplitThreads, 4) k_split_step(const GbfSplitConsts C, const GbfSplitGrid G,
                                                               const int kchunk, const GbfTmaSet* maps, int buf) {
-  __shared__ GbfSplitPlane pl[2];
+  __shared__ GbfSplitPlane pl[TMA ? 3 : 2];
   const int ntx = (C.nx - 2 + kSplitTX - 1) / kSplitTX, nty = (C.ny - 2 + kSplitTY - 1) / kSplitTY;
   const int b = blockIdx.x;
   const int tx = b % ntx, ty = (b / ntx) % nty, kc = b / (ntx * nty);
@@ -98,6 +98,7 @@ __global__ void __launch_bounds__(kSplitThreads, 4) k_split_step(const GbfSplitC
     __shared__ __align__(128) GbfRawRing<kSplitTX, kSplitTY> raw;
     if (threadIdx.x == 0) {
       for (int s = 0; s < kTmaStages; s++) gbf_mbar_init(&raw.bar[s], 1);
+      for (int s = 0; s < kRowStages; s++) gbf_mbar_init(&raw.mbar[s], 1);
       gbf_mbar_fence_init();
     }
     __syncthreads();
@@ -220,9 +221,9 @@ int gbf_split_alloc(gbf_domain* d) {
   // per-block mass partials of the split step kernel
   if (!s) s |= gbf_domain_alloc(d, (void**)&d->split_partials, 2 * sizeof(double) * gbf_split_blocks(d->m));
   if (s) return GBF_ERR_NOMEM;
-  // TMA plane loads: FP32 K field, no media table, rows of whole 16-byte units
+  // TMA plane loads: FP32 K and phi fields, no media table, rows of whole 16-byte units
   const gbf_model& m = d->m;
-  if (d->cells.K && !d->cells.media && gbf_tma_eligible(m.nx, kSplitTX)) {
+  if (d->cells.K && d->cells.phi && !d->cells.media && gbf_tma_eligible(m.nx, kSplitTX)) {
     GbfTmaSet h;
     int e = GBF_OK;
     for (int b = 0; b < 2 && !e; b++) {
@@ -230,6 +231,9 @@ int gbf_split_alloc(gbf_domain* d) {
       e |= gbf_tma_encode_plane(&h.S[b], d->Sf[b], m.nx, m.ny, m.nz, kSplitTX, kSplitTY);
     }
     if (!e) e |= gbf_tma_encode_plane(&h.K, d->cells.K, m.nx, m.ny, m.nz, kSplitTX, kSplitTY);
+    if (!e) e |= gbf_tma_encode_rows(&h.M1, d->M1, 8, m.nx, m.ny, m.nz, kSplitTX, kSplitTY);
+    if (!e) e |= gbf_tma_encode_rows(&h.M2, d->M2, 8, m.nx, m.ny, m.nz, kSplitTX, kSplitTY);
+    if (!e) e |= gbf_tma_encode_rows(&h.phi, d->cells.phi, 4, m.nx, m.ny, m.nz, kSplitTX, kSplitTY);
     if (!e && !gbf_domain_alloc(d, &d->tma, sizeof(GbfTmaSet))) {
       GBF_CUDA(cudaMemcpy(d->tma, &h, sizeof(GbfTmaSet), cudaMemcpyHostToDevice));
     } else {

@@ -141,16 +141,26 @@ struct GbfSplitPlaneT {
 using GbfSplitPlane = GbfSplitPlaneT<kSplitTX, kSplitTY>;
 
 // ----------------------------------------------------- TMA plane staging
-// Ring of raw planes (dP, S, K of one x-y plane of the tile with its halo)
-// filled by cp.async.bulk.tensor; one mbarrier per stage, kStages planes in
-// flight ahead of the plane being built.
-constexpr int kTmaStages = 3;
+// Two rings filled by cp.async.bulk.tensor, one mbarrier per stage:
+//  - halo planes: dP, S, K of one x-y plane of the tile with its 1-cell halo,
+//    up to kTmaStages planes ahead of the plane being built;
+//  - interior rows: M1, M2 (8 bytes a cell) and phi of the plane being
+//    updated, one plane ahead (kRowStages stages).
+// Every array starts on a 128-byte boundary.
+constexpr int kTmaStages = 3, kRowStages = 2;
 template <int TX, int TY>
 struct GbfRawRing {
   static constexpr int BX = gbf_tma_box_x(TX), HY = TY + 2, N = BX * HY;
-  static constexpr int NP = (N + 31) / 32 * 32;  // each array starts on 128 bytes
+  static constexpr int NP = (N + 31) / 32 * 32;
+  static constexpr int MX = gbf_tma_rows_x8(TX), NM = (MX * TY + 15) / 16 * 16;  // 8-byte elements
+  static constexpr int FX = gbf_tma_box_x(TX), NF = (FX * TY + 31) / 32 * 32;   // FP32 elements
+  // bytes that complete one stage of each ring (whole boxes, also where they overhang the grid)
+  static constexpr unsigned kHaloBytes = 3u * N * 4u;
+  static constexpr unsigned kRowsBytes = 2u * MX * TY * 8u + (unsigned)FX * TY * 4u;
   float v[kTmaStages][3][NP];
-  unsigned long long bar[kTmaStages];
+  double m1[kRowStages][NM], m2[kRowStages][NM];
+  float phi[kRowStages][NF];
+  unsigned long long bar[kTmaStages], mbar[kRowStages];
 };
 
 __device__ __forceinline__ unsigned gbf_smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
@@ -178,7 +188,7 @@ __device__ __forceinline__ bool gbf_mbar_wait(unsigned long long* b, unsigned pa
 }
 // One plane box of a 3-D FP32 tensor into shared memory; the barrier
 // receives the transferred bytes.
-__device__ __forceinline__ void gbf_tma_plane(float* dst, const GbfTensorMap* map, int x, int y, int z,
+__device__ __forceinline__ void gbf_tma_plane(void* dst, const GbfTensorMap* map, int x, int y, int z,
                                               unsigned long long* bar) {
   asm volatile(
       "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
@@ -243,11 +253,12 @@ struct GbfSplitAcc {
 // One CTA: interior cells [i0, i0+TX) x [j0, j0+TY) of planes [k0, k1); i0,
 // j0, k0 >= 1. `pl` points to two planes of shared memory.
 //
-// TMA = true: the raw planes arrive by cp.async.bulk.tensor into `raw` (maps
-// of the state buffer `buf` and of K; a K field and no media table); the
-// call returns false if a bounded wait on a plane gave up (the status word
-// then carries GBF_DEV_TIMEOUT). `phases` holds the stages' barrier parities
-// across calls. TMA = false: plain loads, one plane prefetched in registers.
+// TMA = true: halo planes (dP, S of the state buffer `buf`, K) and interior
+// rows (M1, M2, phi) arrive by cp.async.bulk.tensor into the rings of `raw`
+// (a K and a phi field, no media table); `pl` holds three plane buffers. The
+// call returns false if a bounded wait gave up (the status word then carries
+// GBF_DEV_TIMEOUT). `phases` holds the barrier parities across calls.
+// TMA = false: plain loads, one plane prefetched in registers, two buffers.
 template <bool DF, int TX = kSplitTX, int TY = kSplitTY, bool TMA = false>
 __device__ bool split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i0, int j0, int k0, int k1,
                            GbfSplitPlaneT<TX, TY>* pl, GbfSplitAcc<DF>& acc, GbfRawRing<TX, TY>* raw = nullptr,
@@ -312,34 +323,58 @@ __device__ bool split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i
     }
   };
 
-  // TMA staging: plane p goes to stage (p - k0) % kTmaStages; thread 0 issues
+  // TMA staging. Plane p uses stage (p - k0) % kTmaStages of the halo ring,
+  // stage (p - k0) % kRowStages of the rows ring and plane buffer
+  // pl[(p - k0) % 3]. Thread 0 issues the copies; every thread
+  // tracks the stages in flight (`pend`: bits 0.. halo ring, bits 8.. rows
+  // ring) and the barrier parities (`*phases`, same bit layout), so that a
+  // give-up can wait out the copies still in flight.
   using Ring = GbfRawRing<TX, TY>;
-  auto issue = [&](int p) {
+  unsigned pend = 0;
+  auto issue = [&](int p) {  // halo planes of plane p
     if constexpr (TMA) {
       const int s = (p - k0) % kTmaStages;
-      gbf_mbar_expect_tx(&raw->bar[s], 3u * Ring::N * (unsigned)sizeof(float));
-      gbf_tma_plane(raw->v[s][0], &maps->dP[buf], i0 - 1, j0 - 1, p, &raw->bar[s]);
-      gbf_tma_plane(raw->v[s][1], &maps->S[buf], i0 - 1, j0 - 1, p, &raw->bar[s]);
-      gbf_tma_plane(raw->v[s][2], &maps->K, i0 - 1, j0 - 1, p, &raw->bar[s]);
+      if (threadIdx.x == 0) {
+        gbf_mbar_expect_tx(&raw->bar[s], Ring::kHaloBytes);
+        gbf_tma_plane(raw->v[s][0], &maps->dP[buf], i0 - 1, j0 - 1, p, &raw->bar[s]);
+        gbf_tma_plane(raw->v[s][1], &maps->S[buf], i0 - 1, j0 - 1, p, &raw->bar[s]);
+        gbf_tma_plane(raw->v[s][2], &maps->K, i0 - 1, j0 - 1, p, &raw->bar[s]);
+      }
+      pend |= 1u << s;
     }
   };
-  auto wait_plane = [&](int p) -> bool {  // every thread; false once the CTA gave up
+  auto issue_rows = [&](int p) {  // M1, M2, phi rows of plane p
     if constexpr (TMA) {
-      const int s = (p - k0) % kTmaStages;
-      const bool ok = gbf_mbar_wait(&raw->bar[s], (*phases >> s) & 1u, kTmaWaitTries);
-      if (__syncthreads_or(!ok)) {
-        // give up: wait (bounded) for the copies in flight, planes p .. p + stages - 1
-        for (int q = p; q <= k1 && q < p + kTmaStages; q++) {
-          const int sq = (q - k0) % kTmaStages;
-          gbf_mbar_wait(&raw->bar[sq], (*phases >> sq) & 1u, kTmaDrainTries);
-          *phases ^= 1u << sq;
-        }
-        if (threadIdx.x == 0) atomicOr(G.status, GBF_DEV_TIMEOUT);
-        return false;
+      const int s = (p - k0) % kRowStages;
+      if (threadIdx.x == 0) {
+        gbf_mbar_expect_tx(&raw->mbar[s], Ring::kRowsBytes);
+        gbf_tma_plane(raw->m1[s], &maps->M1, i0 - 1, j0, p, &raw->mbar[s]);
+        gbf_tma_plane(raw->m2[s], &maps->M2, i0 - 1, j0, p, &raw->mbar[s]);
+        gbf_tma_plane(raw->phi[s], &maps->phi, i0 - 1, j0, p, &raw->mbar[s]);
       }
-      *phases ^= 1u << s;
+      pend |= 1u << (8 + s);
+    }
+  };
+  auto wait_bit = [&](int bit) -> bool {  // bounded wait for the stage of `bit`
+    if constexpr (TMA) {
+      unsigned long long* b = bit < 8 ? &raw->bar[bit] : &raw->mbar[bit - 8];
+      if (!gbf_mbar_wait(b, (*phases >> bit) & 1u, kTmaWaitTries)) return false;
+      *phases ^= 1u << bit;
+      pend &= ~(1u << bit);
     }
     return true;
+  };
+  auto give_up = [&]() {  // after a wait gave up somewhere in the CTA
+    if constexpr (TMA) {
+      for (int bit = 0; bit < 16; bit++)
+        if ((pend >> bit) & 1u) {
+          unsigned long long* b = bit < 8 ? &raw->bar[bit] : &raw->mbar[bit - 8];
+          gbf_mbar_wait(b, (*phases >> bit) & 1u, kTmaDrainTries);
+          *phases ^= 1u << bit;
+        }
+      pend = 0;
+      if (threadIdx.x == 0) atomicOr(G.status, GBF_DEV_TIMEOUT);
+    }
   };
   auto build_tma = [&](GbfSplitPlane& P, int p) {
     if constexpr (TMA) {
@@ -362,8 +397,8 @@ __device__ bool split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i
 
   // prologue: own column at k0 - 1 (registers), plane k0 (shared)
   if constexpr (TMA) {
-    if (threadIdx.x == 0)
-      for (int q = 0; q < kTmaStages && k0 + q <= k1; q++) issue(k0 + q);
+    for (int q = 0; q < kTmaStages && k0 + q <= k1; q++) issue(k0 + q);
+    for (int q = 0; q < kRowStages && k0 + q < k1; q++) issue_rows(k0 + q);
   }
   float dPm = 0.f, L1m = 0.f, L2m = 0.f;
   if (active) {
@@ -374,10 +409,13 @@ __device__ bool split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i
     split_props(C, md, Kc, dPm, G.S[c], j, L1m, L2m);
   }
   if constexpr (TMA) {
-    if (!wait_plane(k0)) return false;
-    build_tma(pl[0], k0);
-    __syncthreads();
-    if (threadIdx.x == 0 && k0 + kTmaStages <= k1) issue(k0 + kTmaStages);
+    const bool ok = wait_bit(0);
+    if (ok) build_tma(pl[0], k0);
+    if (__syncthreads_or(!ok)) {
+      give_up();
+      return false;
+    }
+    if (k0 + kTmaStages <= k1) issue(k0 + kTmaStages);
   } else {
     fetch(k0);
     build(pl[0]);
@@ -386,24 +424,39 @@ __device__ bool split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i
   }
   int cur = 0;
   const WT R01 = W::c(C.ro01_d, C.ro01_df), R02 = W::c(C.ro02_d, C.ro02_df);
+  const int mi = ty * Ring::MX + tx + 1, fi = ty * Ring::FX + tx + 1;  // own cell in the rows boxes
   for (int k = k0; k < k1; k++) {
-    GbfSplitPlane& Pc = pl[cur];
-    GbfSplitPlane& Pn = pl[cur ^ 1];
+    int sc = 0, sr = 0;  // plane buffer and rows stage of plane k (TMA)
     if constexpr (TMA) {
-      if (!wait_plane(k + 1)) return false;
-      build_tma(Pn, k + 1);  // plane k + 1 from its stage
-      __syncthreads();       // the stage is consumed: refill it with plane k + 1 + stages
-      if (threadIdx.x == 0 && k + 1 + kTmaStages <= k1) issue(k + 1 + kTmaStages);
+      // one barrier per plane: plane k + 1 built into its own buffer (three
+      // buffers rotate, so no thread can still be reading the one written)
+      sc = (k - k0) % kTmaStages;
+      sr = (k - k0) % kRowStages;
+      const int sn = (k + 1 - k0) % kTmaStages;
+      bool ok = wait_bit(sn);
+      ok = ok && wait_bit(8 + sr);
+      if (ok) build_tma(pl[sn], k + 1);
+      if (__syncthreads_or(!ok)) {
+        give_up();
+        return false;
+      }
+      // halo stage sn was consumed by the build above; the rows stage of
+      // plane k - 1 (= that of plane k + 1) by the previous plane's update
+      if (k + 1 + kTmaStages <= k1) issue(k + 1 + kTmaStages);
+      if (k > k0 && k + 1 < k1) issue_rows(k + 1);
     } else {
-      build(Pn);     // plane k + 1 from the prefetched raw values
-      fetch(k + 2);  // prefetch plane k + 2
+      build(pl[cur ^ 1]);  // plane k + 1 from the prefetched raw values
+      fetch(k + 2);        // prefetch plane k + 2
       __syncthreads();
     }
+    GbfSplitPlane& Pc = TMA ? pl[sc] : pl[cur];
+    GbfSplitPlane& Pn = TMA ? pl[(sc + 1) % kTmaStages] : pl[cur ^ 1];
     if (active) {
       const unsigned c = (unsigned)(i + j * nx) + (unsigned)k * pln;
-      const int md = G.media ? __ldg(G.media + c) : 0;
-      const float phi = G.phi ? __ldg(G.phi + c) : C.m[md];
-      const WT M1 = W::load(G.M1, c), M2 = W::load(G.M2, c);
+      const int md = (!TMA && G.media) ? __ldg(G.media + c) : 0;
+      const float phi = TMA ? raw->phi[sr][fi] : (G.phi ? __ldg(G.phi + c) : C.m[md]);
+      const WT M1 = TMA ? W::load(raw->m1[sr], mi) : W::load(G.M1, c);
+      const WT M2 = TMA ? W::load(raw->m2[sr], mi) : W::load(G.M2, c);
       const float dPc = Pc.dP[hc], S0 = Pc.S[hc], L1c = Pc.L1[hc], L2c = Pc.L2[hc];
       const float dPp = Pn.dP[hc], L1p = Pn.L1[hc], L2p = Pn.L2[hc];
       // face potentials relative to the hydrostatic profile (P2 = P1)
@@ -499,8 +552,10 @@ __device__ bool split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i
       L1m = L1c;
       L2m = L2c;
     }
-    __syncthreads();
-    cur ^= 1;
+    if constexpr (!TMA) {
+      __syncthreads();
+      cur ^= 1;
+    }
   }
   return true;
 }

@@ -42,23 +42,36 @@ bool gbf_tma_enabled() { return g_tma_on.load() != 0; }
 // (TX % 4 == 0; tiles start at x = tile * TX).
 bool gbf_tma_eligible(int nx, int TX) { return gbf_tma_enabled() && nx % 4 == 0 && TX % 4 == 0 && encoder() != nullptr; }
 
-int gbf_tma_encode_plane(void* map_out, const float* base, int nx, int ny, int nz, int TX, int TY) {
+namespace {
+// A 3-D map {nx, ny, nz} of `eb`-byte elements with a {bx, by, 1} box.
+int encode(void* map_out, const void* base, int eb, int nx, int ny, int nz, int bx, int by) {
   PFN_cuTensorMapEncodeTiled_v12000 enc = encoder();
   if (!enc) return gbf_fail(GBF_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
-  if (((uintptr_t)base & 15) != 0 || nx % 4 != 0 || TX % 4 != 0)
-    return gbf_fail(GBF_ERR_ARG, "TMA plane map: alignment");
+  if (!base || ((uintptr_t)base & 15) != 0 || ((size_t)nx * eb) % 16 != 0 || (eb != 4 && eb != 8))
+    return gbf_fail(GBF_ERR_ARG, "TMA map: alignment");
+  if (bx > 256 || by > 256 || ((size_t)bx * eb) % 16 != 0) return gbf_fail(GBF_ERR_ARG, "TMA map: box");
   const cuuint64_t dims[3] = {(cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)nz};
-  const cuuint64_t strides[2] = {(cuuint64_t)nx * 4, (cuuint64_t)nx * ny * 4};  // bytes, dims 1 and 2
-  const cuuint32_t box[3] = {(cuuint32_t)gbf_tma_box_x(TX), (cuuint32_t)(TY + 2), 1};
+  const cuuint64_t strides[2] = {(cuuint64_t)nx * eb, (cuuint64_t)nx * ny * eb};  // bytes, dims 1 and 2
+  const cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)by, 1};
   const cuuint32_t elem[3] = {1, 1, 1};
-  if (box[0] > 256 || box[1] > 256 || (box[0] * 4) % 16 != 0) return gbf_fail(GBF_ERR_ARG, "TMA plane map: box");
   CUtensorMap m;
-  CUresult r = enc(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void*)base, dims, strides, box, elem,
-                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  CUresult r = enc(&m, eb == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void*)base,
+                   dims, strides, box, elem, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                   CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return gbf_fail(GBF_ERR_CUDA, "cuTensorMapEncodeTiled");
   memcpy(map_out, &m, sizeof(m));
   return GBF_OK;
+}
+}  // namespace
+
+int gbf_tma_encode_plane(void* map_out, const float* base, int nx, int ny, int nz, int TX, int TY) {
+  if (TX % 4 != 0) return gbf_fail(GBF_ERR_ARG, "TMA plane map: tile width");
+  return encode(map_out, base, 4, nx, ny, nz, gbf_tma_box_x(TX), TY + 2);
+}
+
+int gbf_tma_encode_rows(void* map_out, const void* base, int elem_bytes, int nx, int ny, int nz, int TX, int TY) {
+  if (TX % 4 != 0) return gbf_fail(GBF_ERR_ARG, "TMA rows map: tile width");
+  return encode(map_out, base, elem_bytes, nx, ny, nz, elem_bytes == 8 ? gbf_tma_rows_x8(TX) : gbf_tma_box_x(TX), TY);
 }
 
 extern "C" int gbf_set_tma(int on) {
