@@ -57,7 +57,7 @@ __global__ void __launch_bounds__(TX * TY, 1024 / (TX * TY)) k_ens_split_step(co
                                                                              unsigned* counter, double* partials,
                                                                              unsigned* status,
                                                                              const GbfTmaSet* __restrict__ maps) {
-  __shared__ GbfSplitPlaneT<TX, TY> pl[TMA ? 3 : 2];
+  __shared__ GbfSplitPlaneT<TX, TY, gbf_plane_pitch<TX, TMA>()> pl[TMA ? 3 : 2];
   __shared__ GbfSplitConsts Cs;
   __shared__ GbfSplitGrid Gs;
   __shared__ int s_tile;
@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(TX * TY, 1024 / (TX * TY)) k_ens_split_step(co
     raw = &ring;
     if (threadIdx.x == 0) {
       for (int s = 0; s < kTmaStages; s++) gbf_mbar_init(&ring.bar[s], 1);
-      for (int s = 0; s < kRowStages; s++) gbf_mbar_init(&ring.mbar[s], 1);
+      for (int s = 0; s < GbfRawRing<TX, TY>::RS; s++) gbf_mbar_init(&ring.mbar[s], 1);
       gbf_mbar_fence_init();
     }
     __syncthreads();

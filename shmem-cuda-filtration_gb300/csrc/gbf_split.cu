@@ -87,7 +87,7 @@ int tiles_y(const GbfSplitConsts& C) { return (C.ny - 2 + kSplitTY - 1) / kSplit
 template <bool DF, bool TMA>
 __global__ void __launch_bounds__(kSplitThreads, 4) k_split_step(const GbfSplitConsts C, const GbfSplitGrid G,
                                                               const int kchunk, const GbfTmaSet* maps, int buf) {
-  __shared__ GbfSplitPlane pl[TMA ? 3 : 2];
+  __shared__ GbfSplitPlaneT<kSplitTX, kSplitTY, gbf_plane_pitch<kSplitTX, TMA>()> pl[TMA ? 3 : 2];
   const int ntx = (C.nx - 2 + kSplitTX - 1) / kSplitTX, nty = (C.ny - 2 + kSplitTY - 1) / kSplitTY;
   const int b = blockIdx.x;
   const int tx = b % ntx, ty = (b / ntx) % nty, kc = b / (ntx * nty);
@@ -98,7 +98,7 @@ __global__ void __launch_bounds__(kSplitThreads, 4) k_split_step(const GbfSplitC
     __shared__ __align__(128) GbfRawRing<kSplitTX, kSplitTY> raw;
     if (threadIdx.x == 0) {
       for (int s = 0; s < kTmaStages; s++) gbf_mbar_init(&raw.bar[s], 1);
-      for (int s = 0; s < kRowStages; s++) gbf_mbar_init(&raw.mbar[s], 1);
+      for (int s = 0; s < GbfRawRing<kSplitTX, kSplitTY>::RS; s++) gbf_mbar_init(&raw.mbar[s], 1);
       gbf_mbar_fence_init();
     }
     __syncthreads();

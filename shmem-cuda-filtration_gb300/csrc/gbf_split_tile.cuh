@@ -122,20 +122,25 @@ template <> struct Wide<true> {
 
 // ------------------------------------------------------------- tile shape
 // A CTA of TX x TY threads owns a TX x TY column tile (one column per thread).
-template <int TX, int TY>
+// The halo plane (TX + 2 columns, TY + 2 rows) is stored with a row pitch PX
+// >= TX + 2: TX + 2 for the plain-load tile, the TMA box width for the TMA
+// tile (so that a halo element has the same index in the staged box).
+template <int TX, int TY, int PX = TX + 2>
 struct GbfSplitShape {
   static constexpr int threads = TX * TY;
-  static constexpr int HX = TX + 2, HY = TY + 2, HN = HX * HY;  // plane with its 1-cell halo
-  static constexpr int slots = (HN + threads - 1) / threads;    // halo elements per thread
+  static constexpr int HX = PX, HY = TY + 2, HN = HX * HY;  // pitch, rows, elements
+  static constexpr int slots = (HN + threads - 1) / threads;  // halo elements per thread
 };
+template <int TX, bool TMA>
+__host__ __device__ constexpr int gbf_plane_pitch() { return TMA ? gbf_tma_box_x(TX) : TX + 2; }
 // Default shape of the single-domain kernel.
 constexpr int kSplitTX = 32, kSplitTY = 8;
 constexpr int kSplitThreads = kSplitTX * kSplitTY;
 
 // One x-y plane of the tile with its 1-cell halo.
-template <int TX, int TY>
+template <int TX, int TY, int PX = TX + 2>
 struct GbfSplitPlaneT {
-  static constexpr int HN = GbfSplitShape<TX, TY>::HN;
+  static constexpr int HN = GbfSplitShape<TX, TY, PX>::HN;
   float dP[HN], S[HN], L1[HN], L2[HN];
 };
 using GbfSplitPlane = GbfSplitPlaneT<kSplitTX, kSplitTY>;
@@ -145,11 +150,13 @@ using GbfSplitPlane = GbfSplitPlaneT<kSplitTX, kSplitTY>;
 //  - halo planes: dP, S, K of one x-y plane of the tile with its 1-cell halo,
 //    up to kTmaStages planes ahead of the plane being built;
 //  - interior rows: M1, M2 (8 bytes a cell) and phi of the plane being
-//    updated, one plane ahead (kRowStages stages).
+//    updated, RS - 1 planes ahead (RS = 3 where the static shared memory
+//    of the kernel stays within 48 KB, else 2).
 // Every array starts on a 128-byte boundary.
-constexpr int kTmaStages = 3, kRowStages = 2;
+constexpr int kTmaStages = 3;
 template <int TX, int TY>
 struct GbfRawRing {
+  static constexpr int RS = TX >= 64 ? 2 : 3;
   static constexpr int BX = gbf_tma_box_x(TX), HY = TY + 2, N = BX * HY;
   static constexpr int NP = (N + 31) / 32 * 32;
   static constexpr int MX = gbf_tma_rows_x8(TX), NM = (MX * TY + 15) / 16 * 16;  // 8-byte elements
@@ -158,9 +165,9 @@ struct GbfRawRing {
   static constexpr unsigned kHaloBytes = 3u * N * 4u;
   static constexpr unsigned kRowsBytes = 2u * MX * TY * 8u + (unsigned)FX * TY * 4u;
   float v[kTmaStages][3][NP];
-  double m1[kRowStages][NM], m2[kRowStages][NM];
-  float phi[kRowStages][NF];
-  unsigned long long bar[kTmaStages], mbar[kRowStages];
+  double m1[RS][NM], m2[RS][NM];
+  float phi[RS][NF];
+  unsigned long long bar[kTmaStages], mbar[RS];
 };
 
 __device__ __forceinline__ unsigned gbf_smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
@@ -261,14 +268,17 @@ struct GbfSplitAcc {
 // TMA = false: plain loads, one plane prefetched in registers, two buffers.
 template <bool DF, int TX = kSplitTX, int TY = kSplitTY, bool TMA = false>
 __device__ bool split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i0, int j0, int k0, int k1,
-                           GbfSplitPlaneT<TX, TY>* pl, GbfSplitAcc<DF>& acc, GbfRawRing<TX, TY>* raw = nullptr,
-                           const GbfTmaSet* maps = nullptr, int buf = 0, unsigned* phases = nullptr) {
+                           GbfSplitPlaneT<TX, TY, gbf_plane_pitch<TX, TMA>()>* pl, GbfSplitAcc<DF>& acc,
+                           GbfRawRing<TX, TY>* raw = nullptr, const GbfTmaSet* maps = nullptr, int buf = 0,
+                           unsigned* phases = nullptr) {
   using W = Wide<DF>;
   using WT = typename W::T;
-  using Sh = GbfSplitShape<TX, TY>;
+  constexpr int PX = gbf_plane_pitch<TX, TMA>();
+  using Sh = GbfSplitShape<TX, TY, PX>;
   constexpr int kSplitTX = TX, kSplitThreads = Sh::threads, kSplitHX = Sh::HX, kSplitHN = Sh::HN,
                 kSplitSlots = Sh::slots;
-  using GbfSplitPlane = GbfSplitPlaneT<TX, TY>;
+  using GbfSplitPlane = GbfSplitPlaneT<TX, TY, PX>;
+  static_assert(!TMA || PX == GbfRawRing<TX, TY>::BX, "TMA plane pitch equals the box width");
   const int nx = C.nx, ny = C.ny, nz = C.nz;
   const unsigned pln = (unsigned)nx * (unsigned)ny;  // grids hold < 2^32 cells (checked on the host)
   const int tx = threadIdx.x % kSplitTX, ty = threadIdx.x / kSplitTX;
@@ -285,7 +295,7 @@ __device__ bool split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i
     hq[s] = q;
     hcol[s] = -1;
     hj[s] = 0;
-    if (q < kSplitHN) {
+    if (q < kSplitHN && q % kSplitHX < TX + 2) {
       const int gi = i0 - 1 + q % kSplitHX, gj = j0 - 1 + q / kSplitHX;
       if (gi < nx && gj < ny) {
         hcol[s] = gi + gj * nx;
@@ -324,16 +334,20 @@ __device__ bool split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i
   };
 
   // TMA staging. Plane p uses stage (p - k0) % kTmaStages of the halo ring,
-  // stage (p - k0) % kRowStages of the rows ring and plane buffer
-  // pl[(p - k0) % 3]. Thread 0 issues the copies; every thread
+  // stage (p - k0) % RS of the rows ring and plane buffer pl[(p - k0) % 3];
+  // planes are issued and consumed in order, so each ring keeps rotating
+  // issue and use counters instead. Thread 0 issues the copies; every thread
   // tracks the stages in flight (`pend`: bits 0.. halo ring, bits 8.. rows
   // ring) and the barrier parities (`*phases`, same bit layout), so that a
   // give-up can wait out the copies still in flight.
   using Ring = GbfRawRing<TX, TY>;
+  constexpr int RS = Ring::RS;
   unsigned pend = 0;
+  int h_issue = 0, r_issue = 0;  // next stage to fill, halo and rows rings
   auto issue = [&](int p) {  // halo planes of plane p
     if constexpr (TMA) {
-      const int s = (p - k0) % kTmaStages;
+      const int s = h_issue;
+      h_issue = s == kTmaStages - 1 ? 0 : s + 1;
       if (threadIdx.x == 0) {
         gbf_mbar_expect_tx(&raw->bar[s], Ring::kHaloBytes);
         gbf_tma_plane(raw->v[s][0], &maps->dP[buf], i0 - 1, j0 - 1, p, &raw->bar[s]);
@@ -345,7 +359,8 @@ __device__ bool split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i
   };
   auto issue_rows = [&](int p) {  // M1, M2, phi rows of plane p
     if constexpr (TMA) {
-      const int s = (p - k0) % kRowStages;
+      const int s = r_issue;
+      r_issue = s == RS - 1 ? 0 : s + 1;
       if (threadIdx.x == 0) {
         gbf_mbar_expect_tx(&raw->mbar[s], Ring::kRowsBytes);
         gbf_tma_plane(raw->m1[s], &maps->M1, i0 - 1, j0, p, &raw->mbar[s]);
@@ -376,13 +391,12 @@ __device__ bool split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i
       if (threadIdx.x == 0) atomicOr(G.status, GBF_DEV_TIMEOUT);
     }
   };
-  auto build_tma = [&](GbfSplitPlane& P, int p) {
+  auto build_tma = [&](GbfSplitPlane& P, int s) {  // from halo stage s
     if constexpr (TMA) {
-      const int s = (p - k0) % kTmaStages;
 #pragma unroll
       for (int q = 0; q < kSplitSlots; q++) {
         if (hcol[q] >= 0) {
-          const int ri = (hq[q] / kSplitHX) * Ring::BX + hq[q] % kSplitHX;
+          const int ri = hq[q];  // same pitch in the box and in the plane
           float L1, L2;
           const float rp = raw->v[s][0][ri], rs = raw->v[s][1][ri];
           split_props(C, 0, raw->v[s][2][ri], rp, rs, hj[q], L1, L2);
@@ -398,7 +412,7 @@ __device__ bool split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i
   // prologue: own column at k0 - 1 (registers), plane k0 (shared)
   if constexpr (TMA) {
     for (int q = 0; q < kTmaStages && k0 + q <= k1; q++) issue(k0 + q);
-    for (int q = 0; q < kRowStages && k0 + q < k1; q++) issue_rows(k0 + q);
+    for (int q = 0; q < RS && k0 + q < k1; q++) issue_rows(k0 + q);
   }
   float dPm = 0.f, L1m = 0.f, L2m = 0.f;
   if (active) {
@@ -410,7 +424,7 @@ __device__ bool split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i
   }
   if constexpr (TMA) {
     const bool ok = wait_bit(0);
-    if (ok) build_tma(pl[0], k0);
+    if (ok) build_tma(pl[0], 0);
     if (__syncthreads_or(!ok)) {
       give_up();
       return false;
@@ -422,35 +436,34 @@ __device__ bool split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i
     fetch(k0 + 1);
     __syncthreads();
   }
-  int cur = 0;
+  int cur = 0;                             // plain loads: buffer of plane k
+  int t_cur = 0, t_next = 1, t_rows = 0;   // TMA: buffer/halo stage of planes k, k + 1; rows stage of plane k
   const WT R01 = W::c(C.ro01_d, C.ro01_df), R02 = W::c(C.ro02_d, C.ro02_df);
   const int mi = ty * Ring::MX + tx + 1, fi = ty * Ring::FX + tx + 1;  // own cell in the rows boxes
   for (int k = k0; k < k1; k++) {
-    int sc = 0, sr = 0;  // plane buffer and rows stage of plane k (TMA)
     if constexpr (TMA) {
       // one barrier per plane: plane k + 1 built into its own buffer (three
       // buffers rotate, so no thread can still be reading the one written)
-      sc = (k - k0) % kTmaStages;
-      sr = (k - k0) % kRowStages;
-      const int sn = (k + 1 - k0) % kTmaStages;
+      const int sn = t_next;
       bool ok = wait_bit(sn);
-      ok = ok && wait_bit(8 + sr);
-      if (ok) build_tma(pl[sn], k + 1);
+      ok = ok && wait_bit(8 + t_rows);
+      if (ok) build_tma(pl[sn], sn);
       if (__syncthreads_or(!ok)) {
         give_up();
         return false;
       }
       // halo stage sn was consumed by the build above; the rows stage of
-      // plane k - 1 (= that of plane k + 1) by the previous plane's update
+      // plane k - 1 (= that of plane k - 1 + RS) by the previous plane's update
       if (k + 1 + kTmaStages <= k1) issue(k + 1 + kTmaStages);
-      if (k > k0 && k + 1 < k1) issue_rows(k + 1);
+      if (k > k0 && k - 1 + RS < k1) issue_rows(k - 1 + RS);
     } else {
       build(pl[cur ^ 1]);  // plane k + 1 from the prefetched raw values
       fetch(k + 2);        // prefetch plane k + 2
       __syncthreads();
     }
-    GbfSplitPlane& Pc = TMA ? pl[sc] : pl[cur];
-    GbfSplitPlane& Pn = TMA ? pl[(sc + 1) % kTmaStages] : pl[cur ^ 1];
+    GbfSplitPlane& Pc = TMA ? pl[t_cur] : pl[cur];
+    GbfSplitPlane& Pn = TMA ? pl[t_next] : pl[cur ^ 1];
+    const int sr = t_rows;
     if (active) {
       const unsigned c = (unsigned)(i + j * nx) + (unsigned)k * pln;
       const int md = (!TMA && G.media) ? __ldg(G.media + c) : 0;
@@ -555,6 +568,10 @@ __device__ bool split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i
     if constexpr (!TMA) {
       __syncthreads();
       cur ^= 1;
+    } else {
+      t_cur = t_next;
+      t_next = t_next == kTmaStages - 1 ? 0 : t_next + 1;
+      t_rows = t_rows == RS - 1 ? 0 : t_rows + 1;
     }
   }
   return true;
