@@ -207,6 +207,31 @@ int gbf_set_host_direct(int on);
 int gbf_domain_uses_tma(gbf_domain* d);
 int gbf_ensemble_uses_tma(gbf_ensemble* e);
 
+/* ------------------------------------------------------------ checkpoints
+ * The reference's checkpoint file save/save.dat (main.cpp:485-572), one
+ * domain: int step; double P1, S2, x, y, z, roS1_old, roS2_old; int media;
+ * n = nx*ny*nz values each, index i + j*nx + k*nx*ny, native byte order.
+ * x, y, z are the cell coordinates i*h1, j*h2, k*h3 (main.cpp:115-117); the
+ * reader refuses a file whose size or coordinates do not match the model.
+ * CPU-written checkpoints restore into GPU domains and back.
+ */
+size_t gbf_checkpoint_bytes(const gbf_model* m);
+/* NULL roS1_old/roS2_old/media are written as zeros. */
+int gbf_checkpoint_write(const char* path, const gbf_model* m, int step, const double* P1, const double* S2,
+                         const double* roS1_old, const double* roS2_old, const int* media);
+/* NULL outputs are skipped. */
+int gbf_checkpoint_read(const char* path, const gbf_model* m, int* step, double* P1, double* S2, double* roS1_old,
+                        double* roS2_old, int* media);
+/* The domain's state as such a file. roS1_old/roS2_old are those the
+   reference holds after its last step: start-of-step phase masses of the
+   interior cells (cpu.cpp:222-225, 286-287), computed from the state before
+   that step (zeros before the first step); media is the domain's table index
+   (zeros without one). */
+int gbf_domain_save(gbf_domain* d, const char* path, int step);
+/* Upload (P1, S2) from such a file, after checking that its media equal the
+   domain's; *step receives the file's step. */
+int gbf_domain_restore(gbf_domain* d, const char* path, int* step);
+
 /* ----------------------------------------------------------- ensembles ----
  * Independent realizations of uneven sizes and parameters, advanced
  * together: every gbf_ensemble_step moves every member by one of its own

@@ -185,6 +185,8 @@ class Reference:
         for name in ("ref_ro_P2_Xi", "ref_u", "ref_P1_S2", "ref_boundary"):
             getattr(lib, name).argtypes = [PP, PI, PCo]
         lib.ref_roS.argtypes = [PP, PI, PCo, ctypes.c_double]
+        lib.ref_save.argtypes = [ctypes.c_char_p, PP, PI, PCo, ctypes.c_int]
+        lib.ref_restore.argtypes = [ctypes.c_char_p, PP, PI, PCo, ctypes.POINTER(ctypes.c_int)]
         self.lib = lib
 
     def _args(self, st):
@@ -213,3 +215,15 @@ class Reference:
 
     def boundary(self, st):
         self.lib.ref_boundary(*self._args(st))
+
+    def save(self, st, directory, j):
+        """main.cpp:485 save() into `directory`/save/save.dat."""
+        p, md, c = self._args(st)
+        assert self.lib.ref_save(str(directory).encode(), p, md, c, j) == 0
+
+    def restore(self, st, directory) -> int:
+        """main.cpp:541 restore() from `directory`/save/save.dat; returns the step."""
+        p, md, c = self._args(st)
+        j = ctypes.c_int(0)
+        assert self.lib.ref_restore(str(directory).encode(), p, md, c, ctypes.byref(j)) == 0
+        return j.value

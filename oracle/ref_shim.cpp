@@ -61,3 +61,25 @@ void ref_boundary(double** arrs, int* media, const consts* def) {
 }
 
 }  // extern "C"
+
+// main.cpp:485 save / main.cpp:541 restore (single domain). Both work on
+// "save/save.dat" relative to the working directory, so the call runs in
+// `dir` and returns to the previous working directory afterwards.
+#include <limits.h>
+#include <unistd.h>
+
+extern "C" int ref_save(const char* dir, double** arrs, int* media, const consts* def, int j) {
+  char prev[PATH_MAX];
+  if (!getcwd(prev, sizeof(prev)) || chdir(dir) != 0) return -1;
+  ptr_Arrays H = make_arrays(arrs, media);
+  save(H, H, j, 0, 1, def->NX, *def);
+  return chdir(prev);
+}
+
+extern "C" int ref_restore(const char* dir, double** arrs, int* media, const consts* def, int* j) {
+  char prev[PATH_MAX];
+  if (!getcwd(prev, sizeof(prev)) || chdir(dir) != 0) return -1;
+  ptr_Arrays H = make_arrays(arrs, media);
+  restore(H, j, 0, 1, def->NX, *def);
+  return chdir(prev);
+}

@@ -152,6 +152,13 @@ def _declare(lib) -> None:
         "gbf_set_host_direct": (c_int, [c_int]),
         "gbf_domain_uses_tma": (c_int, [c_void_p]),
         "gbf_ensemble_uses_tma": (c_int, [c_void_p]),
+        "gbf_checkpoint_bytes": (c_size_t, [PM]),
+        "gbf_checkpoint_write": (c_int, [ctypes.c_char_p, PM, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
+                                         c_void_p]),
+        "gbf_checkpoint_read": (c_int, [ctypes.c_char_p, PM, ctypes.POINTER(c_int), c_void_p, c_void_p, c_void_p,
+                                        c_void_p, c_void_p]),
+        "gbf_domain_save": (c_int, [c_void_p, ctypes.c_char_p, c_int]),
+        "gbf_domain_restore": (c_int, [c_void_p, ctypes.c_char_p, ctypes.POINTER(c_int)]),
         "gbf_ensemble_create": (c_int, [c_int, PM, PC, c_int, ctypes.POINTER(c_void_p)]),
         "gbf_ensemble_destroy": (c_int, [c_void_p]),
         "gbf_ensemble_size": (c_int, [c_void_p]),

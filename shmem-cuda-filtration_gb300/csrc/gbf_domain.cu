@@ -285,6 +285,56 @@ int gbf_domain_status(gbf_domain* d) {
 }
 
 long long gbf_domain_steps_done(gbf_domain* d) { return d ? d->steps : -1; }
+
+// Checkpoint in the reference's save/save.dat layout (gbf_checkpoint.cpp).
+// roS1_old, roS2_old are what the reference holds after its last step: the
+// start-of-step masses of the interior cells, i.e. of the state before that
+// step, which is still in the other ping-pong buffer (zeros before a step).
+int gbf_domain_save(gbf_domain* d, const char* path, int step) {
+  if (!d || !path) return gbf_fail(GBF_ERR_ARG, "gbf_domain_save");
+  if (!d->uploaded || d->borrowed) return gbf_fail(GBF_ERR_STATE, "gbf_domain_save without an uploaded state");
+  const size_t n = gbf_geo(d->m).n;
+  std::vector<double> P(n), S(n), old(2 * n, 0.0);
+  std::vector<int> media;
+  if (int s = gbf_domain_download(d, GBF_FIELD_P1, P.data())) return s;
+  if (int s = gbf_domain_download(d, GBF_FIELD_S2, S.data())) return s;
+  if (d->steps > 0) {
+    double* tmp = nullptr;
+    GBF_CUDA(cudaMallocAsync((void**)&tmp, 2 * n * sizeof(double), d->stream));
+    const int prev = d->cur ^ 1;
+    int s = d->precision == GBF_PREC_F64
+                ? gbf_roS_old_launch(d->m, d->P[prev], d->S[prev], nullptr, nullptr, tmp, tmp + n, d->stream)
+                : gbf_roS_old_launch(d->m, nullptr, nullptr, d->Pf[prev], d->Sf[prev], tmp, tmp + n, d->stream);
+    if (!s) s = gbf_cuda_check(cudaMemcpyAsync(old.data(), tmp, 2 * n * sizeof(double), cudaMemcpyDeviceToHost,
+                                               d->stream), "copy roS_old");
+    cudaFreeAsync(tmp, d->stream);
+    if (!s) s = gbf_cuda_check(cudaStreamSynchronize(d->stream), "gbf_domain_save");
+    if (s) return s;
+  }
+  if (d->cells.media) {
+    media.resize(n);
+    GBF_CUDA(cudaMemcpy(media.data(), d->cells.media, n * sizeof(int), cudaMemcpyDeviceToHost));
+  }
+  return gbf_checkpoint_write(path, &d->m, step, P.data(), S.data(), old.data(), old.data() + n,
+                              media.empty() ? nullptr : media.data());
+}
+
+// Restore (P1, S2) from such a file; its media must equal the domain's
+// (all 0 for a domain without a media table).
+int gbf_domain_restore(gbf_domain* d, const char* path, int* step) {
+  if (!d || !path) return gbf_fail(GBF_ERR_ARG, "gbf_domain_restore");
+  if (d->borrowed) return gbf_fail(GBF_ERR_STATE, "gbf_domain_restore on a drop-in domain");
+  const size_t n = gbf_geo(d->m).n;
+  std::vector<double> P(n), S(n);
+  std::vector<int> media(n), mine(n, 0);
+  int j = 0;
+  if (int s = gbf_checkpoint_read(path, &d->m, &j, P.data(), S.data(), nullptr, nullptr, media.data())) return s;
+  if (d->cells.media) GBF_CUDA(cudaMemcpy(mine.data(), d->cells.media, n * sizeof(int), cudaMemcpyDeviceToHost));
+  if (media != mine) return gbf_fail(GBF_ERR_ARG, "gbf_domain_restore: the file's media differ from the domain's");
+  if (int s = gbf_domain_upload(d, P.data(), S.data())) return s;
+  if (step) *step = j;
+  return GBF_OK;
+}
 int gbf_domain_uses_tma(gbf_domain* d) { return d && d->tma ? 1 : 0; }
 
 int gbf_domain_set_timing(gbf_domain* d, int on) {

@@ -85,6 +85,11 @@ struct gbf_domain {
 
 int gbf_domain_alloc(gbf_domain* d, void** p, size_t bytes);
 
+// roS1_old, roS2_old of interior cells from an FP64 state (P, S) or, with P
+// and S NULL, from a split state (dPf, Sf); boundary cells 0 (gbf_eager.cu).
+int gbf_roS_old_launch(const gbf_model& m, const double* P, const double* S, const float* dPf, const float* Sf,
+                       double* o1, double* o2, cudaStream_t st);
+
 // Drop-in helpers (gbf_domain.cu).
 int gbf_domain_attach_dropin(const gbf_model* m, gbf_arrays caller, gbf_cells cells, gbf_domain** out);
 int gbf_dropin_defer(gbf_domain* d, const gbf_model& m, int stage);

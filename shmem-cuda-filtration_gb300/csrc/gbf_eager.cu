@@ -262,7 +262,38 @@ int launched(const char* where) {
   return e == cudaSuccess ? GBF_OK : gbf_cuda_check(e, where);
 }
 
+// Start-of-step phase masses of interior cells from a state (P, S): what
+// assign_rS_nr leaves in roS1_old, roS2_old (cpu.cpp:222-225, 286-287) with
+// the densities of assign_ro1_ro2 at P2 = P1 (cpu.cpp:63-74). FP64 state, or
+// the split state (dP from the hydrostatic profile, S in FP32) when P is NULL.
+// Boundary cells get 0.
+__global__ void __launch_bounds__(kThreads) k_roS_old(const gbf_model m, const double* P, const double* S,
+                                                      const float* dPf, const float* Sf, double* o1, double* o2) {
+  const GbfGeo g = gbf_geo(m);
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < g.n; c += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(c % g.nx), j = (int)((c / g.nx) % g.ny), k = (int)(c / g.pl);
+    if (gbf_is_boundary(g, i, j, k)) {
+      o1[c] = 0.;
+      o2[c] = 0.;
+      continue;
+    }
+    const double p = P ? P[c] : gbf_p_hydrostatic(m, j) + (double)dPf[c];
+    const double s = S ? S[c] : (double)Sf[c];
+    const double ro1 = m.ro01 * (1. + (m.beta1) * (p - m.P_atm));
+    const double ro2 = m.ro02 * (1. + (m.beta2) * (p - m.P_atm));
+    o1[c] = ro1 * (1 - s);
+    o2[c] = ro2 * s;
+  }
+}
+
 }  // namespace
+
+int gbf_roS_old_launch(const gbf_model& m, const double* P, const double* S, const float* dPf, const float* Sf,
+                       double* o1, double* o2, cudaStream_t st) {
+  k_roS_old<<<gbf_grid_for(gbf_geo(m).n, kThreads), kThreads, 0, st>>>(m, P, S, dPf, Sf, o1, o2);
+  GBF_CUDA(cudaGetLastError());
+  return GBF_OK;
+}
 
 extern "C" {
 

@@ -75,6 +75,16 @@ class Domain:
         abi.check(self.lib.gbf_domain_download(self.h, abi.FIELD_ID[field], out.ctypes.data), f"download {field}")
         return out
 
+    def save(self, path, step: int):
+        """Checkpoint in the reference's save/save.dat layout."""
+        abi.check(self.lib.gbf_domain_save(self.h, str(path).encode(), step), "save")
+
+    def restore(self, path) -> int:
+        """Upload (P1, S2) from such a checkpoint; returns its step."""
+        j = ctypes.c_int()
+        abi.check(self.lib.gbf_domain_restore(self.h, str(path).encode(), ctypes.byref(j)), "restore")
+        return j.value
+
     def mass_history(self, max_steps: int) -> np.ndarray:
         out = np.zeros((max_steps, 2), np.float64)
         n = ctypes.c_int()

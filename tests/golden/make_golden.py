@@ -4,7 +4,7 @@ The reference (cpu.cpp + main.cpp + no_communication.cpp) has no tests and no
 golden vectors, so these fixtures are made by running it: oracle/Makefile
 compiles those files from their sources into oracle/_ref/libgbf_refcpu.so and
 this script drives them through their own functions (initial_data,
-time_step_function and the five hot-path calls).
+time_step_function, the five hot-path calls and the checkpoint writer save).
 
 Run from the repository root where the reference sources are present:
     python tests/golden/make_golden.py
@@ -15,6 +15,7 @@ from __future__ import annotations
 import json
 import pathlib
 import sys
+import tempfile
 
 import numpy as np
 
@@ -90,6 +91,20 @@ def main():
     for k in ("P1", "S2"):
         stages[f"boundary_{k}"] = st[k].copy()
     np.savez_compressed(OUT / "ref_stages_8x9x10.npz", model=json.dumps(model_dict(m)), **stages)
+
+    # 4: a checkpoint file written by the reference's own save() (main.cpp:485)
+    # after 7 steps of a run from initial_data; the file's bytes are stored.
+    m = abi.reference_model(10, 8, 6, 0.02)
+    m.source = 1
+    st = O.State(m)
+    ref.initial(st)  # sets media to 0; mixed media afterwards
+    st.media[...] = (np.random.default_rng(5).random(m.shape) < 0.3).astype(np.int32)
+    ref.step(st, 7)
+    with tempfile.TemporaryDirectory() as d:
+        ref.save(st, d, 7)
+        dat = (pathlib.Path(d) / "save" / "save.dat").read_bytes()
+    np.savez_compressed(OUT / "ref_checkpoint_10x8x6_step7.npz", model=json.dumps(model_dict(m)), steps=7,
+                        dat=np.frombuffer(dat, np.uint8))
     for p in sorted(OUT.glob("*.npz")):
         print(p.name, p.stat().st_size)
 
