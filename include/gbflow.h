@@ -232,6 +232,20 @@ int gbf_domain_save(gbf_domain* d, const char* path, int step);
    domain's; *step receives the file's step. */
 int gbf_domain_restore(gbf_domain* d, const char* path, int* step);
 
+/* ------------------------------------------------------------ plot files
+ * The reference's Tecplot output of save_data_plots (main.cpp:319-482) for
+ * one domain, written under `dir`: plot_S2/S2=<t>.dat, plot_P1/P1=<t>.dat,
+ * plot_u/u=<t>.dat, plot_S2_y/S2=<t>.dat, plot_S2_x/S2=<t>.dat (t as
+ * %012.4f) and media.dat, byte for byte as the reference writes them from
+ * the same arrays. Subdirectories are created; a NULL media writes 0.
+ */
+int gbf_write_plots(const char* dir, const gbf_model* m, double t, const double* P1, const double* S2,
+                    const double* u2x, const double* u2y, const double* u2z, const int* media);
+/* The domain's state: P1, S2 as downloaded and the DNAPL velocities the
+   reference holds after its last step (those of the state that step started
+   from; zeros before the first step). */
+int gbf_domain_write_plots(gbf_domain* d, const char* dir, double t);
+
 /* ----------------------------------------------------------- ensembles ----
  * Independent realizations of uneven sizes and parameters, advanced
  * together: every gbf_ensemble_step moves every member by one of its own

@@ -187,6 +187,7 @@ class Reference:
         lib.ref_roS.argtypes = [PP, PI, PCo, ctypes.c_double]
         lib.ref_save.argtypes = [ctypes.c_char_p, PP, PI, PCo, ctypes.c_int]
         lib.ref_restore.argtypes = [ctypes.c_char_p, PP, PI, PCo, ctypes.POINTER(ctypes.c_int)]
+        lib.ref_plots.argtypes = [ctypes.c_char_p, PP, PI, PCo, ctypes.c_double]
         self.lib = lib
 
     def _args(self, st):
@@ -220,6 +221,11 @@ class Reference:
         """main.cpp:485 save() into `directory`/save/save.dat."""
         p, md, c = self._args(st)
         assert self.lib.ref_save(str(directory).encode(), p, md, c, j) == 0
+
+    def plots(self, st, directory, t):
+        """main.cpp:319 save_data_plots() writing into `directory`."""
+        p, md, c = self._args(st)
+        assert self.lib.ref_plots(str(directory).encode(), p, md, c, t) == 0
 
     def restore(self, st, directory) -> int:
         """main.cpp:541 restore() from `directory`/save/save.dat; returns the step."""

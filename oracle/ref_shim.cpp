@@ -83,3 +83,13 @@ extern "C" int ref_restore(const char* dir, double** arrs, int* media, const con
   restore(H, j, 0, 1, def->NX, *def);
   return chdir(prev);
 }
+
+// main.cpp:319 save_data_plots (single domain), run in `dir`: writes the
+// Tecplot files plot_*/...=<t>.dat and media.dat there.
+extern "C" int ref_plots(const char* dir, double** arrs, int* media, const consts* def, double t) {
+  char prev[PATH_MAX];
+  if (!getcwd(prev, sizeof(prev)) || chdir(dir) != 0) return -1;
+  ptr_Arrays H = make_arrays(arrs, media);
+  save_data_plots(H, H, t, 1, 0, def->NX, *def);
+  return chdir(prev);
+}

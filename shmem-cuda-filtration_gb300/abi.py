@@ -159,6 +159,9 @@ def _declare(lib) -> None:
                                         c_void_p, c_void_p]),
         "gbf_domain_save": (c_int, [c_void_p, ctypes.c_char_p, c_int]),
         "gbf_domain_restore": (c_int, [c_void_p, ctypes.c_char_p, ctypes.POINTER(c_int)]),
+        "gbf_write_plots": (c_int, [ctypes.c_char_p, PM, c_double, c_void_p, c_void_p, c_void_p, c_void_p,
+                                    c_void_p, c_void_p]),
+        "gbf_domain_write_plots": (c_int, [c_void_p, ctypes.c_char_p, c_double]),
         "gbf_ensemble_create": (c_int, [c_int, PM, PC, c_int, ctypes.POINTER(c_void_p)]),
         "gbf_ensemble_destroy": (c_int, [c_void_p]),
         "gbf_ensemble_size": (c_int, [c_void_p]),

@@ -71,15 +71,26 @@ void free_all(gbf_domain* d) {
 }
 
 // One FP64 step: current buffer -> next buffer, then flip. In drop-in mode
-// the caller's arrays are the current buffer and the next state is copied
-// back so that they always hold the latest state.
+// the caller's arrays (buffer 0) always hold the latest state: the state the
+// step starts from is first copied to buffer 1, where it stays for the lazily
+// materialised derived arrays (gbf_dropin_materialize).
 int f64_step(gbf_domain* d, int props_flags) {
   const int nxt = d->cur ^ 1;
   GbfF64Step s = {};
-  s.P = d->P[d->cur];
-  s.S = d->S[d->cur];
-  s.Pn = d->P[nxt];
-  s.Sn = d->S[nxt];
+  if (d->borrowed) {
+    const size_t b = gbf_geo(d->m).n * sizeof(double);
+    GBF_CUDA(cudaMemcpyAsync(d->P[1], d->P[0], b, cudaMemcpyDeviceToDevice, d->stream));
+    GBF_CUDA(cudaMemcpyAsync(d->S[1], d->S[0], b, cudaMemcpyDeviceToDevice, d->stream));
+    s.P = d->P[1];
+    s.S = d->S[1];
+    s.Pn = d->P[0];
+    s.Sn = d->S[0];
+  } else {
+    s.P = d->P[d->cur];
+    s.S = d->S[d->cur];
+    s.Pn = d->P[nxt];
+    s.Sn = d->S[nxt];
+  }
   s.L1 = d->L1; s.L2 = d->L2; s.ro1 = d->ro1; s.ro2 = d->ro2; s.lnSe = d->lnSe;
   s.Xi1 = d->outs.Xi1; s.Xi2 = d->outs.Xi2; s.P2 = d->outs.P2;
   s.u1x = d->outs.u1x; s.u1y = d->outs.u1y; s.u1z = d->outs.u1z;
@@ -100,13 +111,10 @@ int f64_step(gbf_domain* d, int props_flags) {
   }
   int st = gbf_f64_launch_step(d->m, d->d, d->cells, s, props_flags, mass_out, d->stream, &d->timer);
   if (st) return st;
-  if (d->borrowed) {
-    const size_t b = gbf_geo(d->m).n * sizeof(double);
-    GBF_CUDA(cudaMemcpyAsync(d->P[d->cur], d->P[nxt], b, cudaMemcpyDeviceToDevice, d->stream));
-    GBF_CUDA(cudaMemcpyAsync(d->S[d->cur], d->S[nxt], b, cudaMemcpyDeviceToDevice, d->stream));
-  } else {
+  if (d->borrowed)
+    d->lazy_dirty = true;
+  else
     d->cur = nxt;
-  }
   d->steps++;
   return GBF_OK;
 }
@@ -319,6 +327,46 @@ int gbf_domain_save(gbf_domain* d, const char* path, int step) {
                               media.empty() ? nullptr : media.data());
 }
 
+// The reference's Tecplot files of the domain's state (gbf_plots.cpp). Like
+// the reference's u arrays after a step, the velocities are those of the
+// state the last step started from (a2 runs before a3-a5, main.cpp:85-92),
+// computed with the one-call-per-stage kernels; zeros before the first step.
+int gbf_domain_write_plots(gbf_domain* d, const char* dir, double t) {
+  if (!d || !dir) return gbf_fail(GBF_ERR_ARG, "gbf_domain_write_plots");
+  if (!d->uploaded || d->borrowed) return gbf_fail(GBF_ERR_STATE, "gbf_domain_write_plots without an uploaded state");
+  const gbf_model& m = d->m;
+  const size_t n = gbf_geo(m).n, b = n * sizeof(double);
+  std::vector<double> P(n), S(n), u(3 * n, 0.0);
+  std::vector<int> media;
+  if (int s = gbf_domain_download(d, GBF_FIELD_P1, P.data())) return s;
+  if (int s = gbf_domain_download(d, GBF_FIELD_S2, S.data())) return s;
+  if (d->steps > 0) {
+    double* w = nullptr;  // P1, S2, P2, ro1, ro2, Xi1, Xi2, u1x, u1y, u1z, u2x, u2y, u2z
+    GBF_CUDA(cudaMallocAsync((void**)&w, 13 * b, d->stream));
+    gbf_arrays a = {};
+    a.P1 = w; a.S2 = w + n; a.P2 = w + 2 * n; a.ro1 = w + 3 * n; a.ro2 = w + 4 * n; a.Xi1 = w + 5 * n;
+    a.Xi2 = w + 6 * n; a.u1x = w + 7 * n; a.u1y = w + 8 * n; a.u1z = w + 9 * n; a.u2x = w + 10 * n;
+    a.u2y = w + 11 * n; a.u2z = w + 12 * n;
+    const int prev = d->cur ^ 1;
+    int s = d->precision == GBF_PREC_F64 ? gbf_cuda_check(cudaMemcpyAsync(a.P1, d->P[prev], b, cudaMemcpyDeviceToDevice, d->stream), "copy P")
+                                         : gbf_split_state_to_f64(m, d->Pf[prev], d->Sf[prev], a.P1, a.S2, d->stream);
+    if (!s && d->precision == GBF_PREC_F64)
+      s = gbf_cuda_check(cudaMemcpyAsync(a.S2, d->S[prev], b, cudaMemcpyDeviceToDevice, d->stream), "copy S");
+    if (!s) s = gbf_props_f64(&m, a, d->cells, d->stream);
+    if (!s) s = gbf_velocity_f64(&m, a, d->stream);
+    if (!s) s = gbf_cuda_check(cudaMemcpyAsync(u.data(), a.u2x, 3 * b, cudaMemcpyDeviceToHost, d->stream), "copy u");
+    cudaFreeAsync(w, d->stream);
+    if (!s) s = gbf_cuda_check(cudaStreamSynchronize(d->stream), "gbf_domain_write_plots");
+    if (s) return s;
+  }
+  if (d->cells.media) {
+    media.resize(n);
+    GBF_CUDA(cudaMemcpy(media.data(), d->cells.media, n * sizeof(int), cudaMemcpyDeviceToHost));
+  }
+  return gbf_write_plots(dir, &m, t, P.data(), S.data(), u.data(), u.data() + n, u.data() + 2 * n,
+                         media.empty() ? nullptr : media.data());
+}
+
 // Restore (P1, S2) from such a file; its media must equal the domain's
 // (all 0 for a domain without a media table).
 int gbf_domain_restore(gbf_domain* d, const char* path, int* step) {
@@ -417,11 +465,36 @@ int gbf_domain_attach_dropin(const gbf_model* m, gbf_arrays caller, gbf_cells ce
     delete d;
     return s;
   }
-  // The fused drop-in writes every array the reference's five calls write.
-  d->outs = caller;
-  d->out_flags = GBF_OUT_VELOCITY | GBF_OUT_MASS_ARRAYS | GBF_OUT_PROPS;
+  // The fused step writes P1, S2 (and the densities ro1, ro2); the other
+  // arrays the reference's five calls write are materialised on demand.
+  d->outs = {};
+  d->out_flags = 0;
   *out = d;
   return GBF_OK;
+}
+
+// The derived arrays of the reference's step (a1: P2, Xi1, Xi2, ro1, ro2;
+// a2: velocities; a3: roS1, roS2, roS1_old, roS2_old) after the last fused
+// step: the eager stage kernels run on the state that step started from.
+int gbf_dropin_materialize(gbf_domain* d) {
+  if (!d || !d->lazy_dirty) return GBF_OK;
+  gbf_arrays a = d->caller;
+  a.P1 = d->P[1];
+  a.S2 = d->S[1];
+  int s = gbf_props_f64(&d->m, a, d->cells, nullptr);
+  s |= gbf_velocity_f64(&d->m, a, nullptr);
+  s |= gbf_mass_f64(&d->m, a, d->cells, nullptr);
+  d->lazy_dirty = false;
+  return s;
+}
+
+bool gbf_dropin_is_derived(const gbf_domain* d, const double* p) {
+  const gbf_arrays& c = d->caller;
+  const double* derived[] = {c.P2, c.ro1, c.ro2, c.Xi1, c.Xi2, c.u1x, c.u1y, c.u1z,
+                             c.u2x, c.u2y, c.u2z, c.roS1, c.roS2, c.roS1_old, c.roS2_old};
+  for (const double* q : derived)
+    if (q == p) return true;
+  return false;
 }
 
 void gbf_domain_detach_dropin(gbf_domain* d) {
@@ -435,7 +508,8 @@ void gbf_domain_detach_dropin(gbf_domain* d) {
 int gbf_dropin_flush(gbf_domain* d) {
   if (!d || !d->pending) return GBF_OK;
   const gbf_arrays a = d->caller;
-  int s = GBF_OK;
+  // the arrays these stages do not rewrite keep the last fused step's values
+  int s = gbf_dropin_materialize(d);
   if (d->pending & 1) s |= gbf_props_f64(&d->m, a, d->cells, nullptr);
   if (d->pending & 2) s |= gbf_velocity_f64(&d->m, a, nullptr);
   if (d->pending & 4) s |= gbf_mass_f64(&d->m, a, d->cells, nullptr);
@@ -463,10 +537,11 @@ int gbf_dropin_defer(gbf_domain* d, const gbf_model& m, int stage) {
     d->pending = 1 << (stage - 1);
     return s | gbf_dropin_flush(d);
   }
-  if (d->pending == 15) {
+  if (d->pending == 15) {  // the whole step: fused (its derived arrays are left to materialise on demand)
     d->pending = 0;
-    return f64_step(d, GBF_PF_WRITE_XI_P2 | GBF_PF_WRITE_U);
+    return f64_step(d, 0);
   }
   int s = gbf_dropin_flush(d);
+  if (!s) s = gbf_dropin_materialize(d);
   return s | gbf_boundary_f64(&d->m, d->caller, d->bscratch, nullptr);
 }

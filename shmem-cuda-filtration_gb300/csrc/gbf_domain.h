@@ -79,6 +79,7 @@ struct gbf_domain {
   gbf_arrays caller = {};
   int pending = 0;
   double* bscratch = nullptr;  // boundary gather scratch of the one-kernel-per-stage fallback
+  bool lazy_dirty = false;     // drop-in: derived arrays not yet materialised for the last fused step
   std::vector<void*> owned;  // every cudaMalloc of this domain
   GbfTimer timer;
 };
@@ -95,3 +96,5 @@ int gbf_domain_attach_dropin(const gbf_model* m, gbf_arrays caller, gbf_cells ce
 int gbf_dropin_defer(gbf_domain* d, const gbf_model& m, int stage);
 int gbf_dropin_flush(gbf_domain* d);
 void gbf_domain_detach_dropin(gbf_domain* d);
+int gbf_dropin_materialize(gbf_domain* d);
+bool gbf_dropin_is_derived(const gbf_domain* d, const double* p);

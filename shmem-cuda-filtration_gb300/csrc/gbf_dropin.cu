@@ -11,7 +11,12 @@
 //     blocking copies of load_data_to_host synchronise;
 //   * errors are printed like checkErrors (gpu.cu:7-27) and also kept as a
 //     sticky status readable through gbf_last_status();
-//   * single domain only (size == 1, the no_communication path).
+//   * single domain only (size == 1, the no_communication path);
+//   * fused mode (gbf_dropin_set_mode(1)) runs time_step_function's five
+//     calls as one fused step that writes P1, S2, ro1, ro2 only; the other
+//     arrays of the step (P2, Xi, velocities, roS, roS_old) are computed when
+//     the host reads one of them, from the state the step started from, with
+//     the same kernels as the one-call-per-stage mode.
 #include <stdio.h>
 
 #include <mutex>
@@ -95,11 +100,15 @@ gbf_domain* fused_of(const ptr_Arrays& D, const gbf_model& m) {
   return dd->fused;
 }
 
-// Any host access observes completed stages: run what is deferred.
-void flush_all() {
+// Any host access observes completed stages: run what is deferred, and
+// materialise the derived arrays of a fused step when `dev` is one of them.
+void flush_all(const double* dev = nullptr) {
   std::lock_guard<std::mutex> lk(g_mu);
   for (auto& kv : g_domains)
-    if (kv.second.fused) gbf_dropin_flush(kv.second.fused);
+    if (gbf_domain* f = kv.second.fused) {
+      gbf_dropin_flush(f);
+      if (dev && gbf_dropin_is_derived(f, dev)) gbf_dropin_materialize(f);
+    }
 }
 
 }  // namespace
@@ -178,13 +187,13 @@ void boundary_conditions(ptr_Arrays HostArraysPtr, ptr_Arrays DevArraysPtr, int 
 
 void load_data_to_host(double* HostArrayPtr, double* DevArrayPtr, int localNx, consts def) {
   size_t n = (size_t)localNx * def.Ny * def.Nz;
-  if (g_mode == 1) flush_all();
+  if (g_mode == 1) flush_all(DevArrayPtr);
   gbf_cuda_check(cudaMemcpy(HostArrayPtr, DevArrayPtr, n * sizeof(double), cudaMemcpyDeviceToHost), "copy data to host");
 }
 
 void load_data_to_device(double* HostArrayPtr, double* DevArrayPtr, int localNx, consts def) {
   size_t n = (size_t)localNx * def.Ny * def.Nz;
-  if (g_mode == 1) flush_all();
+  if (g_mode == 1) flush_all(DevArrayPtr);  // the other derived arrays keep their values
   gbf_cuda_check(cudaMemcpy(DevArrayPtr, HostArrayPtr, n * sizeof(double), cudaMemcpyHostToDevice), "copy double data to device");
 }
 

@@ -326,4 +326,11 @@ int gbf_split_download(gbf_domain* d, int field, double* host) {
   return GBF_OK;
 }
 
+int gbf_split_state_to_f64(const gbf_model& m, const float* dPf, const float* Sf, double* P, double* S,
+                           cudaStream_t st) {
+  k_split_to_f64<<<gbf_grid_for(gbf_geo(m).n, kThreads, 4), kThreads, 0, st>>>(m, dPf, Sf, P, S);
+  GBF_CUDA(cudaGetLastError());
+  return GBF_OK;
+}
+
 int gbf_split_launches_per_step(gbf_domain* d) { return 2 + ((d->out_flags & GBF_OUT_MASS) ? 1 : 0); }

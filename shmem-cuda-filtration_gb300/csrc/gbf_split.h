@@ -49,6 +49,9 @@ int gbf_split_upload(gbf_domain* d, const double* P1, const double* S2, cudaMemc
 int gbf_split_step(gbf_domain* d);
 int gbf_split_download(gbf_domain* d, int field, double* host);
 int gbf_split_launches_per_step(gbf_domain* d);
+// FP64 (P, S) of every cell from a split state (device arrays; either output may be NULL).
+int gbf_split_state_to_f64(const gbf_model& m, const float* dPf, const float* Sf, double* P, double* S,
+                           cudaStream_t st);
 // FP32 state and wide masses of one grid from FP64 device arrays.
 int gbf_split_init_state(const gbf_model& m, const double* P_dev, const double* S_dev, float* dPf, float* Sf,
                          double* M1, double* M2, bool df, cudaStream_t st);

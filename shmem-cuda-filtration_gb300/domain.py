@@ -85,6 +85,10 @@ class Domain:
         abi.check(self.lib.gbf_domain_restore(self.h, str(path).encode(), ctypes.byref(j)), "restore")
         return j.value
 
+    def write_plots(self, directory, t: float):
+        """The reference's Tecplot files (save_data_plots) under `directory`."""
+        abi.check(self.lib.gbf_domain_write_plots(self.h, str(directory).encode(), t), "write_plots")
+
     def mass_history(self, max_steps: int) -> np.ndarray:
         out = np.zeros((max_steps, 2), np.float64)
         n = ctypes.c_int()

@@ -4,7 +4,8 @@ The reference (cpu.cpp + main.cpp + no_communication.cpp) has no tests and no
 golden vectors, so these fixtures are made by running it: oracle/Makefile
 compiles those files from their sources into oracle/_ref/libgbf_refcpu.so and
 this script drives them through their own functions (initial_data,
-time_step_function, the five hot-path calls and the checkpoint writer save).
+time_step_function, the five hot-path calls, the checkpoint writer save and
+the Tecplot writer save_data_plots).
 
 Run from the repository root where the reference sources are present:
     python tests/golden/make_golden.py
@@ -105,6 +106,23 @@ def main():
         dat = (pathlib.Path(d) / "save" / "save.dat").read_bytes()
     np.savez_compressed(OUT / "ref_checkpoint_10x8x6_step7.npz", model=json.dumps(model_dict(m)), steps=7,
                         dat=np.frombuffer(dat, np.uint8))
+    # 5: the Tecplot files of the reference's save_data_plots() (main.cpp:319)
+    # after 4 steps (odd Ny: the S2_x profile's row offset is nx*ny/2).
+    m = abi.reference_model(9, 7, 5, 0.02)
+    m.source = 1
+    st = O.State(m)
+    ref.initial(st)
+    st.media[...] = (np.random.default_rng(6).random(m.shape) < 0.3).astype(np.int32)
+    ref.step(st, 4)
+    t = 4 * m.dt
+    files = {}
+    with tempfile.TemporaryDirectory() as d:
+        ref.plots(st, d, t)
+        for f in sorted(pathlib.Path(d).rglob("*.dat")):
+            files["file:" + str(f.relative_to(d))] = np.frombuffer(f.read_bytes(), np.uint8)
+    np.savez_compressed(OUT / "ref_plots_9x7x5_step4.npz", model=json.dumps(model_dict(m)), t=t,
+                        media=st.media.astype(np.int8), **{k: st[k] for k in ("P1", "S2", "u2x", "u2y", "u2z")},
+                        **files)
     for p in sorted(OUT.glob("*.npz")):
         print(p.name, p.stat().st_size)
 

@@ -187,6 +187,15 @@ def test_dropin_functions_match_oracle(gpu_lib, abi, O, oracle, pkg, mode):
         di.f["load_data_to_host"](out.ctypes.data, getattr(D, name), m.nx, c)
         tol = F64_TOL_GRADIENT if (mode == 1 and name.startswith("u")) else F64_TOL
         assert_field(name, out, st[name], tol=tol)
+    # a1 alone after the steps: its arrays follow the latest state, the
+    # velocities keep the last step's values (fused mode materialises them first)
+    di.f["ro_P2_Xi_calculation"](H, D, c, m.nx, 0, 1, bX.value, bY.value, bZ.value)
+    st2 = st.copy()
+    oracle.props(st2)
+    for name, ref in (("P2", st2["P2"]), ("Xi1", st2["Xi1"]), ("u2x", st["u2x"]), ("roS2_old", st["roS2_old"])):
+        out = np.empty(m.shape, np.float64)
+        di.f["load_data_to_host"](out.ctypes.data, getattr(D, name), m.nx, c)
+        assert_field(name, out, ref, tol=F64_TOL_GRADIENT if name.startswith("u") else F64_TOL)
     assert gpu_lib.gbf_last_status() == 0
     di.f["device_memory_free"](D, buf)
     di.set_mode(0)
