@@ -101,8 +101,8 @@ int gbf_last_status(void);            /* sticky status of the last failing call 
 void gbf_clear_status(void);
 const char* gbf_status_string(int status);
 const char* gbf_version(void);
-/* sizeof of the ABI structs (0: gbf_model, 1: gbf_cells, 2: gbf_arrays), so
-   bindings can check their layout. */
+/* sizeof of the ABI structs (0: gbf_model, 1: gbf_cells, 2: gbf_arrays,
+   3: gbf_run_defines), so bindings can check their layout. */
 size_t gbf_abi_sizeof(int which);
 /* Fill *m with the reference's constants (defines.h:6-26) and the defaults of
    its defines.ini; grid sizes nx, ny, nz and dt are taken from the arguments. */
@@ -110,6 +110,22 @@ void gbf_model_reference(gbf_model* m, int nx, int ny, int nz, double dt);
 /* Largest stable explicit dt (times `safety`) for this model and cell fields.
    Pure host function; K/phi may be NULL (media table used). */
 double gbf_stable_dt(const gbf_model* m, const gbf_cells* cells, double safety);
+/* The reference's run parameters that gbf_model does not hold (consts,
+   defines.h:50-61): the hyperbolic-regularisation constants of the unused
+   t < 2 dt branch (tau, l_w, l_n, c) and main.cpp's output intervals. */
+typedef struct gbf_run_defines {
+  double tau, l_w, l_n, c;
+  int save_plots, print_screen;
+} gbf_run_defines;
+/* Read a defines.ini file (the reference's format, main.cpp:601-684, from a
+   path instead of defines.h:5's fixed Windows path): *m gets
+   gbf_model_reference's values overridden by H1, H2, H3, DT, BETA1, BETA2,
+   SOURCE, NX, NY, NZ and by the physical constants the file lists (K[i],
+   LAMBDA[i], S_WR[i], M[i], P_D[i], MU1, MU2, RO_W, RO_N, S2_GR, P_ATM,
+   G_CONST; the reference takes these from defines.h:6-26 instead, with the
+   same values); *run (may be NULL) TAU, L_W, L_N, C, SAVE_PLOTS,
+   PRINT_SCREEN. NX, NY and NZ are required. */
+int gbf_read_defines(const char* path, gbf_model* m, gbf_run_defines* run);
 /* Host-side validation of a model (sizes, positivity, S_e range of the Dirichlet
    patch, dt against the stability bound when check_dt != 0). */
 int gbf_model_validate(const gbf_model* m, const gbf_cells* cells, int check_dt);

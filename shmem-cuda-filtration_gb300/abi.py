@@ -63,6 +63,11 @@ class GbfCells(ctypes.Structure):
                 ("phi", ctypes.POINTER(ctypes.c_float))]
 
 
+class GbfRunDefines(ctypes.Structure):
+    _fields_ = [("tau", ctypes.c_double), ("l_w", ctypes.c_double), ("l_n", ctypes.c_double),
+                ("c", ctypes.c_double), ("save_plots", ctypes.c_int), ("print_screen", ctypes.c_int)]
+
+
 class GbfArrays(ctypes.Structure):
     _fields_ = [(n, ctypes.c_void_p) for n in ARRAY_ORDER]
 
@@ -159,6 +164,7 @@ def _declare(lib) -> None:
                                         c_void_p, c_void_p]),
         "gbf_domain_save": (c_int, [c_void_p, ctypes.c_char_p, c_int]),
         "gbf_domain_restore": (c_int, [c_void_p, ctypes.c_char_p, ctypes.POINTER(c_int)]),
+        "gbf_read_defines": (c_int, [ctypes.c_char_p, PM, ctypes.POINTER(GbfRunDefines)]),
         "gbf_write_plots": (c_int, [ctypes.c_char_p, PM, c_double, c_void_p, c_void_p, c_void_p, c_void_p,
                                     c_void_p, c_void_p]),
         "gbf_domain_write_plots": (c_int, [c_void_p, ctypes.c_char_p, c_double]),

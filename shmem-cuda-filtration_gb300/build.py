@@ -20,7 +20,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", str(INC
 # Per-file extra flags. The one-kernel-per-function path rounds every
 # multiply and add separately like the CPU reference.
 EXTRA = {"gbf_eager.cu": ["-fmad=false"]}
-SOURCES = ["gbf_host.cpp", "gbf_fields.cpp", "gbf_tma.cpp", "gbf_checkpoint.cpp", "gbf_plots.cpp", "gbf_eager.cu", "gbf_f64.cu", "gbf_split.cu", "gbf_domain.cu", "gbf_dropin.cu",
+SOURCES = ["gbf_host.cpp", "gbf_fields.cpp", "gbf_tma.cpp", "gbf_checkpoint.cpp", "gbf_plots.cpp", "gbf_defines.cpp", "gbf_eager.cu", "gbf_f64.cu", "gbf_split.cu", "gbf_domain.cu", "gbf_dropin.cu",
            "gbf_ensemble.cu"]
 
 

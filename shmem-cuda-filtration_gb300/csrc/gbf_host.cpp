@@ -148,6 +148,7 @@ size_t gbf_abi_sizeof(int which) {
     case 0: return sizeof(gbf_model);
     case 1: return sizeof(gbf_cells);
     case 2: return sizeof(gbf_arrays);
+    case 3: return sizeof(gbf_run_defines);
     default: return 0;
   }
 }

@@ -54,6 +54,7 @@ def test_struct_layouts(abi, lib):
     assert lib.gbf_abi_sizeof(0) == ctypes.sizeof(abi.GbfModel)
     assert lib.gbf_abi_sizeof(1) == ctypes.sizeof(abi.GbfCells)
     assert lib.gbf_abi_sizeof(2) == ctypes.sizeof(abi.GbfArrays)
+    assert lib.gbf_abi_sizeof(3) == ctypes.sizeof(abi.GbfRunDefines)
 
 
 def test_reference_model_matches_library(abi, lib):
