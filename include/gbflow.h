@@ -139,6 +139,15 @@ int gbf_model_validate(const gbf_model* m, const gbf_cells* cells, int check_dt)
 int gbf_fill_lognormal_K(int nx, int ny, int nz, uint64_t seed, double K_geo, double sigma_lnK, double corr_cells,
                          float* K_out);
 int gbf_fill_porosity(int nx, int ny, int nz, uint64_t seed, double base, double amp, float* phi_out);
+/* The same fields generated on the device into device arrays (enqueued on
+   `stream`; the K generator returns after its work completed). Porosity is
+   bit-identical to gbf_fill_porosity; K equals gbf_fill_lognormal_K up to the
+   last-bit differences of the host's and the device's log, cos and exp, i.e.
+   within 1 FP32 ulp, in all but a handful of cells bit for bit. */
+int gbf_fill_lognormal_K_device(int nx, int ny, int nz, uint64_t seed, double K_geo, double sigma_lnK,
+                                double corr_cells, float* d_K, void* stream);
+int gbf_fill_porosity_device(int nx, int ny, int nz, uint64_t seed, double base, double amp, float* d_phi,
+                             void* stream);
 
 /* --------------------------- per-function device entry points (FP64) ----
  * Device pointers (`d_arrays`, `d_cells`), one CUDA stream (NULL = legacy

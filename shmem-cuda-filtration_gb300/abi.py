@@ -149,6 +149,10 @@ def _declare(lib) -> None:
         "gbf_fill_lognormal_K": (c_int, [c_int, c_int, c_int, ctypes.c_uint64, c_double, c_double, c_double,
                                          c_void_p]),
         "gbf_fill_porosity": (c_int, [c_int, c_int, c_int, ctypes.c_uint64, c_double, c_double, c_void_p]),
+        "gbf_fill_lognormal_K_device": (c_int, [c_int, c_int, c_int, ctypes.c_uint64, c_double, c_double, c_double,
+                                                c_void_p, c_void_p]),
+        "gbf_fill_porosity_device": (c_int, [c_int, c_int, c_int, ctypes.c_uint64, c_double, c_double, c_void_p,
+                                             c_void_p]),
         "gbf_domain_set_timing": (c_int, [c_void_p, c_int]),
         "gbf_domain_kernel_times": (c_int, [c_void_p, c_void_p, c_void_p, c_int]),
         "gbf_kernel_kinds": (c_int, []),

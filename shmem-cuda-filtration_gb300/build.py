@@ -18,9 +18,11 @@ INCLUDE = PKG.parent / "include"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", str(INCLUDE), "-I", str(CSRC)]
 # Per-file extra flags. The one-kernel-per-function path rounds every
-# multiply and add separately like the CPU reference.
-EXTRA = {"gbf_eager.cu": ["-fmad=false"]}
-SOURCES = ["gbf_host.cpp", "gbf_fields.cpp", "gbf_tma.cpp", "gbf_checkpoint.cpp", "gbf_plots.cpp", "gbf_defines.cpp", "gbf_eager.cu", "gbf_f64.cu", "gbf_split.cu", "gbf_domain.cu", "gbf_dropin.cu",
+# multiply and add separately like the CPU reference; so does the host field
+# generator (the same fields on x86 and Arm, and porosity bit-identical to
+# the device generator).
+EXTRA = {"gbf_eager.cu": ["-fmad=false"], "gbf_fields.cpp": ["-Xcompiler", "-ffp-contract=off"]}
+SOURCES = ["gbf_host.cpp", "gbf_fields.cpp", "gbf_tma.cpp", "gbf_checkpoint.cpp", "gbf_plots.cpp", "gbf_defines.cpp", "gbf_fields_gpu.cu", "gbf_eager.cu", "gbf_f64.cu", "gbf_split.cu", "gbf_domain.cu", "gbf_dropin.cu",
            "gbf_ensemble.cu"]
 
 
@@ -41,7 +43,7 @@ def _compile(src: pathlib.Path) -> pathlib.Path:
         return obj
     cmd = [nvcc(), *ARCH, *COMMON, *EXTRA.get(src.name, []), "-c", str(src), "-o", str(obj)]
     if src.suffix == ".cpp":
-        cmd = [nvcc(), *COMMON, "-x", "c++", "-c", str(src), "-o", str(obj)]
+        cmd = [nvcc(), *COMMON, *EXTRA.get(src.name, []), "-x", "c++", "-c", str(src), "-o", str(obj)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
