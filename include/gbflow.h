@@ -228,6 +228,12 @@ int gbf_set_tma(int on);
    0 forces staging; negative leaves the setting as it is; default 1. Returns
    the setting in force before the call. */
 int gbf_set_host_direct(int on);
+/* Diagnostic of the device-side failure detection: one block runs the TMA
+   tiles' bounded mbarrier wait on a barrier phase that never completes, with
+   `tries` rounds; it must give up and report GBF_ERR_TIMEOUT (no trap, the
+   context stays usable). *ms (may be NULL) receives the kernel's time. The
+   tiles use 2^18 rounds per wait (about 1 s on GB300). */
+int gbf_diag_bounded_wait(unsigned tries, double* ms);
 /* 1 if the object's split step stages planes by TMA, 0 if by plain loads. */
 int gbf_domain_uses_tma(gbf_domain* d);
 int gbf_ensemble_uses_tma(gbf_ensemble* e);

@@ -159,6 +159,7 @@ def _declare(lib) -> None:
         "gbf_kernel_name": (ctypes.c_char_p, [c_int]),
         "gbf_set_tma": (c_int, [c_int]),
         "gbf_set_host_direct": (c_int, [c_int]),
+        "gbf_diag_bounded_wait": (c_int, [ctypes.c_uint, ctypes.POINTER(c_double)]),
         "gbf_domain_uses_tma": (c_int, [c_void_p]),
         "gbf_ensemble_uses_tma": (c_int, [c_void_p]),
         "gbf_checkpoint_bytes": (c_size_t, [PM]),

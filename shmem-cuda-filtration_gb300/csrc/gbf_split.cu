@@ -334,3 +334,45 @@ int gbf_split_state_to_f64(const gbf_model& m, const float* dPf, const float* Sf
 }
 
 int gbf_split_launches_per_step(gbf_domain* d) { return 2 + ((d->out_flags & GBF_OUT_MASS) ? 1 : 0); }
+
+// ----------------------------------------------------------- diagnostics
+// The bounded mbarrier wait of the TMA tiles, run on a barrier phase that
+// never completes (arrival count 2, one arrival, no copy in flight): every
+// thread must give up after `tries` rounds and the block reports
+// GBF_DEV_TIMEOUT, as the tiles do when a plane never arrives.
+namespace {
+__global__ void k_diag_wait(unsigned tries, unsigned* status) {
+  __shared__ unsigned long long bar;
+  if (threadIdx.x == 0) {
+    gbf_mbar_init(&bar, 2);
+    gbf_mbar_fence_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(gbf_smem_u32(&bar)) : "memory");
+  const bool ok = gbf_mbar_wait(&bar, 0u, tries);
+  if (__syncthreads_or(!ok) && threadIdx.x == 0) atomicOr(status, GBF_DEV_TIMEOUT);
+}
+}  // namespace
+
+extern "C" int gbf_diag_bounded_wait(unsigned tries, double* ms) {
+  unsigned* st = nullptr;
+  GBF_CUDA(cudaMalloc((void**)&st, sizeof(unsigned)));
+  GBF_CUDA(cudaMemset(st, 0, sizeof(unsigned)));
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  cudaEventRecord(a, nullptr);
+  k_diag_wait<<<1, 256>>>(tries, st);
+  cudaEventRecord(b, nullptr);
+  unsigned h = 0;
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpy(&h, st, sizeof(unsigned), cudaMemcpyDeviceToHost);
+  float t = 0.f;
+  if (e == cudaSuccess) cudaEventElapsedTime(&t, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(st);
+  if (e != cudaSuccess) return gbf_cuda_check(e, "gbf_diag_bounded_wait");
+  if (ms) *ms = t;
+  return (h & GBF_DEV_TIMEOUT) ? gbf_fail(GBF_ERR_TIMEOUT, "bounded wait gave up (diagnostic)") : GBF_OK;
+}
