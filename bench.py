@@ -280,7 +280,10 @@ def run_ours(args, rank, world):
     run = Runner(pkg, members, prec, ensemble, cap)
     run.set_stream(stream.cuda_stream)
     tuning = None
-    if ensemble and prec != abi.GBF_PREC_F64 and not args.no_autotune:
+    if ensemble and prec != abi.GBF_PREC_F64 and args.tile >= 0:
+        run.set_tuning(args.tile, 0, 0)
+        tuning = run.tuning()
+    elif ensemble and prec != abi.GBF_PREC_F64 and not args.no_autotune:
         run.upload_initial()
         tuning = run.autotune(2)
     run.upload_initial()
@@ -460,6 +463,7 @@ def main():
     ap.add_argument("--no-compare", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-tma", action="store_true", help="stage split-step planes by plain loads, not TMA")
+    ap.add_argument("--tile", type=int, default=-1, help="ensemble tile shape (gbf_ensemble_set_tuning); skips autotune")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours" and not args.cube:
         args.warmup = 3

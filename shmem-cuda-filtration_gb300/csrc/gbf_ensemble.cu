@@ -44,8 +44,11 @@ struct EnsChunk {
   unsigned begin, end;
 };
 
-enum { kShape32x8 = 0, kShape64x4 = 1, kShape32x4 = 2, kShapes = 3 };
-const int kShapeTX[kShapes] = {32, 64, 32}, kShapeTY[kShapes] = {8, 4, 4};
+// Tile shapes (cells in x by rows); the last one is the x-pair TMA tile
+// (split_tile_x2: two cells per thread, TMA staging only).
+enum { kShape32x8 = 0, kShape64x4 = 1, kShape32x4 = 2, kShape64x8x2 = 3, kShapes = 4 };
+const int kShapeTX[kShapes] = {32, 64, 32, 64}, kShapeTY[kShapes] = {8, 4, 4, 8};
+const bool kShapePairs[kShapes] = {false, false, false, true};
 constexpr int kChunkCells = 16384, kBoundaryChunk = 4096, kThreads = 256;
 
 // ------------------------------------------------------------ split kernels
@@ -104,6 +107,63 @@ __global__ void __launch_bounds__(TX * TY, 1024 / (TX * TY)) k_ens_split_step(co
     const bool ok = split_tile<DF, TX, TY, TMA>(Cs, Gs, tl.y, tl.z, tl.w & 0xffff, tl.w >> 16, pl, acc, raw,
                                                 TMA ? maps + tl.x : nullptr, cur, &phases);
     if (!ok) break;  // a plane wait gave up (status set); the whole CTA stops
+    if (acc.bad) atomicOr(status, GBF_DEV_NONFINITE);
+    if (partials) split_block_mass<DF, NT>(acc, Cs.V, partials + 2 * t);
+    __syncthreads();
+  }
+}
+
+template <bool DF, int TXC, int TY>
+__global__ void __launch_bounds__(TXC / 2 * TY, 512 / (TXC / 2 * TY)) k_ens_split_step_x2(
+    const EnsMember* __restrict__ mem, const int4* __restrict__ tiles, int ntiles, int cur, unsigned* counter,
+    double* partials, unsigned* status, const GbfTmaSet* __restrict__ maps) {
+  extern __shared__ __align__(128) unsigned char dyn[];
+  GbfPairSmem<TXC, TY>& sm = *reinterpret_cast<GbfPairSmem<TXC, TY>*>(dyn);
+  __shared__ GbfSplitConsts Cs;
+  __shared__ GbfSplitGrid Gs;
+  __shared__ int s_tile;
+  constexpr int NT = TXC / 2 * TY;
+  unsigned phases = 0;  // barrier parities of the stages, carried from tile to tile
+  if (gbf_smem_u32(dyn) & 127u) {  // the TMA destinations need it; never expected to fire
+    if (threadIdx.x == 0) atomicOr(status, GBF_DEV_TIMEOUT);
+    return;
+  }
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kTmaStages; s++) gbf_mbar_init(&sm.ring.bar[s], 1);
+    for (int s = 0; s < GbfPairRing<TXC, TY>::RS; s++) gbf_mbar_init(&sm.ring.mbar[s], 1);
+    gbf_mbar_fence_init();
+  }
+  __syncthreads();
+  for (;;) {
+    if (threadIdx.x == 0) s_tile = (int)atomicAdd(counter, 1u);
+    __syncthreads();
+    const int t = s_tile;
+    if (t >= ntiles) break;
+    const int4 tl = tiles[t];
+    const EnsMember* me = mem + tl.x;
+    {
+      const int* src = reinterpret_cast<const int*>(&me->C);
+      int* dst = reinterpret_cast<int*>(&Cs);
+      for (int q = threadIdx.x; q < (int)(sizeof(GbfSplitConsts) / sizeof(int)); q += NT) dst[q] = src[q];
+    }
+    if (threadIdx.x == 0) {
+      Gs.dP = me->dPf[cur];
+      Gs.S = me->Sf[cur];
+      Gs.dPn = me->dPf[cur ^ 1];
+      Gs.Sn = me->Sf[cur ^ 1];
+      Gs.K = me->cells.K;
+      Gs.phi = me->cells.phi;
+      Gs.media = me->cells.media;
+      Gs.M1 = me->M1;
+      Gs.M2 = me->M2;
+      Gs.mass_partials = partials;
+      Gs.status = status;
+    }
+    __syncthreads();
+    GbfSplitAcc<DF> acc;
+    const bool ok = split_tile_x2<DF, TXC, TY>(Cs, Gs, tl.y, tl.z, tl.w & 0xffff, tl.w >> 16, sm, acc,
+                                               maps + tl.x, cur, &phases);
+    if (!ok) break;
     if (acc.bad) atomicOr(status, GBF_DEV_NONFINITE);
     if (partials) split_block_mass<DF, NT>(acc, Cs.V, partials + 2 * t);
     __syncthreads();
@@ -344,6 +404,16 @@ int kchunk_for(const gbf_ensemble* e, const gbf_model& m) {
   return std::min(kc, m.nz - 2);
 }
 
+// Whether every member can stage its planes by TMA for tiles TX cells wide:
+// FP32 K and phi fields, no media table, rows of whole 16-byte units.
+bool tma_possible(const gbf_ensemble* e, int TX) {
+  for (int r = 0; r < e->n; r++) {
+    const EnsMember& me = e->h_mem[r];
+    if (!(me.cells.K && me.cells.phi && !me.cells.media && gbf_tma_eligible(e->models[r].nx, TX))) return false;
+  }
+  return true;
+}
+
 // Packed work lists of the current tuning.
 int build_lists(gbf_ensemble* e) {
   e->tiles.clear();
@@ -366,9 +436,11 @@ int build_lists(gbf_ensemble* e) {
     if (split) {
       me.part_begin = (int)e->tiles.size();
       const int kc = kchunk_for(e, m);
+      // tiles start at i0 = 1 + t TX, or at x0 = t TX for the x-pair shape
+      const int first = kShapePairs[e->shape] ? 0 : 1;
       for (int k0 = 1; k0 < m.nz - 1; k0 += kc)
         for (int j0 = 1; j0 < m.ny - 1; j0 += TY)
-          for (int i0 = 1; i0 < m.nx - 1; i0 += TX) {
+          for (int i0 = first; i0 < m.nx - 1; i0 += TX) {
             const int k1 = std::min(k0 + kc, m.nz - 1);
             e->tiles.push_back(make_int4(r, i0, j0, k0 | (k1 << 16)));
           }
@@ -419,17 +491,25 @@ int build_lists(gbf_ensemble* e) {
     cudaFree(e->d_maps);
     e->d_maps = nullptr;
   }
-  bool tma = split;
-  for (int r = 0; r < e->n && tma; r++) {
-    const EnsMember& me = e->h_mem[r];
-    tma = me.cells.K && me.cells.phi && !me.cells.media && gbf_tma_eligible(e->models[r].nx, TX);
-  }
+  const bool tma = split && tma_possible(e, TX);
+  if (kShapePairs[e->shape] && !tma) return gbf_fail(GBF_ERR_ARG, "the x-pair tile needs TMA staging");
   if (tma && !s) {
     std::vector<GbfTmaSet> maps(e->n);
     int enc = GBF_OK;
     for (int r = 0; r < e->n && !enc; r++) {
       const EnsMember& me = e->h_mem[r];
       const gbf_model& m = e->models[r];
+      if (kShapePairs[e->shape]) {  // split_tile_x2 boxes: halo {TX + 8, TY + 2}, rows {TX, TY}
+        for (int b = 0; b < 2; b++) {
+          enc |= gbf_tma_encode_box(&maps[r].dP[b], me.dPf[b], 4, m.nx, m.ny, m.nz, TX + 8, TY + 2);
+          enc |= gbf_tma_encode_box(&maps[r].S[b], me.Sf[b], 4, m.nx, m.ny, m.nz, TX + 8, TY + 2);
+        }
+        enc |= gbf_tma_encode_box(&maps[r].K, me.cells.K, 4, m.nx, m.ny, m.nz, TX + 8, TY + 2);
+        enc |= gbf_tma_encode_box(&maps[r].M1, me.M1, 8, m.nx, m.ny, m.nz, TX, TY);
+        enc |= gbf_tma_encode_box(&maps[r].M2, me.M2, 8, m.nx, m.ny, m.nz, TX, TY);
+        enc |= gbf_tma_encode_box(&maps[r].phi, me.cells.phi, 4, m.nx, m.ny, m.nz, TX, TY);
+        continue;
+      }
       for (int b = 0; b < 2; b++) {
         enc |= gbf_tma_encode_plane(&maps[r].dP[b], me.dPf[b], m.nx, m.ny, m.nz, TX, TY);
         enc |= gbf_tma_encode_plane(&maps[r].S[b], me.Sf[b], m.nx, m.ny, m.nz, TX, TY);
@@ -468,9 +548,26 @@ int launch_split_step_t(gbf_ensemble* e, double* partials, cudaStream_t st, cons
   return GBF_OK;
 }
 
+template <bool DF, int TXC, int TY>
+int launch_split_step_x2(gbf_ensemble* e, double* partials, cudaStream_t st, const TileRange& tr) {
+  if (!e->d_maps) return gbf_fail(GBF_ERR_STATE, "x-pair tile without TMA maps");
+  auto kern = k_ens_split_step_x2<DF, TXC, TY>;
+  const int bytes = (int)sizeof(GbfPairSmem<TXC, TY>);
+  GBF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  int per_sm = 0;
+  GBF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TXC / 2 * TY, bytes));
+  const int blocks = std::max(1, std::min(tr.nt, std::max(1, per_sm) * gbf_num_sms()));
+  e->persistent_blocks = blocks;
+  kern<<<blocks, TXC / 2 * TY, bytes, st>>>(e->d_mem, e->d_tiles + tr.t0, tr.nt, tr.cur, tr.counter,
+                                             partials ? partials + 2 * (size_t)tr.t0 : nullptr, e->d_status,
+                                             e->d_maps);
+  return GBF_OK;
+}
+
 int launch_split_step(gbf_ensemble* e, double* partials, cudaStream_t st, const TileRange& tr) {
   const bool df = e->precision == GBF_PREC_SPLIT_DF;
   switch (e->shape) {
+    case kShape64x8x2: return df ? launch_split_step_x2<true, 64, 8>(e, partials, st, tr) : launch_split_step_x2<false, 64, 8>(e, partials, st, tr);
     case kShape64x4: return df ? launch_split_step_t<true, 64, 4>(e, partials, st, tr) : launch_split_step_t<false, 64, 4>(e, partials, st, tr);
     case kShape32x4: return df ? launch_split_step_t<true, 32, 4>(e, partials, st, tr) : launch_split_step_t<false, 32, 4>(e, partials, st, tr);
     default: return df ? launch_split_step_t<true, 32, 8>(e, partials, st, tr) : launch_split_step_t<false, 32, 8>(e, partials, st, tr);
@@ -927,9 +1024,15 @@ int gbf_ensemble_launches_per_step(gbf_ensemble* e) {
 int gbf_ensemble_set_tuning(gbf_ensemble* e, int shape, int edge, int kchunk) {
   if (!e || shape < -1 || shape >= kShapes || kchunk < 0) return gbf_fail(GBF_ERR_ARG, "gbf_ensemble_set_tuning");
   GBF_CUDA(cudaStreamSynchronize(e->stream));
+  const int prev = e->shape;
   if (shape >= 0) e->shape = shape;
   if (edge > 0) e->kchunk_by_edge[edge] = kchunk;
-  return build_lists(e);
+  int s = build_lists(e);
+  if (s && e->shape != prev) {  // e.g. the x-pair tile without TMA: keep the previous shape
+    e->shape = prev;
+    build_lists(e);
+  }
+  return s;
 }
 
 int gbf_ensemble_uses_tma(gbf_ensemble* e) { return e && e->d_maps ? 1 : 0; }
@@ -948,7 +1051,7 @@ int gbf_ensemble_get_tuning(gbf_ensemble* e, int* shape, int* edges, int* kchunk
 }
 
 const char* gbf_ensemble_shape_name(int shape) {
-  static const char* names[kShapes] = {"32x8", "64x4", "32x4"};
+  static const char* names[kShapes] = {"32x8", "64x4", "32x4", "64x8 pairs"};
   return (shape >= 0 && shape < kShapes) ? names[shape] : "";
 }
 
@@ -977,6 +1080,7 @@ int gbf_ensemble_autotune(gbf_ensemble* e, int trial_steps) {
   float best = 1e30f;
   int best_shape = e->shape;
   for (int sh = 0; sh < kShapes && !st; sh++) {
+    if (kShapePairs[sh] && !tma_possible(e, kShapeTX[sh])) continue;
     e->shape = sh;
     if ((st = build_lists(e))) break;
     float ms = 0;

@@ -83,33 +83,54 @@ constexpr int kThreads = 256;
 
 int tiles_x(const GbfSplitConsts& C) { return (C.nx - 2 + kSplitTX - 1) / kSplitTX; }
 int tiles_y(const GbfSplitConsts& C) { return (C.ny - 2 + kSplitTY - 1) / kSplitTY; }
+// x-pair tiles (TMA staging): 64 x 8 cells from x0 = 64 t, t such that x0 <= nx - 2
+constexpr int kPairTX = 64, kPairTY = 8;
+__host__ __device__ int tiles_x2(const GbfSplitConsts& C) { return (C.nx - 1 + kPairTX - 1) / kPairTX; }
+__host__ __device__ int tiles_y2(const GbfSplitConsts& C) { return (C.ny - 2 + kPairTY - 1) / kPairTY; }
 
-template <bool DF, bool TMA>
+// The plain-load tile on one grid (grids without TMA staging).
+template <bool DF>
 __global__ void __launch_bounds__(kSplitThreads, 4) k_split_step(const GbfSplitConsts C, const GbfSplitGrid G,
-                                                              const int kchunk, const GbfTmaSet* maps, int buf) {
-  __shared__ GbfSplitPlaneT<kSplitTX, kSplitTY, gbf_plane_pitch<kSplitTX, TMA>()> pl[TMA ? 3 : 2];
+                                                              const int kchunk) {
+  __shared__ GbfSplitPlane pl[2];
   const int ntx = (C.nx - 2 + kSplitTX - 1) / kSplitTX, nty = (C.ny - 2 + kSplitTY - 1) / kSplitTY;
   const int b = blockIdx.x;
   const int tx = b % ntx, ty = (b / ntx) % nty, kc = b / (ntx * nty);
   const int k0 = 1 + kc * kchunk;
   const int k1 = min(k0 + kchunk, C.nz - 1);
   GbfSplitAcc<DF> acc;
-  if constexpr (TMA) {
-    __shared__ __align__(128) GbfRawRing<kSplitTX, kSplitTY> raw;
-    if (threadIdx.x == 0) {
-      for (int s = 0; s < kTmaStages; s++) gbf_mbar_init(&raw.bar[s], 1);
-      for (int s = 0; s < GbfRawRing<kSplitTX, kSplitTY>::RS; s++) gbf_mbar_init(&raw.mbar[s], 1);
-      gbf_mbar_fence_init();
-    }
-    __syncthreads();
-    unsigned phases = 0;
-    split_tile<DF, kSplitTX, kSplitTY, true>(C, G, 1 + tx * kSplitTX, 1 + ty * kSplitTY, k0, k1, pl, acc, &raw,
-                                             maps, buf, &phases);
-  } else {
-    split_tile<DF>(C, G, 1 + tx * kSplitTX, 1 + ty * kSplitTY, k0, k1, pl, acc);
-  }
+  split_tile<DF>(C, G, 1 + tx * kSplitTX, 1 + ty * kSplitTY, k0, k1, pl, acc);
   if (acc.bad) atomicOr(G.status, GBF_DEV_NONFINITE);
   if (G.mass_partials) split_block_mass<DF>(acc, C.V, G.mass_partials + 2 * blockIdx.x);
+}
+
+// The x-pair tile on one grid: one tile (64 x 8 cells, a k range) per CTA.
+template <bool DF>
+__global__ void __launch_bounds__(kPairTX / 2 * kPairTY, 2) k_split_step_x2(const GbfSplitConsts C,
+                                                                         const GbfSplitGrid G, const int kchunk,
+                                                                         const GbfTmaSet* maps, int buf) {
+  extern __shared__ __align__(128) unsigned char dyn[];
+  GbfPairSmem<kPairTX, kPairTY>& sm = *reinterpret_cast<GbfPairSmem<kPairTX, kPairTY>*>(dyn);
+  if (gbf_smem_u32(dyn) & 127u) {  // the TMA destinations need it; never expected to fire
+    if (threadIdx.x == 0) atomicOr(G.status, GBF_DEV_TIMEOUT);
+    return;
+  }
+  const int ntx = tiles_x2(C), nty = tiles_y2(C);
+  const int b = blockIdx.x;
+  const int tx = b % ntx, ty = (b / ntx) % nty, kc = b / (ntx * nty);
+  const int k0 = 1 + kc * kchunk;
+  const int k1 = min(k0 + kchunk, C.nz - 1);
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kTmaStages; s++) gbf_mbar_init(&sm.ring.bar[s], 1);
+    for (int s = 0; s < GbfPairRing<kPairTX, kPairTY>::RS; s++) gbf_mbar_init(&sm.ring.mbar[s], 1);
+    gbf_mbar_fence_init();
+  }
+  __syncthreads();
+  unsigned phases = 0;
+  GbfSplitAcc<DF> acc;
+  split_tile_x2<DF, kPairTX, kPairTY>(C, G, kPairTX * tx, 1 + kPairTY * ty, k0, k1, sm, acc, maps, buf, &phases);
+  if (acc.bad) atomicOr(G.status, GBF_DEV_NONFINITE);
+  if (G.mass_partials) split_block_mass<DF, kPairTX / 2 * kPairTY>(acc, C.V, G.mass_partials + 2 * blockIdx.x);
 }
 
 __global__ void __launch_bounds__(kThreads) k_split_boundary(const gbf_model m, const GbfSplitGrid G, float H) {
@@ -170,22 +191,41 @@ int gbf_split_kchunk(const GbfSplitConsts& C) {
   return kchunk;
 }
 
+// k planes per x-pair CTA, by the same rule.
+int gbf_split_kchunk_x2(const GbfSplitConsts& C) {
+  const long long tiles = (long long)tiles_x2(C) * tiles_y2(C);
+  const long long want = 3LL * gbf_num_sms();  // two CTAs per SM
+  int chunks = (int)((want + tiles - 1) / tiles);
+  if (chunks < 1) chunks = 1;
+  int kchunk = (C.nz - 2 + chunks - 1) / chunks;
+  if (kchunk < 16) kchunk = 16;
+  return kchunk;
+}
+
+template <bool DF>
+int launch_x2(const GbfSplitConsts& C, const GbfSplitGrid& G, const GbfTmaSet* maps, int buf, cudaStream_t st,
+              unsigned& blocks) {
+  const int kchunk = gbf_split_kchunk_x2(C);
+  blocks = (unsigned)(tiles_x2(C) * tiles_y2(C) * ((C.nz - 2 + kchunk - 1) / kchunk));
+  const int bytes = (int)sizeof(GbfPairSmem<kPairTX, kPairTY>);
+  GBF_CUDA(cudaFuncSetAttribute(k_split_step_x2<DF>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  k_split_step_x2<DF><<<blocks, kPairTX / 2 * kPairTY, bytes, st>>>(C, G, kchunk, maps, buf);
+  return GBF_OK;
+}
+
 int gbf_split_launch_domain(const gbf_model& m, const GbfSplitConsts& C, const GbfSplitGrid& G, bool df,
                             double* mass_out, cudaStream_t st, GbfTimer* tm, const GbfTmaSet* maps, int buf) {
   const int kchunk = gbf_split_kchunk(C);
   const int nkc = (C.nz - 2 + kchunk - 1) / kchunk;
-  const unsigned blocks = (unsigned)(tiles_x(C) * tiles_y(C) * nkc);
+  unsigned blocks = (unsigned)(tiles_x(C) * tiles_y(C) * nkc);
   cudaEvent_t e = gbf_timer_begin(tm, st);
-  if (maps) {
-    if (df)
-      k_split_step<true, true><<<blocks, kSplitThreads, 0, st>>>(C, G, kchunk, maps, buf);
-    else
-      k_split_step<false, true><<<blocks, kSplitThreads, 0, st>>>(C, G, kchunk, maps, buf);
+  if (maps) {  // TMA staging: the x-pair tile
+    if (int s = df ? launch_x2<true>(C, G, maps, buf, st, blocks) : launch_x2<false>(C, G, maps, buf, st, blocks))
+      return s;
+  } else if (df) {
+    k_split_step<true><<<blocks, kSplitThreads, 0, st>>>(C, G, kchunk);
   } else {
-    if (df)
-      k_split_step<true, false><<<blocks, kSplitThreads, 0, st>>>(C, G, kchunk, nullptr, 0);
-    else
-      k_split_step<false, false><<<blocks, kSplitThreads, 0, st>>>(C, G, kchunk, nullptr, 0);
+    k_split_step<false><<<blocks, kSplitThreads, 0, st>>>(C, G, kchunk);
   }
   gbf_timer_end(tm, GBF_K_SPLIT_STEP, e, st);
   e = gbf_timer_begin(tm, st);
@@ -200,10 +240,13 @@ int gbf_split_launch_domain(const gbf_model& m, const GbfSplitConsts& C, const G
   return err == cudaSuccess ? GBF_OK : gbf_cuda_check(err, "gbf_split_launch_domain");
 }
 
+// Mass-partial slots: the larger of the two tilings' CTA counts.
 unsigned gbf_split_blocks(const gbf_model& m) {
   const GbfSplitConsts C = gbf_split_consts(m);
-  const int kchunk = gbf_split_kchunk(C);
-  return (unsigned)(tiles_x(C) * tiles_y(C) * ((C.nz - 2 + kchunk - 1) / kchunk));
+  const int kchunk = gbf_split_kchunk(C), kc2 = gbf_split_kchunk_x2(C);
+  const unsigned a = (unsigned)(tiles_x(C) * tiles_y(C) * ((C.nz - 2 + kchunk - 1) / kchunk));
+  const unsigned b = (unsigned)(tiles_x2(C) * tiles_y2(C) * ((C.nz - 2 + kc2 - 1) / kc2));
+  return a > b ? a : b;
 }
 
 // ----------------------------------------------------------------- host side
@@ -223,17 +266,19 @@ int gbf_split_alloc(gbf_domain* d) {
   if (s) return GBF_ERR_NOMEM;
   // TMA plane loads: FP32 K and phi fields, no media table, rows of whole 16-byte units
   const gbf_model& m = d->m;
-  if (d->cells.K && d->cells.phi && !d->cells.media && gbf_tma_eligible(m.nx, kSplitTX)) {
+  if (d->cells.K && d->cells.phi && !d->cells.media && gbf_tma_eligible(m.nx, kPairTX)) {
+    // boxes of the x-pair tile: halo planes {TX + 8, TY + 2}, interior rows {TX, TY}
     GbfTmaSet h;
     int e = GBF_OK;
+    const int hx = kPairTX + 8, hy = kPairTY + 2;
     for (int b = 0; b < 2 && !e; b++) {
-      e |= gbf_tma_encode_plane(&h.dP[b], d->Pf[b], m.nx, m.ny, m.nz, kSplitTX, kSplitTY);
-      e |= gbf_tma_encode_plane(&h.S[b], d->Sf[b], m.nx, m.ny, m.nz, kSplitTX, kSplitTY);
+      e |= gbf_tma_encode_box(&h.dP[b], d->Pf[b], 4, m.nx, m.ny, m.nz, hx, hy);
+      e |= gbf_tma_encode_box(&h.S[b], d->Sf[b], 4, m.nx, m.ny, m.nz, hx, hy);
     }
-    if (!e) e |= gbf_tma_encode_plane(&h.K, d->cells.K, m.nx, m.ny, m.nz, kSplitTX, kSplitTY);
-    if (!e) e |= gbf_tma_encode_rows(&h.M1, d->M1, 8, m.nx, m.ny, m.nz, kSplitTX, kSplitTY);
-    if (!e) e |= gbf_tma_encode_rows(&h.M2, d->M2, 8, m.nx, m.ny, m.nz, kSplitTX, kSplitTY);
-    if (!e) e |= gbf_tma_encode_rows(&h.phi, d->cells.phi, 4, m.nx, m.ny, m.nz, kSplitTX, kSplitTY);
+    if (!e) e |= gbf_tma_encode_box(&h.K, d->cells.K, 4, m.nx, m.ny, m.nz, hx, hy);
+    if (!e) e |= gbf_tma_encode_box(&h.M1, d->M1, 8, m.nx, m.ny, m.nz, kPairTX, kPairTY);
+    if (!e) e |= gbf_tma_encode_box(&h.M2, d->M2, 8, m.nx, m.ny, m.nz, kPairTX, kPairTY);
+    if (!e) e |= gbf_tma_encode_box(&h.phi, d->cells.phi, 4, m.nx, m.ny, m.nz, kPairTX, kPairTY);
     if (!e && !gbf_domain_alloc(d, &d->tma, sizeof(GbfTmaSet))) {
       GBF_CUDA(cudaMemcpy(d->tma, &h, sizeof(GbfTmaSet), cudaMemcpyHostToDevice));
     } else {

@@ -260,6 +260,168 @@ struct GbfSplitAcc {
   __device__ GbfSplitAcc() : m1(Wide<DF>::f(0.f)), m2(Wide<DF>::f(0.f)), bad(0) {}
 };
 
+// ------------------------------------------------------- one cell's update
+// Inputs of one cell at plane k: the cell, its x and y neighbours (y = the
+// vertical j), and its column at planes k - 1 and k + 1.
+struct GbfCellIn {
+  float dPc, S0, L1c, L2c;
+  float dPxm, dPxp, dPym, dPyp;
+  float L1xm, L1xp, L1ym, L1yp, L2xm, L2xp, L2ym, L2yp;
+  float dPm, L1m, L2m;
+  float dPp, L1p, L2p;
+  float phi;
+};
+template <bool DF>
+struct GbfCellOut {
+  float dPn, Sn;
+  typename Wide<DF>::T M1n, M2n;
+};
+
+// The fused a3 + a4 update of N interior cells of one row and plane
+// (cpu.cpp:218-320 in the split form): donor-cell fluxes, FP32 mass
+// increments, wide mass targets (rate source added exactly), the residual
+// split into its exact large part and FP32 small parts, and the FP32
+// increment Newton. Every operation is applied lane by lane in the same
+// order, so that N = 1 and N = 2 (two cells interleaved for instruction-level
+// parallelism) give each cell the same bits; the rare branches (rate source,
+// second Newton iteration) run for all lanes when any lane needs them and
+// select per lane. Lanes with count[n] false are computed but neither added
+// to the mass sums nor checked for non-finite values.
+template <bool DF, int N>
+__device__ __forceinline__ void split_cells(const GbfSplitConsts& C, const GbfCellIn (&in)[N],
+                                            const typename Wide<DF>::T (&M1)[N],
+                                            const typename Wide<DF>::T (&M2)[N], typename Wide<DF>::T R01,
+                                            typename Wide<DF>::T R02, int md, const int (&ci)[N], int j, int k,
+                                            bool phi_field, bool mass, const bool (&count)[N],
+                                            GbfSplitAcc<DF>& acc, GbfCellOut<DF> (&o)[N]) {
+  using W = Wide<DF>;
+  using WT = typename W::T;
+  const bool noflow = C.noflow_bottom && (j == C.ny - 2);
+  float Pp[N], dm1[N], dm2[N];
+  WT T1[N], T2[N];
+#pragma unroll
+  for (int n = 0; n < N; n++) {
+    const float dPc = in[n].dPc, L1c = in[n].L1c, L2c = in[n].L2c;
+    // face potentials relative to the hydrostatic profile (P2 = P1)
+    const float x1 = (in[n].dPxm - dPc) * C.inv_h1, x2 = (dPc - in[n].dPxp) * C.inv_h1;
+    const float yb1 = (in[n].dPym - dPc) * C.inv_h2;
+    const float yb2 = (dPc - in[n].dPyp) * C.inv_h2;
+    const float z1 = (in[n].dPm - dPc) * C.inv_h3, z2 = (dPc - in[n].dPp) * C.inv_h3;
+    Pp[n] = fmaf((float)j, C.H, dPc);  // P - P_atm
+    const float gd1 = C.g_ro01_b1 * Pp[n];  // (rho1 - rho01) g
+    const float gd2 = fmaf(C.g_ro02_b2, Pp[n], C.g_dro);
+    const float y11 = yb1 + gd1, y21 = noflow ? 0.f : yb2 + gd1;
+    const float y12 = yb1 + gd2, y22 = noflow ? 0.f : yb2 + gd2;
+    const float f = split_donor(x1, x2, L1c, in[n].L1xm, in[n].L1xp) * C.inv_h1 +
+                    C.kv * split_donor(y11, y21, L1c, in[n].L1ym, in[n].L1yp) * C.inv_h2 +
+                    split_donor(z1, z2, L1c, in[n].L1m, in[n].L1p) * C.inv_h3;
+    const float gs = split_donor(x1, x2, L2c, in[n].L2xm, in[n].L2xp) * C.inv_h1 +
+                     C.kv * split_donor(y12, y22, L2c, in[n].L2ym, in[n].L2yp) * C.inv_h2 +
+                     split_donor(z1, z2, L2c, in[n].L2m, in[n].L2p) * C.inv_h3;
+    const float dtphi = __fdividef(C.dt, in[n].phi);
+    dm1[n] = -dtphi * f;  // FP32 mass increments
+    dm2[n] = -dtphi * gs;
+    // mass targets T = M + dm (wide)
+    T1[n] = W::add_f(M1[n], dm1[n]);
+    T2[n] = W::add_f(M2[n], dm2[n]);
+  }
+  // the rate source, added exactly
+  float srcf[N];
+  bool insrc[N], anysrc = false;
+#pragma unroll
+  for (int n = 0; n < N; n++) {
+    srcf[n] = 0.f;
+    insrc[n] = j == 1 && ci[n] >= C.ri0 && ci[n] < C.ri0 + C.rn && k >= C.rk0 && k < C.rk0 + C.rn;
+    anysrc |= insrc[n];
+  }
+  if (anysrc) {
+#pragma unroll
+    for (int n = 0; n < N; n++) {
+      const WT src = phi_field ? W::div_f(W::c(C.dtsrc_d, C.dtsrc_df), in[n].phi)
+                               : W::c(C.dtsrc_m_d[md], C.dtsrc_m_df[md]);
+      const WT t2 = W::add(T2[n], src);
+      if (insrc[n]) {
+        T2[n] = t2;
+        srcf[n] = W::tof(src);
+      }
+    }
+  }
+  // residual r = F(P, S) - T at the stored state, cpu.cpp:305-306, split
+  // into its large part rho0 (1 - S) - M (wide; the products of FP32
+  // numbers are exact) and small FP32 parts rho0 beta P' (..) and dm:
+  //   r1 = (rho01 - M1 - rho01 S) + rho01 beta1 P' (1 - S) - dm1
+  //   r2 = (rho02 S - M2) + rho02 beta2 (P' + P_k) S - dm2 - src
+  // then the FP32 Newton on d = (dp, ds): r + [F(x + d) - F(x)] = 0, the
+  // bracket written in increments so that no large terms cancel. The
+  // equations are linear up to terms beta (dp ds, P_k'' ds^2): after the
+  // first (linear) iteration the residual is about rho0 beta |dp ds|; a
+  // second iteration runs when that could move S by more than 1e-9.
+  float r1[N], r2[N], a0[N], b0[N], Pk0[N], dPk0[N], dp[N], ds[N], Pk[N];
+  bool need[N], anyneed = false;
+#pragma unroll
+  for (int n = 0; n < N; n++) {
+    const float S0 = in[n].S0;
+    Pk0[n] = split_Pk(C, md, S0, dPk0[n]);
+    r1[n] = W::rho_1mS_minus(R01, M1[n], S0) + C.ro01b1 * Pp[n] * (1.f - S0) - dm1[n];
+    r2[n] = W::rhoS_minus(R02, M2[n], S0) + C.ro02b2 * (Pp[n] + Pk0[n]) * S0 - dm2[n] - srcf[n];
+    a0[n] = fmaf(C.beta1, Pp[n], 1.f);
+    b0[n] = fmaf(C.beta2, Pp[n] + Pk0[n], 1.f);
+    const float J11 = C.ro01b1 * (1.f - S0), J12 = -C.ro01 * a0[n];
+    const float J21 = C.ro02b2 * S0, J22 = C.ro02 * fmaf(C.beta2 * dPk0[n], S0, b0[n]);
+    const float inv = __fdividef(1.f, J11 * J22 - J12 * J21);
+    dp[n] = -inv * (J22 * r1[n] - J12 * r2[n]);
+    ds[n] = -inv * (J11 * r2[n] - J21 * r1[n]);
+    const float nl = fmaxf(C.beta1, C.beta2) * fabsf(ds[n]) * (fabsf(dp[n]) + 4.f * fabsf(dPk0[n] * ds[n]) + 1.f);
+    need[n] = nl > 1e-9f;
+    anyneed |= need[n];
+    Pk[n] = fmaf(dPk0[n], ds[n], Pk0[n]);
+  }
+  if (anyneed) {
+#pragma unroll
+    for (int n = 0; n < N; n++) {
+      const float S0 = in[n].S0;
+      float dPk1;
+      const float Pk1 = split_Pk(C, md, S0 + ds[n], dPk1);
+      const float S1 = S0 + ds[n];
+      const float G1 = r1[n] + C.ro01 * (C.beta1 * dp[n] * (1.f - S1) - a0[n] * ds[n]);
+      const float G2 = r2[n] + C.ro02 * (b0[n] * ds[n] + C.beta2 * (dp[n] + (Pk1 - Pk0[n])) * S1);
+      const float J11 = C.ro01b1 * (1.f - S1);
+      const float J12 = -C.ro01 * (a0[n] + C.beta1 * dp[n]);
+      const float J21 = C.ro02b2 * S1;
+      const float J22 = C.ro02 * (b0[n] + C.beta2 * (dp[n] + (Pk1 - Pk0[n])) + C.beta2 * dPk1 * S1);
+      const float inv = __fdividef(1.f, J11 * J22 - J12 * J21);
+      const float ep = inv * (J22 * G1 - J12 * G2);
+      const float es = inv * (J11 * G2 - J21 * G1);
+      if (need[n]) {
+        dp[n] -= ep;
+        ds[n] -= es;
+        Pk[n] = fmaf(-dPk1, es, Pk1);  // P_k at the final S, to first order in the last correction
+      }
+    }
+  }
+#pragma unroll
+  for (int n = 0; n < N; n++) {
+    o[n].dPn = in[n].dPc + dp[n];
+    o[n].Sn = in[n].S0 + ds[n];
+    o[n].M1n = T1[n];
+    // next step's ro2 S2 is taken at P2 = P1, without P_k (cpu.cpp:63 vs :306)
+    o[n].M2n = W::add_f(T2[n], -C.ro02b2 * Pk[n] * o[n].Sn);
+    if (count[n]) {
+      if (mass) {  // phi T in the wide type (phi exact: an FP32 input or a wide table value)
+        if (phi_field) {
+          acc.m1 = W::acc_phi(acc.m1, in[n].phi, T1[n]);
+          acc.m2 = W::acc_phi(acc.m2, in[n].phi, T2[n]);
+        } else {
+          const WT phw = W::c(C.m_d[md], C.m_df[md]);
+          acc.m1 = W::add(acc.m1, W::mul(phw, T1[n]));
+          acc.m2 = W::add(acc.m2, W::mul(phw, T2[n]));
+        }
+      }
+      if (!isfinite(o[n].dPn) || !isfinite(o[n].Sn)) acc.bad = 1;
+    }
+  }
+}
+
 // One CTA: interior cells [i0, i0+TX) x [j0, j0+TY) of planes [k0, k1); i0,
 // j0, k0 >= 1. `pl` points to two planes of shared memory.
 //
@@ -473,100 +635,29 @@ __device__ bool split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i
       const float phi = TMA ? raw->phi[sr][fi] : (G.phi ? __ldg(G.phi + c) : C.m[md]);
       const WT M1 = TMA ? W::load(raw->m1[sr], mi) : W::load(G.M1, c);
       const WT M2 = TMA ? W::load(raw->m2[sr], mi) : W::load(G.M2, c);
-      const float dPc = Pc.dP[hc], S0 = Pc.S[hc], L1c = Pc.L1[hc], L2c = Pc.L2[hc];
-      const float dPp = Pn.dP[hc], L1p = Pn.L1[hc], L2p = Pn.L2[hc];
-      // face potentials relative to the hydrostatic profile (P2 = P1)
-      const float x1 = (Pc.dP[hc - 1] - dPc) * C.inv_h1, x2 = (dPc - Pc.dP[hc + 1]) * C.inv_h1;
-      const float yb1 = (Pc.dP[hc - kSplitHX] - dPc) * C.inv_h2;
-      const float yb2 = (dPc - Pc.dP[hc + kSplitHX]) * C.inv_h2;
-      const float z1 = (dPm - dPc) * C.inv_h3, z2 = (dPc - dPp) * C.inv_h3;
-      const bool noflow = C.noflow_bottom && (j == ny - 2);
-      const float Pp = fmaf((float)j, C.H, dPc);  // P - P_atm
-      const float gd1 = C.g_ro01_b1 * Pp;         // (rho1 - rho01) g
-      const float gd2 = fmaf(C.g_ro02_b2, Pp, C.g_dro);
-      const float y11 = yb1 + gd1, y21 = noflow ? 0.f : yb2 + gd1;
-      const float y12 = yb1 + gd2, y22 = noflow ? 0.f : yb2 + gd2;
-      const float f = split_donor(x1, x2, L1c, Pc.L1[hc - 1], Pc.L1[hc + 1]) * C.inv_h1 +
-                      C.kv * split_donor(y11, y21, L1c, Pc.L1[hc - kSplitHX], Pc.L1[hc + kSplitHX]) * C.inv_h2 +
-                      split_donor(z1, z2, L1c, L1m, L1p) * C.inv_h3;
-      const float gs = split_donor(x1, x2, L2c, Pc.L2[hc - 1], Pc.L2[hc + 1]) * C.inv_h1 +
-                       C.kv * split_donor(y12, y22, L2c, Pc.L2[hc - kSplitHX], Pc.L2[hc + kSplitHX]) * C.inv_h2 +
-                       split_donor(z1, z2, L2c, L2m, L2p) * C.inv_h3;
-      const float dtphi = __fdividef(C.dt, phi);
-      const float dm1 = -dtphi * f, dm2 = -dtphi * gs;  // FP32 mass increments
-      // mass targets T = M + dm (wide), the rate source added exactly
-      const WT T1 = W::add_f(M1, dm1);
-      WT T2 = W::add_f(M2, dm2);
-      float srcf = 0.f;
-      if (j == 1 && i >= C.ri0 && i < C.ri0 + C.rn && k >= C.rk0 && k < C.rk0 + C.rn) {
-        const WT src = G.phi ? W::div_f(W::c(C.dtsrc_d, C.dtsrc_df), phi) : W::c(C.dtsrc_m_d[md], C.dtsrc_m_df[md]);
-        T2 = W::add(T2, src);
-        srcf = W::tof(src);
-      }
-      // residual r = F(P, S) - T at the stored state, cpu.cpp:305-306, split
-      // into its large part rho0 (1 - S) - M (wide; the products of FP32
-      // numbers are exact) and small FP32 parts rho0 beta P' (..) and dm:
-      //   r1 = (rho01 - M1 - rho01 S) + rho01 beta1 P' (1 - S) - dm1
-      //   r2 = (rho02 S - M2) + rho02 beta2 (P' + P_k) S - dm2 - src
-      float dPk0;
-      const float Pk0 = split_Pk(C, md, S0, dPk0);
-      const float r1 = W::rho_1mS_minus(R01, M1, S0) + C.ro01b1 * Pp * (1.f - S0) - dm1;
-      const float r2 = W::rhoS_minus(R02, M2, S0) + C.ro02b2 * (Pp + Pk0) * S0 - dm2 - srcf;
-      // FP32 Newton on d = (dp, ds): r + [F(x + d) - F(x)] = 0, the bracket
-      // written in increments so that no large terms cancel. The equations
-      // are linear up to terms beta (dp ds, P_k'' ds^2): after the first
-      // (linear) iteration the residual is about rho0 beta |dp ds|; a second
-      // iteration runs when that could move S by more than 1e-9.
-      const float a0 = fmaf(C.beta1, Pp, 1.f);
-      const float b0 = fmaf(C.beta2, Pp + Pk0, 1.f);
-      float dp, ds, Pk;
-      {
-        const float J11 = C.ro01b1 * (1.f - S0), J12 = -C.ro01 * a0;
-        const float J21 = C.ro02b2 * S0, J22 = C.ro02 * fmaf(C.beta2 * dPk0, S0, b0);
-        const float inv = __fdividef(1.f, J11 * J22 - J12 * J21);
-        dp = -inv * (J22 * r1 - J12 * r2);
-        ds = -inv * (J11 * r2 - J21 * r1);
-      }
-      const float nl = fmaxf(C.beta1, C.beta2) * fabsf(ds) * (fabsf(dp) + 4.f * fabsf(dPk0 * ds) + 1.f);
-      if (nl > 1e-9f) {
-        float dPk1;
-        const float Pk1 = split_Pk(C, md, S0 + ds, dPk1);
-        const float S1 = S0 + ds;
-        const float G1 = r1 + C.ro01 * (C.beta1 * dp * (1.f - S1) - a0 * ds);
-        const float G2 = r2 + C.ro02 * (b0 * ds + C.beta2 * (dp + (Pk1 - Pk0)) * S1);
-        const float J11 = C.ro01b1 * (1.f - S1);
-        const float J12 = -C.ro01 * (a0 + C.beta1 * dp);
-        const float J21 = C.ro02b2 * S1;
-        const float J22 = C.ro02 * (b0 + C.beta2 * (dp + (Pk1 - Pk0)) + C.beta2 * dPk1 * S1);
-        const float inv = __fdividef(1.f, J11 * J22 - J12 * J21);
-        const float ep = inv * (J22 * G1 - J12 * G2);
-        const float es = inv * (J11 * G2 - J21 * G1);
-        dp -= ep;
-        ds -= es;
-        Pk = fmaf(-dPk1, es, Pk1);  // P_k at the final S, to first order in the last correction
-      } else {
-        Pk = fmaf(dPk0, ds, Pk0);
-      }
-      const float dPn = dPc + dp, Sn = S0 + ds;
-      G.dPn[c] = dPn;
-      G.Sn[c] = Sn;
-      W::store(G.M1, c, T1);
-      // next step's ro2 S2 is taken at P2 = P1, without P_k (cpu.cpp:63 vs :306)
-      W::store(G.M2, c, W::add_f(T2, -C.ro02b2 * Pk * Sn));
-      if (G.mass_partials) {  // phi T in the wide type (phi exact: an FP32 input or a wide table value)
-        if (G.phi) {
-          acc.m1 = W::acc_phi(acc.m1, phi, T1);
-          acc.m2 = W::acc_phi(acc.m2, phi, T2);
-        } else {
-          const WT phw = W::c(C.m_d[md], C.m_df[md]);
-          acc.m1 = W::add(acc.m1, W::mul(phw, T1));
-          acc.m2 = W::add(acc.m2, W::mul(phw, T2));
-        }
-      }
-      if (!isfinite(dPn) || !isfinite(Sn)) acc.bad = 1;
-      dPm = dPc;
-      L1m = L1c;
-      L2m = L2c;
+      GbfCellIn in;
+      in.dPc = Pc.dP[hc]; in.S0 = Pc.S[hc]; in.L1c = Pc.L1[hc]; in.L2c = Pc.L2[hc];
+      in.dPxm = Pc.dP[hc - 1]; in.dPxp = Pc.dP[hc + 1];
+      in.dPym = Pc.dP[hc - kSplitHX]; in.dPyp = Pc.dP[hc + kSplitHX];
+      in.L1xm = Pc.L1[hc - 1]; in.L1xp = Pc.L1[hc + 1]; in.L1ym = Pc.L1[hc - kSplitHX]; in.L1yp = Pc.L1[hc + kSplitHX];
+      in.L2xm = Pc.L2[hc - 1]; in.L2xp = Pc.L2[hc + 1]; in.L2ym = Pc.L2[hc - kSplitHX]; in.L2yp = Pc.L2[hc + kSplitHX];
+      in.dPm = dPm; in.L1m = L1m; in.L2m = L2m;
+      in.dPp = Pn.dP[hc]; in.L1p = Pn.L1[hc]; in.L2p = Pn.L2[hc];
+      in.phi = phi;
+      const GbfCellIn ins[1] = {in};
+      const WT m1s[1] = {M1}, m2s[1] = {M2};
+      const int cis[1] = {i};
+      const bool cnt[1] = {true};
+      GbfCellOut<DF> os[1];
+      split_cells<DF, 1>(C, ins, m1s, m2s, R01, R02, md, cis, j, k, G.phi != nullptr, G.mass_partials != nullptr,
+                         cnt, acc, os);
+      G.dPn[c] = os[0].dPn;
+      G.Sn[c] = os[0].Sn;
+      W::store(G.M1, c, os[0].M1n);
+      W::store(G.M2, c, os[0].M2n);
+      dPm = in.dPc;
+      L1m = in.L1c;
+      L2m = in.L2c;
     }
     if constexpr (!TMA) {
       __syncthreads();
@@ -657,4 +748,251 @@ __device__ __forceinline__ void split_block_mass(const GbfSplitAcc<DF>& acc, dou
     out2[0] = x * V;
     out2[1] = y * V;
   }
+}
+
+// ------------------------------------------------ x-pair tile (TMA only)
+// A CTA of (TXC / 2) x TY threads owns TXC x TY cells; each thread updates the
+// two cells x0 + 2 tx, x0 + 2 tx + 1 of row j0 + ty (tiles start at
+// x0 = TXC * t, a multiple of 16 bytes). The halo box of a plane starts at
+// x0 - 4 (16-byte aligned, zeros left of the grid) and is TXC + 8 wide, so a
+// thread's pair sits at an even offset: its x-stencil is three 64-bit
+// shared loads, its y neighbours and the plane above two more per field.
+// The interior rows of M1, M2 and phi arrive as {TXC, TY} boxes at x0 (no
+// halo). Shared memory exceeds the static 48 KB, so the kernel takes it as
+// dynamic shared memory (GbfPairSmem).
+template <int TXC, int TY>
+struct GbfPairRing {
+  static_assert(TXC % 32 == 0 && TXC <= 248, "x-pair tile width");
+  static constexpr int BX = TXC + 8, HY = TY + 2, N = BX * HY, NP = (N + 31) / 32 * 32;
+  static constexpr int NR = TXC * TY;  // interior-row elements per field
+  static constexpr int RS = 3;
+  static constexpr unsigned kHaloBytes = 3u * N * 4u;
+  static constexpr unsigned kRowsBytes = (unsigned)NR * (8u + 8u + 4u);
+  float v[kTmaStages][3][NP];
+  double m1[RS][NR], m2[RS][NR];
+  float phi[RS][NR];
+  unsigned long long bar[kTmaStages], mbar[RS];
+};
+template <int TXC, int TY>
+struct GbfPairSmem {
+  GbfPairRing<TXC, TY> ring;
+  float dP[kTmaStages][GbfPairRing<TXC, TY>::NP], S[kTmaStages][GbfPairRing<TXC, TY>::NP];
+  float L1[kTmaStages][GbfPairRing<TXC, TY>::NP], L2[kTmaStages][GbfPairRing<TXC, TY>::NP];
+};
+
+__device__ __forceinline__ float2 gbf_ld2(const float* p) { return *reinterpret_cast<const float2*>(p); }
+__device__ __forceinline__ void gbf_st2(float* p, float a, float b) { *reinterpret_cast<float2*>(p) = make_float2(a, b); }
+
+template <bool DF> struct WidePair;
+template <> struct WidePair<false> {  // FP64 masses: two doubles
+  static __device__ __forceinline__ void load(const double* p, double& a, double& b) {
+    const double2 v = *reinterpret_cast<const double2*>(p);
+    a = v.x;
+    b = v.y;
+  }
+  static __device__ __forceinline__ void store(double* p, double a, double b) {
+    *reinterpret_cast<double2*>(p) = make_double2(a, b);
+  }
+};
+template <> struct WidePair<true> {  // FP32-pair masses: four floats
+  static __device__ __forceinline__ void load(const double* p, GbfDF& a, GbfDF& b) {
+    const float4 v = *reinterpret_cast<const float4*>(p);
+    a = {v.x, v.y};
+    b = {v.z, v.w};
+  }
+  static __device__ __forceinline__ void store(double* p, GbfDF a, GbfDF b) {
+    *reinterpret_cast<float4*>(p) = make_float4(a.hi, a.lo, b.hi, b.lo);
+  }
+};
+
+// The x-pair z-marching tile: cells x0 .. x0 + TXC - 1 (interior ones only)
+// of rows j0 .. j0 + TY - 1, planes k0 .. k1 - 1. Same staging protocol,
+// bounded waits and give-up as split_tile<..., TMA = true>; each cell is
+// updated by split_cell, so results equal the other tiles' bit for bit.
+template <bool DF, int TXC, int TY>
+__device__ bool split_tile_x2(const GbfSplitConsts& C, const GbfSplitGrid& G, int x0, int j0, int k0, int k1,
+                              GbfPairSmem<TXC, TY>& sm, GbfSplitAcc<DF>& acc, const GbfTmaSet* maps, int buf,
+                              unsigned* phases) {
+  using W = Wide<DF>;
+  using WT = typename W::T;
+  using Ring = GbfPairRing<TXC, TY>;
+  constexpr int THX = TXC / 2, NT = THX * TY, BX = Ring::BX, HY = Ring::HY, RS = Ring::RS;
+  constexpr int PCOLS = (TXC + 4) / 2;  // pair columns 1 .. PCOLS of the box (columns 2 .. TXC + 5)
+  constexpr int NPAIR = PCOLS * HY, SLOTS = (NPAIR + NT - 1) / NT;
+  GbfPairRing<TXC, TY>& raw = sm.ring;
+  const int nx = C.nx, ny = C.ny;
+  const unsigned pln = (unsigned)nx * (unsigned)ny;
+  const int tx = threadIdx.x % THX, ty = threadIdx.x / THX;
+  const int ia = x0 + 2 * tx, j = j0 + ty;
+  const bool row_ok = j <= ny - 2;
+  const bool act_a = row_ok && ia >= 1 && ia <= nx - 2;
+  const bool act_b = row_ok && ia + 1 <= nx - 2;
+  const bool any = row_ok && ia <= nx - 2;  // the pair lies in the grid's row (cell b at most nx - 1)
+  const int hc = (ty + 1) * BX + 2 * tx + 4;  // own pair in the plane buffers (even)
+  const int mi = ty * TXC + 2 * tx;           // own pair in the rows boxes (even)
+
+  // halo pairs of this thread: even plane index, global row (rows or columns
+  // outside the grid hold zeros and give finite, unused properties)
+  int hq[SLOTS], hj[SLOTS];
+#pragma unroll
+  for (int s = 0; s < SLOTS; s++) {
+    const int q = threadIdx.x + s * NT;
+    hq[s] = -1;
+    hj[s] = 0;
+    if (q < NPAIR) {
+      const int r = q / PCOLS, c2 = 1 + q % PCOLS;
+      hq[s] = r * BX + 2 * c2;
+      hj[s] = j0 - 1 + r;
+    }
+  }
+
+  unsigned pend = 0;
+  int h_issue = 0, r_issue = 0;
+  auto issue = [&](int p) {
+    const int s = h_issue;
+    h_issue = s == kTmaStages - 1 ? 0 : s + 1;
+    if (threadIdx.x == 0) {
+      gbf_mbar_expect_tx(&raw.bar[s], Ring::kHaloBytes);
+      gbf_tma_plane(raw.v[s][0], &maps->dP[buf], x0 - 4, j0 - 1, p, &raw.bar[s]);
+      gbf_tma_plane(raw.v[s][1], &maps->S[buf], x0 - 4, j0 - 1, p, &raw.bar[s]);
+      gbf_tma_plane(raw.v[s][2], &maps->K, x0 - 4, j0 - 1, p, &raw.bar[s]);
+    }
+    pend |= 1u << s;
+  };
+  auto issue_rows = [&](int p) {
+    const int s = r_issue;
+    r_issue = s == RS - 1 ? 0 : s + 1;
+    if (threadIdx.x == 0) {
+      gbf_mbar_expect_tx(&raw.mbar[s], Ring::kRowsBytes);
+      gbf_tma_plane(raw.m1[s], &maps->M1, x0, j0, p, &raw.mbar[s]);
+      gbf_tma_plane(raw.m2[s], &maps->M2, x0, j0, p, &raw.mbar[s]);
+      gbf_tma_plane(raw.phi[s], &maps->phi, x0, j0, p, &raw.mbar[s]);
+    }
+    pend |= 1u << (8 + s);
+  };
+  auto wait_bit = [&](int bit) -> bool {
+    unsigned long long* b = bit < 8 ? &raw.bar[bit] : &raw.mbar[bit - 8];
+    if (!gbf_mbar_wait(b, (*phases >> bit) & 1u, kTmaWaitTries)) return false;
+    *phases ^= 1u << bit;
+    pend &= ~(1u << bit);
+    return true;
+  };
+  auto give_up = [&]() {
+    for (int bit = 0; bit < 16; bit++)
+      if ((pend >> bit) & 1u) {
+        unsigned long long* b = bit < 8 ? &raw.bar[bit] : &raw.mbar[bit - 8];
+        gbf_mbar_wait(b, (*phases >> bit) & 1u, kTmaDrainTries);
+        *phases ^= 1u << bit;
+      }
+    pend = 0;
+    if (threadIdx.x == 0) atomicOr(G.status, GBF_DEV_TIMEOUT);
+  };
+  auto build = [&](int s) {  // plane buffer s from halo stage s
+#pragma unroll
+    for (int q = 0; q < SLOTS; q++) {
+      if (hq[q] >= 0) {
+        const int e = hq[q];
+        const float2 p = gbf_ld2(&raw.v[s][0][e]), sv = gbf_ld2(&raw.v[s][1][e]), kv = gbf_ld2(&raw.v[s][2][e]);
+        float l1a, l2a, l1b, l2b;
+        split_props(C, 0, kv.x, p.x, sv.x, hj[q], l1a, l2a);
+        split_props(C, 0, kv.y, p.y, sv.y, hj[q], l1b, l2b);
+        gbf_st2(&sm.dP[s][e], p.x, p.y);
+        gbf_st2(&sm.S[s][e], sv.x, sv.y);
+        gbf_st2(&sm.L1[s][e], l1a, l1b);
+        gbf_st2(&sm.L2[s][e], l2a, l2b);
+      }
+    }
+  };
+
+  // prologue: own pair at k0 - 1 (registers), plane k0 (shared)
+  for (int q = 0; q < kTmaStages && k0 + q <= k1; q++) issue(k0 + q);
+  for (int q = 0; q < RS && k0 + q < k1; q++) issue_rows(k0 + q);
+  float dPma = 0.f, L1ma = 0.f, L2ma = 0.f, dPmb = 0.f, L1mb = 0.f, L2mb = 0.f;
+  if (any) {
+    const unsigned c = (unsigned)(ia + j * nx) + (unsigned)(k0 - 1) * pln;
+    const float2 p = gbf_ld2(G.dP + c), sv = gbf_ld2(G.S + c), kv = gbf_ld2(G.K + c);
+    dPma = p.x;
+    dPmb = p.y;
+    split_props(C, 0, kv.x, p.x, sv.x, j, L1ma, L2ma);
+    split_props(C, 0, kv.y, p.y, sv.y, j, L1mb, L2mb);
+  }
+  {
+    const bool ok = wait_bit(0);
+    if (ok) build(0);
+    if (__syncthreads_or(!ok)) {
+      give_up();
+      return false;
+    }
+    if (k0 + kTmaStages <= k1) issue(k0 + kTmaStages);
+  }
+  const WT R01 = W::c(C.ro01_d, C.ro01_df), R02 = W::c(C.ro02_d, C.ro02_df);
+  int t_cur = 0, t_next = 1, t_rows = 0;
+  for (int k = k0; k < k1; k++) {
+    {
+      const int sn = t_next;
+      bool ok = wait_bit(sn);
+      ok = ok && wait_bit(8 + t_rows);
+      if (ok) build(sn);
+      if (__syncthreads_or(!ok)) {
+        give_up();
+        return false;
+      }
+      if (k + 1 + kTmaStages <= k1) issue(k + 1 + kTmaStages);
+      if (k > k0 && k - 1 + RS < k1) issue_rows(k - 1 + RS);
+    }
+    if (any) {
+      const float* Pd = sm.dP[t_cur];
+      const float* P1 = sm.L1[t_cur];
+      const float* P2 = sm.L2[t_cur];
+      const float2 d0 = gbf_ld2(Pd + hc), dl = gbf_ld2(Pd + hc - 2), dr = gbf_ld2(Pd + hc + 2);
+      const float2 du = gbf_ld2(Pd + hc - BX), dd = gbf_ld2(Pd + hc + BX);
+      const float2 a0 = gbf_ld2(P1 + hc), al = gbf_ld2(P1 + hc - 2), ar = gbf_ld2(P1 + hc + 2);
+      const float2 au = gbf_ld2(P1 + hc - BX), ad = gbf_ld2(P1 + hc + BX);
+      const float2 b0 = gbf_ld2(P2 + hc), bl = gbf_ld2(P2 + hc - 2), br = gbf_ld2(P2 + hc + 2);
+      const float2 bu = gbf_ld2(P2 + hc - BX), bd = gbf_ld2(P2 + hc + BX);
+      const float2 s0 = gbf_ld2(sm.S[t_cur] + hc);
+      const float2 dp = gbf_ld2(sm.dP[t_next] + hc), ap = gbf_ld2(sm.L1[t_next] + hc),
+                   bp = gbf_ld2(sm.L2[t_next] + hc);
+      const float2 ph = gbf_ld2(&raw.phi[t_rows][mi]);
+      WT M1a, M1b, M2a, M2b;
+      WidePair<DF>::load(&raw.m1[t_rows][mi], M1a, M1b);
+      WidePair<DF>::load(&raw.m2[t_rows][mi], M2a, M2b);
+      GbfCellIn in[2];
+      // cell a
+      in[0].dPc = d0.x; in[0].S0 = s0.x; in[0].L1c = a0.x; in[0].L2c = b0.x;
+      in[0].dPxm = dl.y; in[0].dPxp = d0.y; in[0].dPym = du.x; in[0].dPyp = dd.x;
+      in[0].L1xm = al.y; in[0].L1xp = a0.y; in[0].L1ym = au.x; in[0].L1yp = ad.x;
+      in[0].L2xm = bl.y; in[0].L2xp = b0.y; in[0].L2ym = bu.x; in[0].L2yp = bd.x;
+      in[0].dPm = dPma; in[0].L1m = L1ma; in[0].L2m = L2ma;
+      in[0].dPp = dp.x; in[0].L1p = ap.x; in[0].L2p = bp.x;
+      in[0].phi = ph.x;
+      // cell b
+      in[1].dPc = d0.y; in[1].S0 = s0.y; in[1].L1c = a0.y; in[1].L2c = b0.y;
+      in[1].dPxm = d0.x; in[1].dPxp = dr.x; in[1].dPym = du.y; in[1].dPyp = dd.y;
+      in[1].L1xm = a0.x; in[1].L1xp = ar.x; in[1].L1ym = au.y; in[1].L1yp = ad.y;
+      in[1].L2xm = b0.x; in[1].L2xp = br.x; in[1].L2ym = bu.y; in[1].L2yp = bd.y;
+      in[1].dPm = dPmb; in[1].L1m = L1mb; in[1].L2m = L2mb;
+      in[1].dPp = dp.y; in[1].L1p = ap.y; in[1].L2p = bp.y;
+      in[1].phi = ph.y;
+      const WT m1s[2] = {M1a, M1b}, m2s[2] = {M2a, M2b};
+      const int cis[2] = {ia, ia + 1};
+      const bool cnt[2] = {act_a, act_b};
+      GbfCellOut<DF> o[2];
+      split_cells<DF, 2>(C, in, m1s, m2s, R01, R02, 0, cis, j, k, true, G.mass_partials != nullptr, cnt, acc, o);
+      // cells outside the interior (boundary cell 0 or nx - 1 of the pair) keep their values
+      const GbfCellOut<DF> oa = act_a ? o[0] : GbfCellOut<DF>{d0.x, s0.x, M1a, M2a};
+      const GbfCellOut<DF> ob = act_b ? o[1] : GbfCellOut<DF>{d0.y, s0.y, M1b, M2b};
+      const unsigned c = (unsigned)(ia + j * nx) + (unsigned)k * pln;  // even: nx and ia are
+      gbf_st2(G.dPn + c, oa.dPn, ob.dPn);
+      gbf_st2(G.Sn + c, oa.Sn, ob.Sn);
+      WidePair<DF>::store(G.M1 + c, oa.M1n, ob.M1n);
+      WidePair<DF>::store(G.M2 + c, oa.M2n, ob.M2n);
+      dPma = d0.x; L1ma = a0.x; L2ma = b0.x;
+      dPmb = d0.y; L1mb = a0.y; L2mb = b0.y;
+    }
+    t_cur = t_next;
+    t_next = t_next == kTmaStages - 1 ? 0 : t_next + 1;
+    t_rows = t_rows == RS - 1 ? 0 : t_rows + 1;
+  }
+  return true;
 }

@@ -74,6 +74,10 @@ int gbf_tma_encode_rows(void* map_out, const void* base, int elem_bytes, int nx,
   return encode(map_out, base, elem_bytes, nx, ny, nz, elem_bytes == 8 ? gbf_tma_rows_x8(TX) : gbf_tma_box_x(TX), TY);
 }
 
+int gbf_tma_encode_box(void* map_out, const void* base, int elem_bytes, int nx, int ny, int nz, int bx, int by) {
+  return encode(map_out, base, elem_bytes, nx, ny, nz, bx, by);
+}
+
 extern "C" int gbf_set_tma(int on) {
   if (on < 0) return g_tma_on.load();
   return g_tma_on.exchange(on ? 1 : 0);

@@ -24,6 +24,9 @@ int gbf_tma_encode_plane(void* map_out, const float* base, int nx, int ny, int n
 // {gbf_tma_box_x(TX) or gbf_tma_rows_x8(TX), TY, 1}.
 int gbf_tma_encode_rows(void* map_out, const void* base, int elem_bytes, int nx, int ny, int nz, int TX, int TY);
 
+// Any {bx, by, 1} box of a field of 4- or 8-byte elements.
+int gbf_tma_encode_box(void* map_out, const void* base, int elem_bytes, int nx, int ny, int nz, int bx, int by);
+
 // The plane maps of one grid: halo planes of dP and S (both state buffers)
 // and K; interior rows of the phase masses M1, M2 (8 bytes a cell) and phi.
 struct GbfTmaSet {

@@ -89,7 +89,7 @@ def test_ensemble_members_equal_single_domains(gpu_lib, abi, pkg, p):
         d.step(steps)
         single.append((d.download("P1"), d.download("S2"), d.mass_history(steps)))
         d.close()
-    shapes = [0] if p == "f64" else [0, 1, 2]
+    shapes = [0] if p == "f64" else [0, 1, 2, 3]  # 3: two cells per thread (TMA staging)
     for shape in shapes:
         ens = E.Ensemble(mems, precision=prec(abi, p))
         if p != "f64":
@@ -164,7 +164,7 @@ def test_ensemble_autotune(gpu_lib, abi, pkg):
     ens = E.Ensemble(mems, precision=abi.GBF_PREC_SPLIT_DF)
     ens.upload_initial()
     tuning = ens.autotune(2)
-    assert tuning["tile"] in ("32x8", "64x4", "32x4")
+    assert tuning["tile"] in ("32x8", "64x4", "32x4", "64x8 pairs")
     assert set(tuning["kchunk_by_edge"]) == {m.model.nx for m in mems}
     # after tuning, a fresh run still equals the default-tuned one
     ens.upload_initial()
@@ -188,12 +188,17 @@ def test_ensemble_tma_staging_equals_plain_loads(gpu_lib, abi, pkg, p):
     steps = 12
     prev = gpu_lib.gbf_set_tma(-1)
     try:
-        for shape in (0, 1, 2):
+        for shape in (0, 1, 2, 3):
             res = {}
             for tma in (1, 0):
                 gpu_lib.gbf_set_tma(tma)
                 ens = E.Ensemble(mems, precision=prec(abi, p))
-                ens.set_tuning(shape, 0, 0)
+                if shape == 3 and not tma:  # the x-pair tile has no plain-load form
+                    assert gpu_lib.gbf_ensemble_set_tuning(ens.h, 3, 0, 0) == abi.GBF_ERR_ARG
+                    gpu_lib.gbf_clear_status()
+                    ens.set_tuning(0, 0, 0)
+                else:
+                    ens.set_tuning(shape, 0, 0)
                 ens.set_tuning(-1, 36, 2)
                 assert gpu_lib.gbf_ensemble_uses_tma(ens.h) == tma
                 ens.upload_initial()
