@@ -452,7 +452,8 @@ int build_lists(gbf_ensemble* e) {
       for (unsigned b = 0; b < nint; b += kChunkCells) e->flux.push_back({r, b, (unsigned)std::min<size_t>(nint, b + kChunkCells)});
       me.part_end = (int)e->flux.size();
     }
-    const size_t nb = gbf_boundary_count(g);
+    // the x-pair split tile writes the x faces itself
+    const size_t nb = (split && kShapePairs[e->shape]) ? gbf_boundary_count_no_xfaces(g) : gbf_boundary_count(g);
     for (unsigned b = 0; b < nb; b += kBoundaryChunk) e->bnd.push_back({r, b, (unsigned)std::min<size_t>(nb, b + kBoundaryChunk)});
     for (unsigned b = 0; b < g.n; b += kChunkCells) e->all.push_back({r, b, (unsigned)std::min<size_t>(g.n, b + kChunkCells)});
   }

@@ -47,6 +47,9 @@ GBF_HD bool gbf_is_boundary(const GbfGeo& g, int i, int j, int k) {
 GBF_HD size_t gbf_boundary_count(const GbfGeo& g) {
   return 2 * g.pl + 2 * (size_t)g.nx * (g.nz - 2) + 2 * (size_t)(g.ny - 2) * (g.nz - 2);
 }
+// The first two groups only: every boundary cell but the x faces with j, k
+// interior (which the x-pair split tile writes itself).
+GBF_HD size_t gbf_boundary_count_no_xfaces(const GbfGeo& g) { return 2 * g.pl + 2 * (size_t)g.nx * (g.nz - 2); }
 GBF_HD void gbf_boundary_cell(const GbfGeo& g, size_t id, int& i, int& j, int& k) {
   size_t a = 2 * g.pl;
   if (id < a) {

@@ -133,9 +133,11 @@ __global__ void __launch_bounds__(kPairTX / 2 * kPairTY, 2) k_split_step_x2(cons
   if (G.mass_partials) split_block_mass<DF, kPairTX / 2 * kPairTY>(acc, C.V, G.mass_partials + 2 * blockIdx.x);
 }
 
-__global__ void __launch_bounds__(kThreads) k_split_boundary(const gbf_model m, const GbfSplitGrid G, float H) {
+// Boundary cells [0, nb) of gbf_boundary_cell's enumeration (all, or all but
+// the x faces that the x-pair tile writes).
+__global__ void __launch_bounds__(kThreads) k_split_boundary(const gbf_model m, const GbfSplitGrid G, float H,
+                                                             size_t nb) {
   const GbfGeo g = gbf_geo(m);
-  const size_t nb = gbf_boundary_count(g);
   for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < nb; t += (size_t)gridDim.x * blockDim.x) {
     int i, j, k;
     gbf_boundary_cell(g, t, i, j, k);
@@ -229,7 +231,8 @@ int gbf_split_launch_domain(const gbf_model& m, const GbfSplitConsts& C, const G
   }
   gbf_timer_end(tm, GBF_K_SPLIT_STEP, e, st);
   e = gbf_timer_begin(tm, st);
-  k_split_boundary<<<gbf_grid_for(gbf_boundary_count(gbf_geo(m)), kThreads, 4), kThreads, 0, st>>>(m, G, C.H);
+  const size_t nb = maps ? gbf_boundary_count_no_xfaces(gbf_geo(m)) : gbf_boundary_count(gbf_geo(m));
+  k_split_boundary<<<gbf_grid_for(nb, kThreads, 4), kThreads, 0, st>>>(m, G, C.H, nb);
   gbf_timer_end(tm, GBF_K_SPLIT_BOUNDARY, e, st);
   if (G.mass_partials && mass_out) {
     e = gbf_timer_begin(tm, st);

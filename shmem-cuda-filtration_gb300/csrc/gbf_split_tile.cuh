@@ -979,9 +979,13 @@ __device__ bool split_tile_x2(const GbfSplitConsts& C, const GbfSplitGrid& G, in
       const bool cnt[2] = {act_a, act_b};
       GbfCellOut<DF> o[2];
       split_cells<DF, 2>(C, in, m1s, m2s, R01, R02, 0, cis, j, k, true, G.mass_partials != nullptr, cnt, acc, o);
-      // cells outside the interior (boundary cell 0 or nx - 1 of the pair) keep their values
-      const GbfCellOut<DF> oa = act_a ? o[0] : GbfCellOut<DF>{d0.x, s0.x, M1a, M2a};
-      const GbfCellOut<DF> ob = act_b ? o[1] : GbfCellOut<DF>{d0.y, s0.y, M1b, M2b};
+      // The x faces i = 0 and i = nx - 1 (rows and planes interior) take the
+      // boundary rules' values here: the new S of the x-neighbour and its dP
+      // (cpu.cpp:327-331, 366-372), or the hydrostatic side value dP = 0 with
+      // GBF_BC_HYDROSTATIC_SIDES; no other boundary rule reads these cells, so
+      // the face pass skips them (gbf_boundary_count_no_xfaces).
+      const GbfCellOut<DF> oa = act_a ? o[0] : GbfCellOut<DF>{C.noflow_bottom ? 0.f : o[1].dPn, o[1].Sn, M1a, M2a};
+      const GbfCellOut<DF> ob = act_b ? o[1] : GbfCellOut<DF>{C.noflow_bottom ? 0.f : o[0].dPn, o[0].Sn, M1b, M2b};
       const unsigned c = (unsigned)(ia + j * nx) + (unsigned)k * pln;  // even: nx and ia are
       gbf_st2(G.dPn + c, oa.dPn, ob.dPn);
       gbf_st2(G.Sn + c, oa.Sn, ob.Sn);
