@@ -37,7 +37,8 @@ def members(abi, lib):
     """Uneven members: sizes, fields, closures, anisotropy, sources, BCs."""
     out = []
     rng = np.random.default_rng(21)
-    for r, (nx, ny, nz) in enumerate([(24, 20, 18), (36, 16, 22), (16, 16, 16), (40, 24, 12)]):
+    # (72, 14, 10): two x tiles of the 64-wide x-pair tile
+    for r, (nx, ny, nz) in enumerate([(24, 20, 18), (36, 16, 22), (16, 16, 16), (40, 24, 12), (72, 14, 10)]):
         m = abi.reference_model(nx, ny, nz, 1.0)
         m.h1 = m.h2 = m.h3 = 0.05
         m.S_wr[:] = [0.1, 0.1]
@@ -252,7 +253,7 @@ def test_ensemble_advance_host_equals_three_calls(gpu_lib, abi, pkg, p):
     with aliased output arrays, and leaves the ensemble in the same state."""
     import torch
     E, _ = mods(pkg)
-    mems = members(abi, gpu_lib) * 3  # 12 members: several groups
+    mems = members(abi, gpu_lib) * 3  # 15 members: several groups
     cells = sum(m.model.nx * m.model.ny * m.model.nz for m in mems)
     P0 = np.concatenate([m.initial_state()[0].ravel() for m in mems])
     S0 = np.concatenate([m.initial_state()[1].ravel() for m in mems])
@@ -288,3 +289,35 @@ def test_ensemble_advance_host_equals_three_calls(gpu_lib, abi, pkg, p):
             assert np.array_equal(dut.download(r, "P1"), ref.download(r, "P1"))
         ref.close()
         dut.close()
+
+
+def test_ensemble_without_tma_refuses_pair_tile(gpu_lib, abi, pkg):
+    """A member whose rows are not whole 16-byte units (nx % 4 != 0) rules out
+    TMA staging for the ensemble: plain loads, the x-pair tile refused and
+    skipped by the autotuner, results still those of single domains."""
+    E, D = mods(pkg)
+    mems = members(abi, gpu_lib)[:2]
+    m = abi.reference_model(18, 12, 10, 1.0)  # nx = 18
+    m.h1 = m.h2 = m.h3 = 0.05
+    K = np.full(m.shape, 6.64e-11, np.float32)
+    phi = np.full(m.shape, 0.35, np.float32)
+    cells = abi.GbfCells()
+    cells.K = K.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+    cells.phi = phi.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+    m.dt = 0.5 * gpu_lib.gbf_stable_dt(ctypes.byref(m), ctypes.byref(cells), 1.0)
+    mems.append(Mem(m, K, phi))
+    ens = E.Ensemble(mems, precision=abi.GBF_PREC_SPLIT_DF)
+    assert gpu_lib.gbf_ensemble_uses_tma(ens.h) == 0
+    assert gpu_lib.gbf_ensemble_set_tuning(ens.h, 3, 0, 0) == abi.GBF_ERR_ARG
+    gpu_lib.gbf_clear_status()
+    assert ens.autotune(1)["tile"] != "64x8 pairs"
+    ens.upload_initial()
+    ens.step(6)
+    assert ens.status() == abi.GBF_OK
+    d = D.Domain(m, None, K, phi, precision=abi.GBF_PREC_SPLIT_DF)
+    d.upload(*mems[2].initial_state())
+    d.step(6)
+    assert np.array_equal(ens.download(2, "S2"), d.download("S2"))
+    assert np.array_equal(ens.download(2, "P1"), d.download("P1"))
+    d.close()
+    ens.close()
