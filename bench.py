@@ -385,10 +385,54 @@ def run_ours(args, rank, world):
         out["same_members"] = comp
         if "f64" in comp:
             out["split_batched_over_fp64_batched"] = value / comp["f64"]["value"]
+    if rank == 0 and not args.no_compare and prec != abi.GBF_PREC_F64:
+        out["accuracy"] = accuracy_block(pkg, ge.load_oracle_module(), members, prec, ensemble)
     if rank == 0 and not args.no_cpu_baseline:
         O = ge.load_oracle_module()
         out["cpu_baseline"] = cpu_baseline(O, abi, members, budget_s=args.cpu_budget)
     return out
+
+
+def accuracy_block(pkg, O, members, prec, ensemble, steps=20):
+    """The measured form against plain FP64 on the same members and steps
+    (the GPU FP64 path, itself pinned to the oracle at 1e-12), and against
+    the oracle on the smallest member: max|dS|, relative L2 of P, relative
+    phase-mass difference per step, and how far S moved (max|S - S0|)."""
+    import numpy as np
+    abi = pkg.abi
+
+    def run(p):
+        r = Runner(pkg, members, p, ensemble, steps + 2)
+        r.upload_initial()
+        r.step(steps)
+        out = [(r.download(i, "P1"), r.download(i, "S2")) for i in range(len(members))] if ensemble else \
+            [(r.download(0, "P1"), r.download(0, "S2"))]
+        mass = r.mass_history(steps)
+        r.close()
+        return out, mass
+
+    got, mg = run(prec)
+    ref, mr = run(abi.GBF_PREC_F64)
+    ds = max(float(np.abs(a[1] - b[1]).max()) for a, b in zip(got, ref))
+    num = sum(float(np.sum((a[0] - b[0]) ** 2)) for a, b in zip(got, ref))
+    den = sum(float(np.sum(b[0] ** 2)) for b in ref)
+    moved = max(float(np.abs(b[1] - m.initial_state()[1]).max()) for b, m in zip(ref, members))
+    scale = np.maximum(np.abs(mr), 1e-300)
+    drift = float(np.max(np.abs(mg - mr) / scale * (np.abs(mr) > 0)))
+    block = {"vs": "plain FP64 GPU path of the same members (pinned to the oracle at 1e-12)", "steps": steps,
+             "max_dS": ds, "rel_l2_P": (num / den) ** 0.5, "phase_mass_rel_diff_max": drift, "S_moved_max": moved}
+    # the oracle itself on the smallest member
+    i = min(range(len(members)), key=lambda q: members[q].ncells)
+    mem = members[i]
+    st = O.State(mem.model, mem.media, mem.K, mem.phi)
+    P0, S0 = mem.initial_state()
+    st["P1"][...] = P0
+    st["S2"][...] = S0
+    O.Oracle(abi).step(st, steps)
+    block["oracle_sample"] = {"member": i, "shape": list(mem.model.shape), "steps": steps,
+                              "max_dS": float(np.abs(got[i][1] - st["S2"]).max()),
+                              "rel_l2_P": float(np.linalg.norm(got[i][0] - st["P1"]) / np.linalg.norm(st["P1"]))}
+    return block
 
 
 def run_reference(args, rank, world):
