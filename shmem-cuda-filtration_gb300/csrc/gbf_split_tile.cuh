@@ -237,12 +237,18 @@ __device__ __forceinline__ void split_props(const GbfSplitConsts& C, int md, flo
   L2 = K * kr2 * C.nmr2 * fmaf(C.beta2, Pp, 1.f);
 }
 
-// Donor-cell flux difference of one direction (see gbf_f64.cu): max/min
-// forms of the reference's (x +- |x|)/2 (cpu.cpp:260-262).
+// Upwinded flux through one face: the potential x times the mobility of the
+// cell the flow comes from, L_pos for x >= 0 and L_neg otherwise — the
+// reference's ((x + |x|) L_pos + (x - |x|) L_neg) / 2 (cpu.cpp:260-262). In x
+// and z both phases share the potential (P2 = P1), and so the comparison.
+// Donor-cell flux difference of one direction: in through face 1 (from the
+// minus side, a rounded product), out through face 2 (fused into the
+// difference). The rounding is fixed explicitly: two cells of one thread
+// share a face, and a compiler free to merge the two products in one tile
+// shape and not in another would give the shapes different bits.
 __device__ __forceinline__ float split_donor(float x1, float x2, float Lc, float Lm, float Lp) {
-  const float x2p = fmaxf(x2, 0.f), x2m = fminf(x2, 0.f);
-  const float x1p = fmaxf(x1, 0.f), x1m = fminf(x1, 0.f);
-  return (x1p * Lm - (x2p - x1m) * Lc) - x2m * Lp;
+  const float in1 = __fmul_rn(x1, x1 >= 0.f ? Lm : Lc);
+  return fmaf(-x2, x2 >= 0.f ? Lc : Lp, in1);
 }
 
 // Brooks-Corey capillary pressure P_d S_e^(-1/lambda) and its S-derivative (cpu.cpp:303-308).
