@@ -8,7 +8,7 @@
 // the FP32 arithmetic; FP64 and FP32-pair copies for the wide residual.
 struct GbfSplitConsts {
   int nx, ny, nz;
-  int noflow_bottom;
+  int noflow_bottom;  // GBF_BC_HYDROSTATIC_SIDES: no-flow bottom face and hydrostatic P on the i and k sides
   int ri0, rk0, rn;  // rate-injection patch on the j = 1 layer (rn = 0: none)
   float inv_h1, inv_h2, inv_h3, kv, dt;
   float H;  // rho01 g h2: hydrostatic pressure step per cell (main.cpp:114)
@@ -56,6 +56,7 @@ int gbf_split_state_to_f64(const gbf_model& m, const float* dPf, const float* Sf
 int gbf_split_init_state(const gbf_model& m, const double* P_dev, const double* S_dev, float* dPf, float* Sf,
                          double* M1, double* M2, bool df, cudaStream_t st);
 struct GbfTmaSet;
-// `maps` (device memory) selects the TMA plane loads for state buffer `buf`.
+// `maps` (device memory; boxes of the x-pair tile) selects the x-pair TMA
+// tile for state buffer `buf`; without it the plain-load 32x8 tile runs.
 int gbf_split_launch_domain(const gbf_model& m, const GbfSplitConsts& C, const GbfSplitGrid& G, bool df,
                             double* mass_out, cudaStream_t st, GbfTimer* tm, const GbfTmaSet* maps, int buf);
