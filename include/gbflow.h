@@ -188,7 +188,9 @@ typedef struct gbf_ensemble gbf_ensemble; /* batched grids, declared below */
 enum { GBF_OUT_MASS = 1,        /* phase masses after the mass update, every step */
        GBF_OUT_VELOCITY = 2,    /* u1x..u2z of the reference's a2 (FP64 only)      */
        GBF_OUT_MASS_ARRAYS = 4, /* roS1, roS2, roS1_old, roS2_old (FP64 only)       */
-       GBF_OUT_PROPS = 8 };     /* keep P2/Xi/ro of the last step readable        */
+       GBF_OUT_PROPS = 8,       /* keep P2/Xi/ro of the last step readable        */
+       GBF_OUT_CFL = 16 };      /* with GBF_OUT_MASS, split forms: CFL numbers per
+                                   step (cell maximum of face flux dt / (phi h) per phase) */
 int gbf_domain_create(const gbf_model* m, const gbf_cells* host_cells, int precision, gbf_domain** out);
 int gbf_domain_destroy(gbf_domain* d);
 int gbf_domain_set_outputs(gbf_domain* d, int out_flags, int mass_history_capacity);
@@ -202,6 +204,10 @@ int gbf_domain_step(gbf_domain* d, int nsteps);
 int gbf_domain_download(gbf_domain* d, int field, double* host);
 /* Phase masses [step][2] recorded since the last upload (GBF_OUT_MASS). */
 int gbf_domain_mass_history(gbf_domain* d, double* host, int max_steps, int* nsteps_out);
+/* CFL numbers [step][2] (water, DNAPL) of the same steps (GBF_OUT_CFL): the
+   largest over interior cells and their six faces of the phase's volumetric
+   face flux (mass flux / reference density) times dt / (phi h). */
+int gbf_domain_cfl_history(gbf_domain* d, float* host, int max_steps, int* nsteps_out);
 /* Synchronise and return the device-side status (non-finite P/S, timeouts). */
 int gbf_domain_status(gbf_domain* d);
 int gbf_domain_sync(gbf_domain* d);
@@ -295,6 +301,9 @@ long long gbf_ensemble_interior_cells(gbf_ensemble* e);
 int gbf_ensemble_set_stream(gbf_ensemble* e, void* stream);
 /* GBF_OUT_MASS only: per-member phase masses every step. */
 int gbf_ensemble_set_outputs(gbf_ensemble* e, int out_flags, int mass_history_capacity);
+/* GBF_OUT_CFL (with GBF_OUT_MASS, split forms): [step][member][2] CFL numbers,
+   as gbf_domain_cfl_history. */
+int gbf_ensemble_cfl_history(gbf_ensemble* e, float* host, int max_steps, int* nsteps_out);
 int gbf_ensemble_upload(gbf_ensemble* e, int member, const double* P1, const double* S2);
 /* Every member at once: P_all and S_all hold all members' nx*ny*nz doubles
    back to back in member order (host or device memory; pinned host memory

@@ -17,7 +17,7 @@ GBF_OK, GBF_ERR_ARG, GBF_ERR_CUDA, GBF_ERR_NOMEM, GBF_ERR_NONFINITE, GBF_ERR_UNS
 GBF_SOURCE_DIRICHLET_PATCH, GBF_SOURCE_RATE = 0, 1
 GBF_BC_REFERENCE, GBF_BC_HYDROSTATIC_SIDES = 0, 1
 GBF_PREC_F64, GBF_PREC_SPLIT, GBF_PREC_SPLIT_DF = 0, 1, 2
-GBF_OUT_MASS, GBF_OUT_VELOCITY, GBF_OUT_MASS_ARRAYS, GBF_OUT_PROPS = 1, 2, 4, 8
+GBF_OUT_MASS, GBF_OUT_VELOCITY, GBF_OUT_MASS_ARRAYS, GBF_OUT_PROPS, GBF_OUT_CFL = 1, 2, 4, 8, 16
 
 FIELDS = ["P1", "S2", "P2", "ro1", "ro2", "Xi1", "Xi2", "u1x", "u1y", "u1z",
           "u2x", "u2y", "u2z", "roS1", "roS2", "roS1_old", "roS2_old"]
@@ -140,6 +140,8 @@ def _declare(lib) -> None:
         "gbf_domain_step": (c_int, [c_void_p, c_int]),
         "gbf_domain_download": (c_int, [c_void_p, c_int, c_void_p]),
         "gbf_domain_mass_history": (c_int, [c_void_p, c_void_p, c_int, ctypes.POINTER(c_int)]),
+        "gbf_domain_cfl_history": (c_int, [c_void_p, c_void_p, c_int, ctypes.POINTER(c_int)]),
+        "gbf_ensemble_cfl_history": (c_int, [c_void_p, c_void_p, c_int, ctypes.POINTER(c_int)]),
         "gbf_domain_status": (c_int, [c_void_p]),
         "gbf_domain_sync": (c_int, [c_void_p]),
         "gbf_domain_steps_done": (ctypes.c_longlong, [c_void_p]),

@@ -201,9 +201,11 @@ int gbf_domain_set_outputs(gbf_domain* d, int flags, int mass_cap) {
   const size_t n = gbf_geo(d->m).n, b = n * sizeof(double);
   if ((flags & GBF_OUT_MASS) && mass_cap > d->mass_cap) {
     if (int s = gbf_domain_alloc(d, (void**)&d->mass_hist, 2 * sizeof(double) * (size_t)mass_cap)) return s;
+    if (int s = gbf_domain_alloc(d, (void**)&d->cfl_hist, 2 * sizeof(float) * (size_t)mass_cap)) return s;
     d->mass_cap = mass_cap;
     d->mass_count = 0;
   }
+  if (d->cfl_hist) GBF_CUDA(cudaMemsetAsync(d->cfl_hist, 0, 2 * sizeof(float) * (size_t)d->mass_cap, d->stream));
   if ((flags & GBF_OUT_VELOCITY) && !d->outs.u1x) {
     double** f[] = {&d->outs.u1x, &d->outs.u1y, &d->outs.u1z, &d->outs.u2x, &d->outs.u2y, &d->outs.u2z};
     for (double** p : f)
@@ -236,6 +238,7 @@ int gbf_domain_upload_device(gbf_domain* d, const double* P1, const double* S2) 
   d->mass_count = 0;
   d->steps = 0;
   d->uploaded = true;
+  if (d->cfl_hist) GBF_CUDA(cudaMemsetAsync(d->cfl_hist, 0, 2 * sizeof(float) * (size_t)d->mass_cap, d->stream));
   GBF_CUDA(cudaMemsetAsync(d->status, 0, sizeof(unsigned), d->stream));
   return GBF_OK;
 }
@@ -253,6 +256,7 @@ int gbf_domain_upload(gbf_domain* d, const double* P1, const double* S2) {
   d->mass_count = 0;
   d->steps = 0;
   d->uploaded = true;
+  if (d->cfl_hist) GBF_CUDA(cudaMemsetAsync(d->cfl_hist, 0, 2 * sizeof(float) * (size_t)d->mass_cap, d->stream));
   GBF_CUDA(cudaMemsetAsync(d->status, 0, sizeof(unsigned), d->stream));
   return GBF_OK;
 }
@@ -423,6 +427,16 @@ int gbf_domain_download(gbf_domain* d, int field, double* host) {
   if (!src) return gbf_fail(GBF_ERR_STATE, "field not produced (enable it with gbf_domain_set_outputs)");
   GBF_CUDA(cudaMemcpyAsync(host, src, b, cudaMemcpyDeviceToHost, d->stream));
   GBF_CUDA(cudaStreamSynchronize(d->stream));
+  return GBF_OK;
+}
+
+int gbf_domain_cfl_history(gbf_domain* d, float* host, int max_steps, int* nsteps_out) {
+  if (!d || !host || max_steps < 0) return gbf_fail(GBF_ERR_ARG, "gbf_domain_cfl_history");
+  long long n = d->mass_count < max_steps ? d->mass_count : max_steps;
+  if (n > 0 && d->cfl_hist)
+    GBF_CUDA(cudaMemcpyAsync(host, d->cfl_hist, 2 * sizeof(float) * (size_t)n, cudaMemcpyDeviceToHost, d->stream));
+  GBF_CUDA(cudaStreamSynchronize(d->stream));
+  if (nsteps_out) *nsteps_out = (int)n;
   return GBF_OK;
 }
 

@@ -69,6 +69,7 @@ struct gbf_domain {
   // mass tracking
   double* mass_partials = nullptr;
   double* mass_hist = nullptr;
+  float* cfl_hist = nullptr;  // [mass_cap][2] (GBF_OUT_CFL)
   int mass_cap = 0;
   long long mass_count = 0;
   unsigned* status = nullptr;

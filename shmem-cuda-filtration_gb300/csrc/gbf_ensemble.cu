@@ -53,13 +53,27 @@ constexpr int kChunkCells = 16384, kBoundaryChunk = 4096, kThreads = 256;
 
 // ------------------------------------------------------------ split kernels
 
-template <bool DF, int TX, int TY, bool TMA>
+// Where a step's CFL numbers go (GBF_OUT_CFL): hist[step][member][2],
+// step = *step_count (the mass history's step counter); NULL hist: off.
+struct EnsCfl {
+  const unsigned* step_count;
+  float* hist;
+  int n, cap;
+};
+__device__ __forceinline__ float* ens_cfl_slot(const EnsCfl& cfl, int member) {
+  if (!cfl.hist) return nullptr;
+  const unsigned step = *cfl.step_count;
+  return step < (unsigned)cfl.cap ? cfl.hist + 2 * ((size_t)step * cfl.n + member) : nullptr;
+}
+
+template <bool DF, int TX, int TY, bool TMA, bool CFL>
 __global__ void __launch_bounds__(TX * TY, 1024 / (TX * TY)) k_ens_split_step(const EnsMember* __restrict__ mem,
                                                                              const int4* __restrict__ tiles,
                                                                              int ntiles, int cur,
                                                                              unsigned* counter, double* partials,
                                                                              unsigned* status,
-                                                                             const GbfTmaSet* __restrict__ maps) {
+                                                                             const GbfTmaSet* __restrict__ maps,
+                                                                             const EnsCfl cfl) {
   __shared__ GbfSplitPlaneT<TX, TY, gbf_plane_pitch<TX, TMA>()> pl[TMA ? 3 : 2];
   __shared__ GbfSplitConsts Cs;
   __shared__ GbfSplitGrid Gs;
@@ -101,22 +115,25 @@ __global__ void __launch_bounds__(TX * TY, 1024 / (TX * TY)) k_ens_split_step(co
       Gs.M2 = me->M2;
       Gs.mass_partials = partials;
       Gs.status = status;
+      Gs.cfl_out = CFL ? ens_cfl_slot(cfl, tl.x) : nullptr;
     }
     __syncthreads();
     GbfSplitAcc<DF> acc;
-    const bool ok = split_tile<DF, TX, TY, TMA>(Cs, Gs, tl.y, tl.z, tl.w & 0xffff, tl.w >> 16, pl, acc, raw,
+    const bool ok = split_tile<DF, TX, TY, TMA, CFL>(Cs, Gs, tl.y, tl.z, tl.w & 0xffff, tl.w >> 16, pl, acc, raw,
                                                 TMA ? maps + tl.x : nullptr, cur, &phases);
     if (!ok) break;  // a plane wait gave up (status set); the whole CTA stops
     if (acc.bad) atomicOr(status, GBF_DEV_NONFINITE);
     if (partials) split_block_mass<DF, NT>(acc, Cs.V, partials + 2 * t);
+    if constexpr (CFL)
+      if (Gs.cfl_out) split_block_cfl<NT>(acc.cfl1, acc.cfl2, Gs.cfl_out);
     __syncthreads();
   }
 }
 
-template <bool DF, int TXC, int TY>
+template <bool DF, int TXC, int TY, bool CFL>
 __global__ void __launch_bounds__(TXC / 2 * TY, 512 / (TXC / 2 * TY)) k_ens_split_step_x2(
     const EnsMember* __restrict__ mem, const int4* __restrict__ tiles, int ntiles, int cur, unsigned* counter,
-    double* partials, unsigned* status, const GbfTmaSet* __restrict__ maps) {
+    double* partials, unsigned* status, const GbfTmaSet* __restrict__ maps, const EnsCfl cfl) {
   extern __shared__ __align__(128) unsigned char dyn[];
   GbfPairSmem<TXC, TY>& sm = *reinterpret_cast<GbfPairSmem<TXC, TY>*>(dyn);
   __shared__ GbfSplitConsts Cs;
@@ -158,14 +175,17 @@ __global__ void __launch_bounds__(TXC / 2 * TY, 512 / (TXC / 2 * TY)) k_ens_spli
       Gs.M2 = me->M2;
       Gs.mass_partials = partials;
       Gs.status = status;
+      Gs.cfl_out = CFL ? ens_cfl_slot(cfl, tl.x) : nullptr;
     }
     __syncthreads();
     GbfSplitAcc<DF> acc;
-    const bool ok = split_tile_x2<DF, TXC, TY>(Cs, Gs, tl.y, tl.z, tl.w & 0xffff, tl.w >> 16, sm, acc,
+    const bool ok = split_tile_x2<DF, TXC, TY, CFL>(Cs, Gs, tl.y, tl.z, tl.w & 0xffff, tl.w >> 16, sm, acc,
                                                maps + tl.x, cur, &phases);
     if (!ok) break;
     if (acc.bad) atomicOr(status, GBF_DEV_NONFINITE);
     if (partials) split_block_mass<DF, NT>(acc, Cs.V, partials + 2 * t);
+    if constexpr (CFL)
+      if (Gs.cfl_out) split_block_cfl<NT>(acc.cfl1, acc.cfl2, Gs.cfl_out);
     __syncthreads();
   }
 }
@@ -352,6 +372,7 @@ struct gbf_ensemble {
   double* d_partials = nullptr;
   unsigned *d_counter = nullptr, *d_status = nullptr, *d_mass_count = nullptr;
   double* d_mass_hist = nullptr;
+  float* d_cfl_hist = nullptr;  // [mass_cap][n][2] (GBF_OUT_CFL)
   int mass_cap = 0;
   int out_flags = 0;
   cudaStream_t stream = nullptr;
@@ -536,23 +557,30 @@ struct TileRange {
   unsigned* counter;
 };
 
+EnsCfl ens_cfl(const gbf_ensemble* e) {
+  const bool on = (e->out_flags & GBF_OUT_CFL) && (e->out_flags & GBF_OUT_MASS) && e->d_cfl_hist;
+  return {e->d_mass_count, on ? e->d_cfl_hist : nullptr, e->n, e->mass_cap};
+}
+
 template <bool DF, int TX, int TY>
 int launch_split_step_t(gbf_ensemble* e, double* partials, cudaStream_t st, const TileRange& tr) {
-  const bool tma = e->d_maps != nullptr;
-  auto kern = tma ? k_ens_split_step<DF, TX, TY, true> : k_ens_split_step<DF, TX, TY, false>;
+  const bool tma = e->d_maps != nullptr, cfl = partials && ens_cfl(e).hist;
+  auto kern = tma ? (cfl ? k_ens_split_step<DF, TX, TY, true, true> : k_ens_split_step<DF, TX, TY, true, false>)
+                  : (cfl ? k_ens_split_step<DF, TX, TY, false, true> : k_ens_split_step<DF, TX, TY, false, false>);
   int per_sm = 0;
   GBF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TX * TY, 0));
   const int blocks = std::max(1, std::min(tr.nt, per_sm * gbf_num_sms()));
   e->persistent_blocks = blocks;
   kern<<<blocks, TX * TY, 0, st>>>(e->d_mem, e->d_tiles + tr.t0, tr.nt, tr.cur, tr.counter,
-                                    partials ? partials + 2 * (size_t)tr.t0 : nullptr, e->d_status, e->d_maps);
+                                    partials ? partials + 2 * (size_t)tr.t0 : nullptr, e->d_status, e->d_maps,
+                                    ens_cfl(e));
   return GBF_OK;
 }
 
 template <bool DF, int TXC, int TY>
 int launch_split_step_x2(gbf_ensemble* e, double* partials, cudaStream_t st, const TileRange& tr) {
   if (!e->d_maps) return gbf_fail(GBF_ERR_STATE, "x-pair tile without TMA maps");
-  auto kern = k_ens_split_step_x2<DF, TXC, TY>;
+  auto kern = (partials && ens_cfl(e).hist) ? k_ens_split_step_x2<DF, TXC, TY, true> : k_ens_split_step_x2<DF, TXC, TY, false>;
   const int bytes = (int)sizeof(GbfPairSmem<TXC, TY>);
   GBF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
   int per_sm = 0;
@@ -561,7 +589,7 @@ int launch_split_step_x2(gbf_ensemble* e, double* partials, cudaStream_t st, con
   e->persistent_blocks = blocks;
   kern<<<blocks, TXC / 2 * TY, bytes, st>>>(e->d_mem, e->d_tiles + tr.t0, tr.nt, tr.cur, tr.counter,
                                              partials ? partials + 2 * (size_t)tr.t0 : nullptr, e->d_status,
-                                             e->d_maps);
+                                             e->d_maps, ens_cfl(e));
   return GBF_OK;
 }
 
@@ -798,13 +826,17 @@ int gbf_ensemble_set_stream(gbf_ensemble* e, void* stream) {
 }
 
 int gbf_ensemble_set_outputs(gbf_ensemble* e, int flags, int mass_cap) {
-  if (!e || mass_cap < 0 || (flags & ~GBF_OUT_MASS)) return gbf_fail(GBF_ERR_ARG, "gbf_ensemble_set_outputs");
+  if (!e || mass_cap < 0 || (flags & ~(GBF_OUT_MASS | GBF_OUT_CFL)))
+    return gbf_fail(GBF_ERR_ARG, "gbf_ensemble_set_outputs");
   if ((flags & GBF_OUT_MASS) && mass_cap > e->mass_cap) {
     if (int s = ens_alloc(e, (void**)&e->d_mass_hist, 2 * sizeof(double) * (size_t)mass_cap * e->n)) return s;
+    if (int s = ens_alloc(e, (void**)&e->d_cfl_hist, 2 * sizeof(float) * (size_t)mass_cap * e->n)) return s;
     e->mass_cap = mass_cap;
   }
   e->out_flags = flags;
   GBF_CUDA(cudaMemsetAsync(e->d_mass_count, 0, sizeof(unsigned), e->stream));
+  if (e->d_cfl_hist)
+    GBF_CUDA(cudaMemsetAsync(e->d_cfl_hist, 0, 2 * sizeof(float) * (size_t)e->mass_cap * e->n, e->stream));
   drop_graphs(e);
   return GBF_OK;
 }
@@ -835,6 +867,8 @@ int gbf_ensemble_upload(gbf_ensemble* e, int r, const double* P1, const double* 
   e->steps = 0;
   GBF_CUDA(cudaMemsetAsync(e->d_status, 0, sizeof(unsigned), e->stream));
   GBF_CUDA(cudaMemsetAsync(e->d_mass_count, 0, sizeof(unsigned), e->stream));
+  if (e->d_cfl_hist)
+    GBF_CUDA(cudaMemsetAsync(e->d_cfl_hist, 0, 2 * sizeof(float) * (size_t)e->mass_cap * e->n, e->stream));
   return GBF_OK;
 }
 
@@ -864,6 +898,8 @@ int gbf_ensemble_upload_all(gbf_ensemble* e, const double* P_all, const double* 
   e->steps = 0;
   GBF_CUDA(cudaMemsetAsync(e->d_status, 0, sizeof(unsigned), e->stream));
   GBF_CUDA(cudaMemsetAsync(e->d_mass_count, 0, sizeof(unsigned), e->stream));
+  if (e->d_cfl_hist)
+    GBF_CUDA(cudaMemsetAsync(e->d_cfl_hist, 0, 2 * sizeof(float) * (size_t)e->mass_cap * e->n, e->stream));
   // the host arrays may be reused as soon as this returns
   GBF_CUDA(cudaStreamSynchronize(e->stream));
   return GBF_OK;
@@ -941,6 +977,8 @@ int gbf_ensemble_advance_host(gbf_ensemble* e, const double* P_in, const double*
   e->cur = c0 ^ (nsteps & 1);
   e->steps = nsteps;
   GBF_CUDA(cudaMemsetAsync(e->d_mass_count, 0, sizeof(unsigned), cs));
+  if (e->d_cfl_hist)
+    GBF_CUDA(cudaMemsetAsync(e->d_cfl_hist, 0, 2 * sizeof(float) * (size_t)e->mass_cap * e->n, cs));
   GBF_CUDA(cudaStreamSynchronize(cs));
   return GBF_OK;
 }
@@ -1001,6 +1039,18 @@ int gbf_ensemble_mass_history(gbf_ensemble* e, double* host, int max_steps, int*
   int n = (int)std::min<unsigned>(cnt, (unsigned)std::min(max_steps, e->mass_cap));
   if (n > 0)
     GBF_CUDA(cudaMemcpy(host, e->d_mass_hist, 2 * sizeof(double) * (size_t)n * e->n, cudaMemcpyDeviceToHost));
+  if (nsteps_out) *nsteps_out = n;
+  return GBF_OK;
+}
+
+int gbf_ensemble_cfl_history(gbf_ensemble* e, float* host, int max_steps, int* nsteps_out) {
+  if (!e || !host || max_steps < 0) return gbf_fail(GBF_ERR_ARG, "gbf_ensemble_cfl_history");
+  unsigned cnt = 0;
+  GBF_CUDA(cudaMemcpyAsync(&cnt, e->d_mass_count, sizeof(unsigned), cudaMemcpyDeviceToHost, e->stream));
+  GBF_CUDA(cudaStreamSynchronize(e->stream));
+  int n = (int)std::min<unsigned>(cnt, (unsigned)std::min(max_steps, e->mass_cap));
+  if (n > 0 && e->d_cfl_hist)
+    GBF_CUDA(cudaMemcpy(host, e->d_cfl_hist, 2 * sizeof(float) * (size_t)n * e->n, cudaMemcpyDeviceToHost));
   if (nsteps_out) *nsteps_out = n;
   return GBF_OK;
 }

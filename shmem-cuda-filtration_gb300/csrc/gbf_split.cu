@@ -36,6 +36,7 @@ GbfSplitConsts gbf_split_consts(const gbf_model& m) {
   const double H = m.ro01 * m.g * m.h2;
   C.H = (float)H;
   C.ro01 = (float)m.ro01; C.ro02 = (float)m.ro02; C.beta1 = (float)m.beta1; C.beta2 = (float)m.beta2;
+  C.cfl1 = (float)(1.0 / m.ro01); C.cfl2 = (float)(1.0 / m.ro02);
   C.g_ro01_b1 = (float)(m.g * m.ro01 * m.beta1);
   C.g_ro02_b2 = (float)(m.g * m.ro02 * m.beta2);
   C.g_dro = (float)(m.g * (m.ro02 - m.ro01));
@@ -89,7 +90,7 @@ __host__ __device__ int tiles_x2(const GbfSplitConsts& C) { return (C.nx - 1 + k
 __host__ __device__ int tiles_y2(const GbfSplitConsts& C) { return (C.ny - 2 + kPairTY - 1) / kPairTY; }
 
 // The plain-load tile on one grid (grids without TMA staging).
-template <bool DF>
+template <bool DF, bool CFL>
 __global__ void __launch_bounds__(kSplitThreads, 4) k_split_step(const GbfSplitConsts C, const GbfSplitGrid G,
                                                               const int kchunk) {
   __shared__ GbfSplitPlane pl[2];
@@ -99,13 +100,14 @@ __global__ void __launch_bounds__(kSplitThreads, 4) k_split_step(const GbfSplitC
   const int k0 = 1 + kc * kchunk;
   const int k1 = min(k0 + kchunk, C.nz - 1);
   GbfSplitAcc<DF> acc;
-  split_tile<DF>(C, G, 1 + tx * kSplitTX, 1 + ty * kSplitTY, k0, k1, pl, acc);
+  split_tile<DF, kSplitTX, kSplitTY, false, CFL>(C, G, 1 + tx * kSplitTX, 1 + ty * kSplitTY, k0, k1, pl, acc);
   if (acc.bad) atomicOr(G.status, GBF_DEV_NONFINITE);
   if (G.mass_partials) split_block_mass<DF>(acc, C.V, G.mass_partials + 2 * blockIdx.x);
+  if constexpr (CFL) split_block_cfl<kSplitThreads>(acc.cfl1, acc.cfl2, G.cfl_out);
 }
 
 // The x-pair tile on one grid: one tile (64 x 8 cells, a k range) per CTA.
-template <bool DF>
+template <bool DF, bool CFL>
 __global__ void __launch_bounds__(kPairTX / 2 * kPairTY, 2) k_split_step_x2(const GbfSplitConsts C,
                                                                          const GbfSplitGrid G, const int kchunk,
                                                                          const GbfTmaSet* maps, int buf) {
@@ -128,9 +130,11 @@ __global__ void __launch_bounds__(kPairTX / 2 * kPairTY, 2) k_split_step_x2(cons
   __syncthreads();
   unsigned phases = 0;
   GbfSplitAcc<DF> acc;
-  split_tile_x2<DF, kPairTX, kPairTY>(C, G, kPairTX * tx, 1 + kPairTY * ty, k0, k1, sm, acc, maps, buf, &phases);
+  split_tile_x2<DF, kPairTX, kPairTY, CFL>(C, G, kPairTX * tx, 1 + kPairTY * ty, k0, k1, sm, acc, maps, buf,
+                                           &phases);
   if (acc.bad) atomicOr(G.status, GBF_DEV_NONFINITE);
   if (G.mass_partials) split_block_mass<DF, kPairTX / 2 * kPairTY>(acc, C.V, G.mass_partials + 2 * blockIdx.x);
+  if constexpr (CFL) split_block_cfl<kPairTX / 2 * kPairTY>(acc.cfl1, acc.cfl2, G.cfl_out);
 }
 
 // Boundary cells [0, nb) of gbf_boundary_cell's enumeration (all, or all but
@@ -204,14 +208,14 @@ int gbf_split_kchunk_x2(const GbfSplitConsts& C) {
   return kchunk;
 }
 
-template <bool DF>
+template <bool DF, bool CFL>
 int launch_x2(const GbfSplitConsts& C, const GbfSplitGrid& G, const GbfTmaSet* maps, int buf, cudaStream_t st,
               unsigned& blocks) {
   const int kchunk = gbf_split_kchunk_x2(C);
   blocks = (unsigned)(tiles_x2(C) * tiles_y2(C) * ((C.nz - 2 + kchunk - 1) / kchunk));
   const int bytes = (int)sizeof(GbfPairSmem<kPairTX, kPairTY>);
-  GBF_CUDA(cudaFuncSetAttribute(k_split_step_x2<DF>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-  k_split_step_x2<DF><<<blocks, kPairTX / 2 * kPairTY, bytes, st>>>(C, G, kchunk, maps, buf);
+  GBF_CUDA(cudaFuncSetAttribute(k_split_step_x2<DF, CFL>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  k_split_step_x2<DF, CFL><<<blocks, kPairTX / 2 * kPairTY, bytes, st>>>(C, G, kchunk, maps, buf);
   return GBF_OK;
 }
 
@@ -221,13 +225,17 @@ int gbf_split_launch_domain(const gbf_model& m, const GbfSplitConsts& C, const G
   const int nkc = (C.nz - 2 + kchunk - 1) / kchunk;
   unsigned blocks = (unsigned)(tiles_x(C) * tiles_y(C) * nkc);
   cudaEvent_t e = gbf_timer_begin(tm, st);
+  const bool cfl = G.cfl_out != nullptr;
   if (maps) {  // TMA staging: the x-pair tile
-    if (int s = df ? launch_x2<true>(C, G, maps, buf, st, blocks) : launch_x2<false>(C, G, maps, buf, st, blocks))
-      return s;
+    int s = df ? (cfl ? launch_x2<true, true>(C, G, maps, buf, st, blocks) : launch_x2<true, false>(C, G, maps, buf, st, blocks))
+               : (cfl ? launch_x2<false, true>(C, G, maps, buf, st, blocks) : launch_x2<false, false>(C, G, maps, buf, st, blocks));
+    if (s) return s;
   } else if (df) {
-    k_split_step<true><<<blocks, kSplitThreads, 0, st>>>(C, G, kchunk);
+    if (cfl) k_split_step<true, true><<<blocks, kSplitThreads, 0, st>>>(C, G, kchunk);
+    else k_split_step<true, false><<<blocks, kSplitThreads, 0, st>>>(C, G, kchunk);
   } else {
-    k_split_step<false><<<blocks, kSplitThreads, 0, st>>>(C, G, kchunk);
+    if (cfl) k_split_step<false, true><<<blocks, kSplitThreads, 0, st>>>(C, G, kchunk);
+    else k_split_step<false, false><<<blocks, kSplitThreads, 0, st>>>(C, G, kchunk);
   }
   gbf_timer_end(tm, GBF_K_SPLIT_STEP, e, st);
   e = gbf_timer_begin(tm, st);
@@ -341,10 +349,12 @@ int gbf_split_step(gbf_domain* d) {
   G.M2 = d->M2;
   G.mass_partials = nullptr;
   G.status = d->status;
+  G.cfl_out = nullptr;
   double* mass_out = nullptr;
   if ((d->out_flags & GBF_OUT_MASS) && d->mass_hist && d->mass_count < d->mass_cap) {
     G.mass_partials = d->split_partials;
     mass_out = d->mass_hist + 2 * d->mass_count;
+    if ((d->out_flags & GBF_OUT_CFL) && d->cfl_hist) G.cfl_out = d->cfl_hist + 2 * d->mass_count;
     d->mass_count++;
   }
   const GbfSplitConsts C = gbf_split_consts(d->m);

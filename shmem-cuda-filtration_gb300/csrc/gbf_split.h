@@ -12,6 +12,7 @@ struct GbfSplitConsts {
   int ri0, rk0, rn;  // rate-injection patch on the j = 1 layer (rn = 0: none)
   float inv_h1, inv_h2, inv_h3, kv, dt;
   float H;  // rho01 g h2: hydrostatic pressure step per cell (main.cpp:114)
+  float cfl1, cfl2;  // 1 / rho0 of each phase: face mass flux -> volumetric flux (CFL numbers)
   float ro01, ro02, beta1, beta2;
   float g_ro01_b1, g_ro02_b2, g_dro;  // g rho01 beta1, g rho02 beta2, g (rho02 - rho01)
   float neg_inv_mu1, neg_inv_mu2;
@@ -42,6 +43,7 @@ struct GbfSplitGrid {
   double* M2;
   double* mass_partials;  // NULL: no phase-mass sums
   unsigned* status;
+  float* cfl_out;  // NULL: no CFL numbers; else the step's [2] slot (max-combined with atomicMax)
 };
 
 int gbf_split_alloc(gbf_domain* d);

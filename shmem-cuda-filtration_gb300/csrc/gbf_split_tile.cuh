@@ -262,8 +262,9 @@ __device__ __forceinline__ float split_Pk(const GbfSplitConsts& C, int md, float
 template <bool DF>
 struct GbfSplitAcc {
   typename Wide<DF>::T m1, m2;
+  float cfl1, cfl2;  // largest CFL numbers of the thread's cells (when requested)
   unsigned bad;
-  __device__ GbfSplitAcc() : m1(Wide<DF>::f(0.f)), m2(Wide<DF>::f(0.f)), bad(0) {}
+  __device__ GbfSplitAcc() : m1(Wide<DF>::f(0.f)), m2(Wide<DF>::f(0.f)), cfl1(0.f), cfl2(0.f), bad(0) {}
 };
 
 // ------------------------------------------------------- one cell's update
@@ -293,7 +294,7 @@ struct GbfCellOut {
 // second Newton iteration) run for all lanes when any lane needs them and
 // select per lane. Lanes with count[n] false are computed but neither added
 // to the mass sums nor checked for non-finite values.
-template <bool DF, int N>
+template <bool DF, int N, bool CFL = false>
 __device__ __forceinline__ void split_cells(const GbfSplitConsts& C, const GbfCellIn (&in)[N],
                                             const typename Wide<DF>::T (&M1)[N],
                                             const typename Wide<DF>::T (&M2)[N], typename Wide<DF>::T R01,
@@ -327,6 +328,20 @@ __device__ __forceinline__ void split_cells(const GbfSplitConsts& C, const GbfCe
     const float dtphi = __fdividef(C.dt, in[n].phi);
     dm1[n] = -dtphi * f;  // FP32 mass increments
     dm2[n] = -dtphi * gs;
+    if (CFL && count[n]) {
+      // CFL number of each phase: the largest face volumetric flux of the cell
+      // (mass flux x L_upwind over the reference density) times dt / (phi h)
+      // (the mobilities L are <= 0: magnitudes by fabsf)
+      auto face = [](float x, float Lpos, float Lneg) { return fabsf(x * (x >= 0.f ? Lpos : Lneg)); };
+      const float c1 = fmaxf(fmaxf(fmaxf(face(x1, in[n].L1xm, L1c), face(x2, L1c, in[n].L1xp)) * C.inv_h1,
+                                   C.kv * fmaxf(face(y11, in[n].L1ym, L1c), face(y21, L1c, in[n].L1yp)) * C.inv_h2),
+                             fmaxf(face(z1, in[n].L1m, L1c), face(z2, L1c, in[n].L1p)) * C.inv_h3);
+      const float c2 = fmaxf(fmaxf(fmaxf(face(x1, in[n].L2xm, L2c), face(x2, L2c, in[n].L2xp)) * C.inv_h1,
+                                   C.kv * fmaxf(face(y12, in[n].L2ym, L2c), face(y22, L2c, in[n].L2yp)) * C.inv_h2),
+                             fmaxf(face(z1, in[n].L2m, L2c), face(z2, L2c, in[n].L2p)) * C.inv_h3);
+      acc.cfl1 = fmaxf(acc.cfl1, c1 * dtphi * C.cfl1);
+      acc.cfl2 = fmaxf(acc.cfl2, c2 * dtphi * C.cfl2);
+    }
     // mass targets T = M + dm (wide)
     T1[n] = W::add_f(M1[n], dm1[n]);
     T2[n] = W::add_f(M2[n], dm2[n]);
@@ -437,7 +452,7 @@ __device__ __forceinline__ void split_cells(const GbfSplitConsts& C, const GbfCe
 // call returns false if a bounded wait gave up (the status word then carries
 // GBF_DEV_TIMEOUT). `phases` holds the barrier parities across calls.
 // TMA = false: plain loads, one plane prefetched in registers, two buffers.
-template <bool DF, int TX = kSplitTX, int TY = kSplitTY, bool TMA = false>
+template <bool DF, int TX = kSplitTX, int TY = kSplitTY, bool TMA = false, bool CFL = false>
 __device__ bool split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i0, int j0, int k0, int k1,
                            GbfSplitPlaneT<TX, TY, gbf_plane_pitch<TX, TMA>()>* pl, GbfSplitAcc<DF>& acc,
                            GbfRawRing<TX, TY>* raw = nullptr, const GbfTmaSet* maps = nullptr, int buf = 0,
@@ -655,8 +670,8 @@ __device__ bool split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i
       const int cis[1] = {i};
       const bool cnt[1] = {true};
       GbfCellOut<DF> os[1];
-      split_cells<DF, 1>(C, ins, m1s, m2s, R01, R02, md, cis, j, k, G.phi != nullptr, G.mass_partials != nullptr,
-                         cnt, acc, os);
+      split_cells<DF, 1, CFL>(C, ins, m1s, m2s, R01, R02, md, cis, j, k, G.phi != nullptr,
+                              G.mass_partials != nullptr, cnt, acc, os);
       G.dPn[c] = os[0].dPn;
       G.Sn[c] = os[0].Sn;
       W::store(G.M1, c, os[0].M1n);
@@ -734,6 +749,29 @@ __device__ __forceinline__ float gbf_split_sweep_dP(const gbf_model& m, const Gb
     break;
   }
   return has_add ? base + add : base;
+}
+
+// Block maximum of the threads' CFL numbers (warp shuffles, then one thread
+// over the warps' maxima), max-combined into out[2] with atomicMax on the
+// bit patterns (non-negative floats order like their bits; NaN left out).
+// Every thread of the block calls it.
+template <int NT>
+__device__ __forceinline__ void split_block_cfl(float c1, float c2, float* out) {
+  __shared__ float red[2][NT / 32];
+  for (int o = 16; o > 0; o >>= 1) {
+    c1 = fmaxf(c1, __shfl_xor_sync(0xffffffffu, c1, o));
+    c2 = fmaxf(c2, __shfl_xor_sync(0xffffffffu, c2, o));
+  }
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) { red[0][w] = c1; red[1][w] = c2; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float a = 0.f, b = 0.f;
+    for (int q = 0; q < NT / 32; q++) { a = fmaxf(a, red[0][q]); b = fmaxf(b, red[1][q]); }
+    atomicMax(reinterpret_cast<unsigned*>(out), __float_as_uint(a));
+    atomicMax(reinterpret_cast<unsigned*>(out) + 1, __float_as_uint(b));
+  }
+  __syncthreads();  // red is reused by the next tile of a persistent CTA
 }
 
 // Deterministic block reduction of the phase-mass partial sums (FP64).
@@ -815,7 +853,7 @@ template <> struct WidePair<true> {  // FP32-pair masses: four floats
 // of rows j0 .. j0 + TY - 1, planes k0 .. k1 - 1. Same staging protocol,
 // bounded waits and give-up as split_tile<..., TMA = true>; each cell is
 // updated by split_cell, so results equal the other tiles' bit for bit.
-template <bool DF, int TXC, int TY>
+template <bool DF, int TXC, int TY, bool CFL = false>
 __device__ bool split_tile_x2(const GbfSplitConsts& C, const GbfSplitGrid& G, int x0, int j0, int k0, int k1,
                               GbfPairSmem<TXC, TY>& sm, GbfSplitAcc<DF>& acc, const GbfTmaSet* maps, int buf,
                               unsigned* phases) {
@@ -984,7 +1022,8 @@ __device__ bool split_tile_x2(const GbfSplitConsts& C, const GbfSplitGrid& G, in
       const int cis[2] = {ia, ia + 1};
       const bool cnt[2] = {act_a, act_b};
       GbfCellOut<DF> o[2];
-      split_cells<DF, 2>(C, in, m1s, m2s, R01, R02, 0, cis, j, k, true, G.mass_partials != nullptr, cnt, acc, o);
+      split_cells<DF, 2, CFL>(C, in, m1s, m2s, R01, R02, 0, cis, j, k, true, G.mass_partials != nullptr, cnt,
+                              acc, o);
       // The x faces i = 0 and i = nx - 1 (rows and planes interior) take the
       // boundary rules' values here: the new S of the x-neighbour and its dP
       // (cpu.cpp:327-331, 366-372), or the hydrostatic side value dP = 0 with

@@ -89,6 +89,13 @@ class Domain:
         """The reference's Tecplot files (save_data_plots) under `directory`."""
         abi.check(self.lib.gbf_domain_write_plots(self.h, str(directory).encode(), t), "write_plots")
 
+    def cfl_history(self, max_steps: int) -> np.ndarray:
+        """CFL numbers [step][2] (GBF_OUT_CFL with GBF_OUT_MASS)."""
+        out = np.zeros((max_steps, 2), np.float32)
+        n = ctypes.c_int()
+        abi.check(self.lib.gbf_domain_cfl_history(self.h, out.ctypes.data, max_steps, ctypes.byref(n)), "cfl")
+        return out[: n.value]
+
     def mass_history(self, max_steps: int) -> np.ndarray:
         out = np.zeros((max_steps, 2), np.float64)
         n = ctypes.c_int()

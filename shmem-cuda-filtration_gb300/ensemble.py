@@ -113,6 +113,13 @@ class Ensemble:
         abi.check(self.lib.gbf_ensemble_download(self.h, r, abi.FIELD_ID[field], out.ctypes.data), "download")
         return out
 
+    def cfl_history(self, max_steps: int) -> np.ndarray:
+        """CFL numbers [step][member][2] (GBF_OUT_CFL with GBF_OUT_MASS)."""
+        out = np.zeros((max_steps, self.n, 2), np.float32)
+        k = ctypes.c_int()
+        abi.check(self.lib.gbf_ensemble_cfl_history(self.h, out.ctypes.data, max_steps, ctypes.byref(k)), "cfl")
+        return out[: k.value]
+
     def mass_history(self, max_steps: int) -> np.ndarray:
         out = np.zeros((max_steps, self.n, 2), np.float64)
         k = ctypes.c_int()
