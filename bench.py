@@ -403,16 +403,20 @@ def accuracy_block(pkg, O, members, prec, ensemble, steps=20):
 
     def run(p):
         r = Runner(pkg, members, p, ensemble, steps + 2)
+        split = p != abi.GBF_PREC_F64
+        if split:
+            r.set_outputs(abi.GBF_OUT_MASS | abi.GBF_OUT_CFL, steps + 2)
         r.upload_initial()
         r.step(steps)
         out = [(r.download(i, "P1"), r.download(i, "S2")) for i in range(len(members))] if ensemble else \
             [(r.download(0, "P1"), r.download(0, "S2"))]
         mass = r.mass_history(steps)
+        cfl = r.cfl_history(steps) if split else None
         r.close()
-        return out, mass
+        return out, mass, cfl
 
-    got, mg = run(prec)
-    ref, mr = run(abi.GBF_PREC_F64)
+    got, mg, cfl = run(prec)
+    ref, mr, _ = run(abi.GBF_PREC_F64)
     ds = max(float(np.abs(a[1] - b[1]).max()) for a, b in zip(got, ref))
     num = sum(float(np.sum((a[0] - b[0]) ** 2)) for a, b in zip(got, ref))
     den = sum(float(np.sum(b[0] ** 2)) for b in ref)
@@ -420,7 +424,8 @@ def accuracy_block(pkg, O, members, prec, ensemble, steps=20):
     scale = np.maximum(np.abs(mr), 1e-300)
     drift = float(np.max(np.abs(mg - mr) / scale * (np.abs(mr) > 0)))
     block = {"vs": "plain FP64 GPU path of the same members (pinned to the oracle at 1e-12)", "steps": steps,
-             "max_dS": ds, "rel_l2_P": (num / den) ** 0.5, "phase_mass_rel_diff_max": drift, "S_moved_max": moved}
+             "max_dS": ds, "rel_l2_P": (num / den) ** 0.5, "phase_mass_rel_diff_max": drift, "S_moved_max": moved,
+             "cfl_max": [float(cfl[..., 0].max()), float(cfl[..., 1].max())]}
     # the oracle itself on the smallest member
     i = min(range(len(members)), key=lambda q: members[q].ncells)
     mem = members[i]
