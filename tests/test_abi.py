@@ -93,6 +93,24 @@ def test_validate_rejects_bad_models(abi, lib):
     cells = abi.GbfCells()
     cells.media = media.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
     assert lib.gbf_model_validate(ctypes.byref(m), ctypes.byref(cells), 0) == abi.GBF_ERR_ARG
+    # the largest grid the 32-bit cell offsets allow, and one cell-plane more
+    ok = abi.reference_model(1024, 1024, 2047, 0.02)  # 2^31 - 2^20 cells
+    assert lib.gbf_model_validate(ctypes.byref(ok), None, 0) == abi.GBF_OK
+    big = abi.reference_model(1024, 1024, 2048, 0.02)  # 2^31 cells
+    assert lib.gbf_model_validate(ctypes.byref(big), None, 0) == abi.GBF_ERR_ARG
+    for dims in ((3, 3, 3), (3, 40, 3)):  # the smallest grids with an interior cell
+        assert lib.gbf_model_validate(ctypes.byref(abi.reference_model(*dims, 0.001)), None, 0) == abi.GBF_OK
+    for dims in ((0, 16, 16), (16, -1, 16), (16, 16, 2)):
+        assert lib.gbf_model_validate(ctypes.byref(abi.reference_model(*dims, 0.02)), None, 0) == abi.GBF_ERR_ARG
+    bad = m.copy(); bad.h2 = 0.0
+    assert lib.gbf_model_validate(ctypes.byref(bad), None, 0) == abi.GBF_ERR_ARG
+    bad = m.copy(); bad.kv = -1.0
+    assert lib.gbf_model_validate(ctypes.byref(bad), None, 0) == abi.GBF_ERR_ARG
+    K = np.full(m.shape, 6.64e-11, np.float32)
+    K[3, 4, 5] = np.nan
+    cells = abi.GbfCells()
+    cells.K = K.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+    assert lib.gbf_model_validate(ctypes.byref(m), ctypes.byref(cells), 0) == abi.GBF_ERR_ARG
     lib.gbf_clear_status()
 
 
