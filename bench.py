@@ -5,9 +5,10 @@
 
 Workloads are <config>_<precision>: config0..config4 (the benchmark
 configurations as seeded synthetic inputs, see workloads.py) and f64, split
-(FP64 masses), splitdf (FP32-pair masses). The default, config4_splitdf, is
-the combined precision + batching form on the 256-member ensemble; the same
-line also reports plain FP64 and FP64-mass split on the same members.
+(FP64 masses), splitdf (FP32-pair masses), splitdefect (FP32 mass defects).
+The default, config4_splitdf, is the combined precision + batching form on
+the 256-member ensemble; the same line also reports plain FP64 and the other
+split forms on the same members.
 
 One JSON line on rank 0. `value` is device-resident throughput (inputs in
 HBM, CUDA events on the stream the kernels run on, CUDA graphs for
@@ -133,7 +134,9 @@ def barrier(world):
 PRECISIONS = {"f64": ("GBF_PREC_F64", "plain FP64", "f64"),
               "split": ("GBF_PREC_SPLIT", "FP32 state and fluxes, FP64 masses and residual", "f32+f64"),
               "splitdf": ("GBF_PREC_SPLIT_DF", "FP32 state and fluxes, FP32-pair masses and residual",
-                          "f32+f32x2")}
+                          "f32+f32x2"),
+              "splitdefect": ("GBF_PREC_SPLIT_DEFECT", "FP32 state and fluxes, phase masses as FP32 defects over "
+                              "the state's mass at the row's hydrostatic density", "f32")}
 
 
 def make_members(pkg, lib, cfg, cube):
@@ -212,6 +215,8 @@ ALGO_BYTES = {
     "split_step": (56.0, "interior"),       # read dP, S, K, phi (16), M1, M2 (16); write dP, S (8), M1, M2 (16)
     "ensemble_step": (56.0, "interior"),
 }
+# The defect form holds M1, M2 in 4 bytes: read 16 + 8, write 8 + 8.
+ALGO_BYTES_DEFECT = {"split_step": (40.0, "interior"), "ensemble_step": (40.0, "interior")}
 
 
 def timed(runner, steps, stream, world, clocks=None):
@@ -303,7 +308,7 @@ def run_ours(args, rank, world):
     hbm, peak_kind = peaks()
     kname, (kms, klaunch) = max(ktimes.items(), key=lambda kv: kv[1][0])
     per_launch_s = kms / 1e3 / max(klaunch, 1)
-    bpc, which = ALGO_BYTES.get(kname, (0.0, "all"))
+    bpc, which = (ALGO_BYTES_DEFECT if p == "splitdefect" else ALGO_BYTES).get(kname, ALGO_BYTES.get(kname, (0.0, "all")))
     algo = bpc * (run.interior_cells if which == "interior" else cells)
     achieved = algo / per_launch_s / 1e9 if per_launch_s > 0 else 0.0
     traffic = None
@@ -369,7 +374,7 @@ def run_ours(args, rank, world):
 
     if ensemble and not args.no_compare and rank == 0:
         comp = {}
-        for q in ("f64", "split", "splitdf"):
+        for q in ("f64", "split", "splitdf", "splitdefect"):
             if q == p:
                 continue
             r2 = Runner(pkg, members, getattr(abi, PRECISIONS[q][0]), True, cap)

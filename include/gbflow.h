@@ -43,8 +43,14 @@ enum { GBF_BC_REFERENCE = 0,           /* reference Border_S2/Border_P1 rules   
                                           no-flow bottom face for both phases          */
 enum { GBF_PREC_F64 = 0,               /* plain FP64 state and arithmetic               */
        GBF_PREC_SPLIT = 1,             /* FP32 P,S,K,fluxes; FP64 phase masses and residual */
-       GBF_PREC_SPLIT_DF = 2 };        /* as SPLIT, masses and residual as FP32 pairs
+       GBF_PREC_SPLIT_DF = 2,          /* as SPLIT, masses and residual as FP32 pairs
                                           (about 48 significant bits, FP32 pipes only)  */
+       GBF_PREC_SPLIT_DEFECT = 3 };    /* as SPLIT, each phase mass held as its FP32
+                                          excess ("defect") over the mass the FP32 state
+                                          gives at the row's hydrostatic density, an
+                                          exact product: 4 bytes a phase and cell, the
+                                          residual and mass update in FP32 on small
+                                          numbers (FP32 pipes only)                     */
 
 /* Fields that can be read back (gbf_domain_download / ensemble download). */
 enum {
@@ -179,7 +185,9 @@ int gbf_boundary_f64_noalloc(const gbf_model* m, gbf_arrays d_arrays, void* stre
  * GBF_PREC_F64 (plain FP64: two passes per step — properties, then fluxes,
  * mass update and Newton fused — plus a face pass for the boundaries) or
  * GBF_PREC_SPLIT (FP32 P, S, K, phi and fluxes; FP64 per-cell phase masses
- * and one FP64 residual per cell). All calls are ordered on the domain's
+ * and one FP64 residual per cell), GBF_PREC_SPLIT_DF (the masses and residual
+ * as FP32 pairs) or GBF_PREC_SPLIT_DEFECT (the masses as FP32 defects). All
+ * calls are ordered on the domain's
  * stream; gbf_domain_step only enqueues work.
  */
 typedef struct gbf_domain gbf_domain;

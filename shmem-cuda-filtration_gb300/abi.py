@@ -16,7 +16,7 @@ GBF_OK, GBF_ERR_ARG, GBF_ERR_CUDA, GBF_ERR_NOMEM, GBF_ERR_NONFINITE, GBF_ERR_UNS
     GBF_ERR_TIMEOUT, GBF_ERR_STATE = range(8)
 GBF_SOURCE_DIRICHLET_PATCH, GBF_SOURCE_RATE = 0, 1
 GBF_BC_REFERENCE, GBF_BC_HYDROSTATIC_SIDES = 0, 1
-GBF_PREC_F64, GBF_PREC_SPLIT, GBF_PREC_SPLIT_DF = 0, 1, 2
+GBF_PREC_F64, GBF_PREC_SPLIT, GBF_PREC_SPLIT_DF, GBF_PREC_SPLIT_DEFECT = 0, 1, 2, 3
 GBF_OUT_MASS, GBF_OUT_VELOCITY, GBF_OUT_MASS_ARRAYS, GBF_OUT_PROPS, GBF_OUT_CFL = 1, 2, 4, 8, 16
 
 FIELDS = ["P1", "S2", "P2", "ro1", "ro2", "Xi1", "Xi2", "u1x", "u1y", "u1z",

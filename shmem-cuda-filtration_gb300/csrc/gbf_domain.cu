@@ -148,7 +148,8 @@ int gbf_domain_create(const gbf_model* m, const gbf_cells* host_cells, int preci
   if (!out) return gbf_fail(GBF_ERR_ARG, "gbf_domain_create: out");
   *out = nullptr;
   if (int s = gbf_model_validate(m, host_cells, 0)) return s;
-  if (precision != GBF_PREC_F64 && precision != GBF_PREC_SPLIT && precision != GBF_PREC_SPLIT_DF)
+  if (precision != GBF_PREC_F64 && precision != GBF_PREC_SPLIT && precision != GBF_PREC_SPLIT_DF &&
+      precision != GBF_PREC_SPLIT_DEFECT)
     return gbf_fail(GBF_ERR_ARG, "precision");
   gbf_domain* d = new gbf_domain();
   d->m = *m;

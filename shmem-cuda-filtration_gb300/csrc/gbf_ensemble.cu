@@ -66,7 +66,7 @@ __device__ __forceinline__ float* ens_cfl_slot(const EnsCfl& cfl, int member) {
   return step < (unsigned)cfl.cap ? cfl.hist + 2 * ((size_t)step * cfl.n + member) : nullptr;
 }
 
-template <bool DF, int TX, int TY, bool TMA, bool CFL>
+template <int MR, int TX, int TY, bool TMA, bool CFL>
 __global__ void __launch_bounds__(TX * TY, 1024 / (TX * TY)) k_ens_split_step(const EnsMember* __restrict__ mem,
                                                                              const int4* __restrict__ tiles,
                                                                              int ntiles, int cur,
@@ -79,14 +79,14 @@ __global__ void __launch_bounds__(TX * TY, 1024 / (TX * TY)) k_ens_split_step(co
   __shared__ GbfSplitGrid Gs;
   __shared__ int s_tile;
   constexpr int NT = TX * TY;
-  GbfRawRing<TX, TY>* raw = nullptr;
+  GbfRawRing<TX, TY, MR>* raw = nullptr;
   unsigned phases = 0;  // barrier parities of the stages, carried from tile to tile
   if constexpr (TMA) {
-    __shared__ __align__(128) GbfRawRing<TX, TY> ring;
+    __shared__ __align__(128) GbfRawRing<TX, TY, MR> ring;
     raw = &ring;
     if (threadIdx.x == 0) {
       for (int s = 0; s < kTmaStages; s++) gbf_mbar_init(&ring.bar[s], 1);
-      for (int s = 0; s < GbfRawRing<TX, TY>::RS; s++) gbf_mbar_init(&ring.mbar[s], 1);
+      for (int s = 0; s < GbfRawRing<TX, TY, MR>::RS; s++) gbf_mbar_init(&ring.mbar[s], 1);
       gbf_mbar_fence_init();
     }
     __syncthreads();
@@ -118,24 +118,25 @@ __global__ void __launch_bounds__(TX * TY, 1024 / (TX * TY)) k_ens_split_step(co
       Gs.cfl_out = CFL ? ens_cfl_slot(cfl, tl.x) : nullptr;
     }
     __syncthreads();
-    GbfSplitAcc<DF> acc;
-    const bool ok = split_tile<DF, TX, TY, TMA, CFL>(Cs, Gs, tl.y, tl.z, tl.w & 0xffff, tl.w >> 16, pl, acc, raw,
+    GbfSplitAcc<MR> acc;
+    const bool ok = split_tile<MR, TX, TY, TMA, CFL>(Cs, Gs, tl.y, tl.z, tl.w & 0xffff, tl.w >> 16, pl, acc, raw,
                                                 TMA ? maps + tl.x : nullptr, cur, &phases);
     if (!ok) break;  // a plane wait gave up (status set); the whole CTA stops
     if (acc.bad) atomicOr(status, GBF_DEV_NONFINITE);
-    if (partials) split_block_mass<DF, NT>(acc, Cs.V, partials + 2 * t);
+    if (partials) split_block_mass<MR, NT>(acc, Cs.V, partials + 2 * t);
     if constexpr (CFL)
       if (Gs.cfl_out) split_block_cfl<NT>(acc.cfl1, acc.cfl2, Gs.cfl_out);
     __syncthreads();
   }
 }
 
-template <bool DF, int TXC, int TY, bool CFL>
+template <int MR, int TXC, int TY, bool CFL>
 __global__ void __launch_bounds__(TXC / 2 * TY, 512 / (TXC / 2 * TY)) k_ens_split_step_x2(
     const EnsMember* __restrict__ mem, const int4* __restrict__ tiles, int ntiles, int cur, unsigned* counter,
     double* partials, unsigned* status, const GbfTmaSet* __restrict__ maps, const EnsCfl cfl) {
   extern __shared__ __align__(128) unsigned char dyn[];
-  GbfPairSmem<TXC, TY>& sm = *reinterpret_cast<GbfPairSmem<TXC, TY>*>(dyn);
+  using Smem = GbfPairSmem<TXC, TY, MR>;
+  Smem& sm = *reinterpret_cast<Smem*>(dyn);
   __shared__ GbfSplitConsts Cs;
   __shared__ GbfSplitGrid Gs;
   __shared__ int s_tile;
@@ -147,7 +148,7 @@ __global__ void __launch_bounds__(TXC / 2 * TY, 512 / (TXC / 2 * TY)) k_ens_spli
   }
   if (threadIdx.x == 0) {
     for (int s = 0; s < kTmaStages; s++) gbf_mbar_init(&sm.ring.bar[s], 1);
-    for (int s = 0; s < GbfPairRing<TXC, TY>::RS; s++) gbf_mbar_init(&sm.ring.mbar[s], 1);
+    for (int s = 0; s < Smem::Ring::RS; s++) gbf_mbar_init(&sm.ring.mbar[s], 1);
     gbf_mbar_fence_init();
   }
   __syncthreads();
@@ -178,12 +179,12 @@ __global__ void __launch_bounds__(TXC / 2 * TY, 512 / (TXC / 2 * TY)) k_ens_spli
       Gs.cfl_out = CFL ? ens_cfl_slot(cfl, tl.x) : nullptr;
     }
     __syncthreads();
-    GbfSplitAcc<DF> acc;
-    const bool ok = split_tile_x2<DF, TXC, TY, CFL>(Cs, Gs, tl.y, tl.z, tl.w & 0xffff, tl.w >> 16, sm, acc,
+    GbfSplitAcc<MR> acc;
+    const bool ok = split_tile_x2<MR, TXC, TY, CFL>(Cs, Gs, tl.y, tl.z, tl.w & 0xffff, tl.w >> 16, sm, acc,
                                                maps + tl.x, cur, &phases);
     if (!ok) break;
     if (acc.bad) atomicOr(status, GBF_DEV_NONFINITE);
-    if (partials) split_block_mass<DF, NT>(acc, Cs.V, partials + 2 * t);
+    if (partials) split_block_mass<MR, NT>(acc, Cs.V, partials + 2 * t);
     if constexpr (CFL)
       if (Gs.cfl_out) split_block_cfl<NT>(acc.cfl1, acc.cfl2, Gs.cfl_out);
     __syncthreads();
@@ -314,7 +315,7 @@ __global__ void __launch_bounds__(kThreads) k_ens_load(const EnsMember* __restri
     } else {
       const int j = (int)((c / (unsigned)m.nx) % (unsigned)m.ny);
       float dPf, Sf;
-      gbf_split_init_cell(m, p, s, j, dPf, Sf, me.M1, me.M2, c, precision == GBF_PREC_SPLIT_DF);
+      gbf_split_init_cell(m, p, s, j, dPf, Sf, me.M1, me.M2, c, gbf_mass_rep(precision));
       me.dPf[cur][c] = dPf;
       me.Sf[cur][c] = Sf;
       me.dPf[cur ^ 1][c] = dPf;
@@ -515,6 +516,7 @@ int build_lists(gbf_ensemble* e) {
   }
   const bool tma = split && tma_possible(e, TX);
   if (kShapePairs[e->shape] && !tma) return gbf_fail(GBF_ERR_ARG, "the x-pair tile needs TMA staging");
+  const int mb = gbf_mass_bytes(gbf_mass_rep(e->precision));  // bytes of a mass element
   if (tma && !s) {
     std::vector<GbfTmaSet> maps(e->n);
     int enc = GBF_OK;
@@ -527,8 +529,8 @@ int build_lists(gbf_ensemble* e) {
           enc |= gbf_tma_encode_box(&maps[r].S[b], me.Sf[b], 4, m.nx, m.ny, m.nz, TX + 8, TY + 2);
         }
         enc |= gbf_tma_encode_box(&maps[r].K, me.cells.K, 4, m.nx, m.ny, m.nz, TX + 8, TY + 2);
-        enc |= gbf_tma_encode_box(&maps[r].M1, me.M1, 8, m.nx, m.ny, m.nz, TX, TY);
-        enc |= gbf_tma_encode_box(&maps[r].M2, me.M2, 8, m.nx, m.ny, m.nz, TX, TY);
+        enc |= gbf_tma_encode_box(&maps[r].M1, me.M1, mb, m.nx, m.ny, m.nz, TX, TY);
+        enc |= gbf_tma_encode_box(&maps[r].M2, me.M2, mb, m.nx, m.ny, m.nz, TX, TY);
         enc |= gbf_tma_encode_box(&maps[r].phi, me.cells.phi, 4, m.nx, m.ny, m.nz, TX, TY);
         continue;
       }
@@ -537,8 +539,8 @@ int build_lists(gbf_ensemble* e) {
         enc |= gbf_tma_encode_plane(&maps[r].S[b], me.Sf[b], m.nx, m.ny, m.nz, TX, TY);
       }
       enc |= gbf_tma_encode_plane(&maps[r].K, me.cells.K, m.nx, m.ny, m.nz, TX, TY);
-      enc |= gbf_tma_encode_rows(&maps[r].M1, me.M1, 8, m.nx, m.ny, m.nz, TX, TY);
-      enc |= gbf_tma_encode_rows(&maps[r].M2, me.M2, 8, m.nx, m.ny, m.nz, TX, TY);
+      enc |= gbf_tma_encode_rows(&maps[r].M1, me.M1, mb, m.nx, m.ny, m.nz, TX, TY);
+      enc |= gbf_tma_encode_rows(&maps[r].M2, me.M2, mb, m.nx, m.ny, m.nz, TX, TY);
       enc |= gbf_tma_encode_rows(&maps[r].phi, me.cells.phi, 4, m.nx, m.ny, m.nz, TX, TY);
     }
     if (!enc)
@@ -562,11 +564,11 @@ EnsCfl ens_cfl(const gbf_ensemble* e) {
   return {e->d_mass_count, on ? e->d_cfl_hist : nullptr, e->n, e->mass_cap};
 }
 
-template <bool DF, int TX, int TY>
+template <int MR, int TX, int TY>
 int launch_split_step_t(gbf_ensemble* e, double* partials, cudaStream_t st, const TileRange& tr) {
   const bool tma = e->d_maps != nullptr, cfl = partials && ens_cfl(e).hist;
-  auto kern = tma ? (cfl ? k_ens_split_step<DF, TX, TY, true, true> : k_ens_split_step<DF, TX, TY, true, false>)
-                  : (cfl ? k_ens_split_step<DF, TX, TY, false, true> : k_ens_split_step<DF, TX, TY, false, false>);
+  auto kern = tma ? (cfl ? k_ens_split_step<MR, TX, TY, true, true> : k_ens_split_step<MR, TX, TY, true, false>)
+                  : (cfl ? k_ens_split_step<MR, TX, TY, false, true> : k_ens_split_step<MR, TX, TY, false, false>);
   int per_sm = 0;
   GBF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TX * TY, 0));
   const int blocks = std::max(1, std::min(tr.nt, per_sm * gbf_num_sms()));
@@ -577,11 +579,11 @@ int launch_split_step_t(gbf_ensemble* e, double* partials, cudaStream_t st, cons
   return GBF_OK;
 }
 
-template <bool DF, int TXC, int TY>
+template <int MR, int TXC, int TY>
 int launch_split_step_x2(gbf_ensemble* e, double* partials, cudaStream_t st, const TileRange& tr) {
   if (!e->d_maps) return gbf_fail(GBF_ERR_STATE, "x-pair tile without TMA maps");
-  auto kern = (partials && ens_cfl(e).hist) ? k_ens_split_step_x2<DF, TXC, TY, true> : k_ens_split_step_x2<DF, TXC, TY, false>;
-  const int bytes = (int)sizeof(GbfPairSmem<TXC, TY>);
+  auto kern = (partials && ens_cfl(e).hist) ? k_ens_split_step_x2<MR, TXC, TY, true> : k_ens_split_step_x2<MR, TXC, TY, false>;
+  const int bytes = (int)sizeof(GbfPairSmem<TXC, TY, MR>);
   GBF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
   int per_sm = 0;
   GBF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TXC / 2 * TY, bytes));
@@ -593,13 +595,21 @@ int launch_split_step_x2(gbf_ensemble* e, double* partials, cudaStream_t st, con
   return GBF_OK;
 }
 
-int launch_split_step(gbf_ensemble* e, double* partials, cudaStream_t st, const TileRange& tr) {
-  const bool df = e->precision == GBF_PREC_SPLIT_DF;
+template <int MR>
+int launch_split_form(gbf_ensemble* e, double* partials, cudaStream_t st, const TileRange& tr) {
   switch (e->shape) {
-    case kShape64x8x2: return df ? launch_split_step_x2<true, 64, 8>(e, partials, st, tr) : launch_split_step_x2<false, 64, 8>(e, partials, st, tr);
-    case kShape64x4: return df ? launch_split_step_t<true, 64, 4>(e, partials, st, tr) : launch_split_step_t<false, 64, 4>(e, partials, st, tr);
-    case kShape32x4: return df ? launch_split_step_t<true, 32, 4>(e, partials, st, tr) : launch_split_step_t<false, 32, 4>(e, partials, st, tr);
-    default: return df ? launch_split_step_t<true, 32, 8>(e, partials, st, tr) : launch_split_step_t<false, 32, 8>(e, partials, st, tr);
+    case kShape64x8x2: return launch_split_step_x2<MR, 64, 8>(e, partials, st, tr);
+    case kShape64x4: return launch_split_step_t<MR, 64, 4>(e, partials, st, tr);
+    case kShape32x4: return launch_split_step_t<MR, 32, 4>(e, partials, st, tr);
+    default: return launch_split_step_t<MR, 32, 8>(e, partials, st, tr);
+  }
+}
+
+int launch_split_step(gbf_ensemble* e, double* partials, cudaStream_t st, const TileRange& tr) {
+  switch (gbf_mass_rep(e->precision)) {
+    case kMassDefect: return launch_split_form<kMassDefect>(e, partials, st, tr);
+    case kMassDF: return launch_split_form<kMassDF>(e, partials, st, tr);
+    default: return launch_split_form<kMassF64>(e, partials, st, tr);
   }
 }
 
@@ -727,7 +737,8 @@ int gbf_ensemble_create(int n, const gbf_model* models, const gbf_cells* host_ce
                         gbf_ensemble** out) {
   if (!out || n < 1 || !models) return gbf_fail(GBF_ERR_ARG, "gbf_ensemble_create");
   *out = nullptr;
-  if (precision != GBF_PREC_F64 && precision != GBF_PREC_SPLIT && precision != GBF_PREC_SPLIT_DF)
+  if (precision != GBF_PREC_F64 && precision != GBF_PREC_SPLIT && precision != GBF_PREC_SPLIT_DF &&
+      precision != GBF_PREC_SPLIT_DEFECT)
     return gbf_fail(GBF_ERR_ARG, "precision");
   for (int r = 0; r < n; r++)
     if (int s = gbf_model_validate(&models[r], host_cells ? &host_cells[r] : nullptr, 0)) return s;
@@ -764,8 +775,8 @@ int gbf_ensemble_create(int n, const gbf_model* models, const gbf_cells* host_ce
         s |= ens_alloc(e, (void**)&me.dPf[b], nc * sizeof(float));
         s |= ens_alloc(e, (void**)&me.Sf[b], nc * sizeof(float));
       }
-      s |= ens_alloc(e, (void**)&me.M1, nc * sizeof(double));
-      s |= ens_alloc(e, (void**)&me.M2, nc * sizeof(double));
+      s |= ens_alloc(e, (void**)&me.M1, nc * gbf_mass_bytes(gbf_mass_rep(precision)));
+      s |= ens_alloc(e, (void**)&me.M2, nc * gbf_mass_bytes(gbf_mass_rep(precision)));
     } else {
       for (int b = 0; b < 2; b++) {
         s |= ens_alloc(e, (void**)&me.P[b], nc * sizeof(double));
@@ -857,7 +868,7 @@ int gbf_ensemble_upload(gbf_ensemble* e, int r, const double* P1, const double* 
     GBF_CUDA(cudaMemcpyAsync(tmp, P1, b, cudaMemcpyDefault, e->stream));
     GBF_CUDA(cudaMemcpyAsync(tmp + nc, S2, b, cudaMemcpyDefault, e->stream));
     if (int s = gbf_split_init_state(m, tmp, tmp + nc, me.dPf[c], me.Sf[c], me.M1, me.M2,
-                                     e->precision == GBF_PREC_SPLIT_DF, e->stream))
+                                     gbf_mass_rep(e->precision), e->stream))
       return s;
     // the next-state buffer's faces are rewritten every step; start them equal
     GBF_CUDA(cudaMemcpyAsync(me.dPf[c ^ 1], me.dPf[c], nc * sizeof(float), cudaMemcpyDeviceToDevice, e->stream));

@@ -10,8 +10,9 @@
 //   S   = S2, FP32.
 //   M1, M2 (interior cells): the phase masses per pore volume the
 //         reference's mass update starts from, ro1 (1 - S2) and ro2 S2 with
-//         ro2 at P2 = P1 (cpu.cpp:224-225), in FP64 (GBF_PREC_SPLIT) or as an
-//         unevaluated sum of two FP32 (GBF_PREC_SPLIT_DF).
+//         ro2 at P2 = P1 (cpu.cpp:224-225), in FP64 (GBF_PREC_SPLIT), as an
+//         unevaluated sum of two FP32 (GBF_PREC_SPLIT_DF), or as FP32 defects
+//         over c1(j) (1 - S), c2(j) S (GBF_PREC_SPLIT_DEFECT).
 // The tile routine (gbf_split_tile.cuh) does the fused update of one column
 // tile; this file holds the single-domain kernels and the host side.
 #include <math.h>
@@ -63,6 +64,8 @@ GbfSplitConsts gbf_split_consts(const gbf_model& m) {
   C.H_d = H; C.beta1_d = m.beta1; C.beta2_d = m.beta2; C.ro01_d = m.ro01; C.ro02_d = m.ro02;
   C.dtsrc_d = m.dt * src;
   C.V = V;
+  C.ro01b1_d = m.ro01 * m.beta1;
+  C.ro02b2_d = m.ro02 * m.beta2;
   C.H_df = gbf_df_from_double(H);
   C.beta1_df = gbf_df_from_double(m.beta1);
   C.beta2_df = gbf_df_from_double(m.beta2);
@@ -90,7 +93,7 @@ __host__ __device__ int tiles_x2(const GbfSplitConsts& C) { return (C.nx - 1 + k
 __host__ __device__ int tiles_y2(const GbfSplitConsts& C) { return (C.ny - 2 + kPairTY - 1) / kPairTY; }
 
 // The plain-load tile on one grid (grids without TMA staging).
-template <bool DF, bool CFL>
+template <int MR, bool CFL>
 __global__ void __launch_bounds__(kSplitThreads, 4) k_split_step(const GbfSplitConsts C, const GbfSplitGrid G,
                                                               const int kchunk) {
   __shared__ GbfSplitPlane pl[2];
@@ -99,20 +102,21 @@ __global__ void __launch_bounds__(kSplitThreads, 4) k_split_step(const GbfSplitC
   const int tx = b % ntx, ty = (b / ntx) % nty, kc = b / (ntx * nty);
   const int k0 = 1 + kc * kchunk;
   const int k1 = min(k0 + kchunk, C.nz - 1);
-  GbfSplitAcc<DF> acc;
-  split_tile<DF, kSplitTX, kSplitTY, false, CFL>(C, G, 1 + tx * kSplitTX, 1 + ty * kSplitTY, k0, k1, pl, acc);
+  GbfSplitAcc<MR> acc;
+  split_tile<MR, kSplitTX, kSplitTY, false, CFL>(C, G, 1 + tx * kSplitTX, 1 + ty * kSplitTY, k0, k1, pl, acc);
   if (acc.bad) atomicOr(G.status, GBF_DEV_NONFINITE);
-  if (G.mass_partials) split_block_mass<DF>(acc, C.V, G.mass_partials + 2 * blockIdx.x);
+  if (G.mass_partials) split_block_mass<MR>(acc, C.V, G.mass_partials + 2 * blockIdx.x);
   if constexpr (CFL) split_block_cfl<kSplitThreads>(acc.cfl1, acc.cfl2, G.cfl_out);
 }
 
 // The x-pair tile on one grid: one tile (64 x 8 cells, a k range) per CTA.
-template <bool DF, bool CFL>
+template <int MR, bool CFL>
 __global__ void __launch_bounds__(kPairTX / 2 * kPairTY, 2) k_split_step_x2(const GbfSplitConsts C,
                                                                          const GbfSplitGrid G, const int kchunk,
                                                                          const GbfTmaSet* maps, int buf) {
   extern __shared__ __align__(128) unsigned char dyn[];
-  GbfPairSmem<kPairTX, kPairTY>& sm = *reinterpret_cast<GbfPairSmem<kPairTX, kPairTY>*>(dyn);
+  using Smem = GbfPairSmem<kPairTX, kPairTY, MR>;
+  Smem& sm = *reinterpret_cast<Smem*>(dyn);
   if (gbf_smem_u32(dyn) & 127u) {  // the TMA destinations need it; never expected to fire
     if (threadIdx.x == 0) atomicOr(G.status, GBF_DEV_TIMEOUT);
     return;
@@ -124,16 +128,16 @@ __global__ void __launch_bounds__(kPairTX / 2 * kPairTY, 2) k_split_step_x2(cons
   const int k1 = min(k0 + kchunk, C.nz - 1);
   if (threadIdx.x == 0) {
     for (int s = 0; s < kTmaStages; s++) gbf_mbar_init(&sm.ring.bar[s], 1);
-    for (int s = 0; s < GbfPairRing<kPairTX, kPairTY>::RS; s++) gbf_mbar_init(&sm.ring.mbar[s], 1);
+    for (int s = 0; s < Smem::Ring::RS; s++) gbf_mbar_init(&sm.ring.mbar[s], 1);
     gbf_mbar_fence_init();
   }
   __syncthreads();
   unsigned phases = 0;
-  GbfSplitAcc<DF> acc;
-  split_tile_x2<DF, kPairTX, kPairTY, CFL>(C, G, kPairTX * tx, 1 + kPairTY * ty, k0, k1, sm, acc, maps, buf,
+  GbfSplitAcc<MR> acc;
+  split_tile_x2<MR, kPairTX, kPairTY, CFL>(C, G, kPairTX * tx, 1 + kPairTY * ty, k0, k1, sm, acc, maps, buf,
                                            &phases);
   if (acc.bad) atomicOr(G.status, GBF_DEV_NONFINITE);
-  if (G.mass_partials) split_block_mass<DF, kPairTX / 2 * kPairTY>(acc, C.V, G.mass_partials + 2 * blockIdx.x);
+  if (G.mass_partials) split_block_mass<MR, kPairTX / 2 * kPairTY>(acc, C.V, G.mass_partials + 2 * blockIdx.x);
   if constexpr (CFL) split_block_cfl<kPairTX / 2 * kPairTY>(acc.cfl1, acc.cfl2, G.cfl_out);
 }
 
@@ -166,11 +170,11 @@ __global__ void k_split_mass_tail(const double* partials, int nblocks, double* o
 }
 
 __global__ void k_split_init(const gbf_model m, const double* P, const double* S, float* dPf, float* Sf,
-                             double* M1, double* M2, int df) {
+                             double* M1, double* M2, int mr) {
   const GbfGeo g = gbf_geo(m);
   for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < g.n; c += (size_t)gridDim.x * blockDim.x) {
     const int j = (int)((c / g.nx) % g.ny);
-    gbf_split_init_cell(m, P[c], S[c], j, dPf[c], Sf[c], M1, M2, c, df != 0);
+    gbf_split_init_cell(m, P[c], S[c], j, dPf[c], Sf[c], M1, M2, c, mr);
   }
 }
 
@@ -208,35 +212,38 @@ int gbf_split_kchunk_x2(const GbfSplitConsts& C) {
   return kchunk;
 }
 
-template <bool DF, bool CFL>
+template <int MR, bool CFL>
 int launch_x2(const GbfSplitConsts& C, const GbfSplitGrid& G, const GbfTmaSet* maps, int buf, cudaStream_t st,
               unsigned& blocks) {
   const int kchunk = gbf_split_kchunk_x2(C);
   blocks = (unsigned)(tiles_x2(C) * tiles_y2(C) * ((C.nz - 2 + kchunk - 1) / kchunk));
-  const int bytes = (int)sizeof(GbfPairSmem<kPairTX, kPairTY>);
-  GBF_CUDA(cudaFuncSetAttribute(k_split_step_x2<DF, CFL>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-  k_split_step_x2<DF, CFL><<<blocks, kPairTX / 2 * kPairTY, bytes, st>>>(C, G, kchunk, maps, buf);
+  const int bytes = (int)sizeof(GbfPairSmem<kPairTX, kPairTY, MR>);
+  GBF_CUDA(cudaFuncSetAttribute(k_split_step_x2<MR, CFL>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  k_split_step_x2<MR, CFL><<<blocks, kPairTX / 2 * kPairTY, bytes, st>>>(C, G, kchunk, maps, buf);
   return GBF_OK;
 }
 
-int gbf_split_launch_domain(const gbf_model& m, const GbfSplitConsts& C, const GbfSplitGrid& G, bool df,
+template <int MR>
+int launch_form(const GbfSplitConsts& C, const GbfSplitGrid& G, const GbfTmaSet* maps, int buf, cudaStream_t st,
+                unsigned& blocks, int kchunk) {
+  const bool cfl = G.cfl_out != nullptr;
+  if (maps) return cfl ? launch_x2<MR, true>(C, G, maps, buf, st, blocks) : launch_x2<MR, false>(C, G, maps, buf, st, blocks);
+  if (cfl) k_split_step<MR, true><<<blocks, kSplitThreads, 0, st>>>(C, G, kchunk);
+  else k_split_step<MR, false><<<blocks, kSplitThreads, 0, st>>>(C, G, kchunk);
+  return GBF_OK;
+}
+
+int gbf_split_launch_domain(const gbf_model& m, const GbfSplitConsts& C, const GbfSplitGrid& G, int mr,
                             double* mass_out, cudaStream_t st, GbfTimer* tm, const GbfTmaSet* maps, int buf) {
   const int kchunk = gbf_split_kchunk(C);
   const int nkc = (C.nz - 2 + kchunk - 1) / kchunk;
   unsigned blocks = (unsigned)(tiles_x(C) * tiles_y(C) * nkc);
   cudaEvent_t e = gbf_timer_begin(tm, st);
-  const bool cfl = G.cfl_out != nullptr;
-  if (maps) {  // TMA staging: the x-pair tile
-    int s = df ? (cfl ? launch_x2<true, true>(C, G, maps, buf, st, blocks) : launch_x2<true, false>(C, G, maps, buf, st, blocks))
-               : (cfl ? launch_x2<false, true>(C, G, maps, buf, st, blocks) : launch_x2<false, false>(C, G, maps, buf, st, blocks));
-    if (s) return s;
-  } else if (df) {
-    if (cfl) k_split_step<true, true><<<blocks, kSplitThreads, 0, st>>>(C, G, kchunk);
-    else k_split_step<true, false><<<blocks, kSplitThreads, 0, st>>>(C, G, kchunk);
-  } else {
-    if (cfl) k_split_step<false, true><<<blocks, kSplitThreads, 0, st>>>(C, G, kchunk);
-    else k_split_step<false, false><<<blocks, kSplitThreads, 0, st>>>(C, G, kchunk);
-  }
+  // TMA staging (maps): the x-pair tile; else the plain-load tile
+  const int s = mr == kMassDefect ? launch_form<kMassDefect>(C, G, maps, buf, st, blocks, kchunk)
+                : mr == kMassDF   ? launch_form<kMassDF>(C, G, maps, buf, st, blocks, kchunk)
+                                  : launch_form<kMassF64>(C, G, maps, buf, st, blocks, kchunk);
+  if (s) return s;
   gbf_timer_end(tm, GBF_K_SPLIT_STEP, e, st);
   e = gbf_timer_begin(tm, st);
   const size_t nb = maps ? gbf_boundary_count_no_xfaces(gbf_geo(m)) : gbf_boundary_count(gbf_geo(m));
@@ -269,9 +276,10 @@ int gbf_split_alloc(gbf_domain* d) {
     s |= gbf_domain_alloc(d, (void**)&d->Pf[b], n * sizeof(float));
     s |= gbf_domain_alloc(d, (void**)&d->Sf[b], n * sizeof(float));
   }
-  // FP64 masses or FP32 pairs: 8 bytes per cell and phase either way
-  if (!s) s |= gbf_domain_alloc(d, (void**)&d->M1, n * sizeof(double));
-  if (!s) s |= gbf_domain_alloc(d, (void**)&d->M2, n * sizeof(double));
+  // FP64 masses or FP32 pairs: 8 bytes per cell and phase; FP32 defects: 4
+  const int mb = gbf_mass_bytes(gbf_mass_rep(d->precision));
+  if (!s) s |= gbf_domain_alloc(d, (void**)&d->M1, n * mb);
+  if (!s) s |= gbf_domain_alloc(d, (void**)&d->M2, n * mb);
   // per-block mass partials of the split step kernel
   if (!s) s |= gbf_domain_alloc(d, (void**)&d->split_partials, 2 * sizeof(double) * gbf_split_blocks(d->m));
   if (s) return GBF_ERR_NOMEM;
@@ -287,8 +295,8 @@ int gbf_split_alloc(gbf_domain* d) {
       e |= gbf_tma_encode_box(&h.S[b], d->Sf[b], 4, m.nx, m.ny, m.nz, hx, hy);
     }
     if (!e) e |= gbf_tma_encode_box(&h.K, d->cells.K, 4, m.nx, m.ny, m.nz, hx, hy);
-    if (!e) e |= gbf_tma_encode_box(&h.M1, d->M1, 8, m.nx, m.ny, m.nz, kPairTX, kPairTY);
-    if (!e) e |= gbf_tma_encode_box(&h.M2, d->M2, 8, m.nx, m.ny, m.nz, kPairTX, kPairTY);
+    if (!e) e |= gbf_tma_encode_box(&h.M1, d->M1, mb, m.nx, m.ny, m.nz, kPairTX, kPairTY);
+    if (!e) e |= gbf_tma_encode_box(&h.M2, d->M2, mb, m.nx, m.ny, m.nz, kPairTX, kPairTY);
     if (!e) e |= gbf_tma_encode_box(&h.phi, d->cells.phi, 4, m.nx, m.ny, m.nz, kPairTX, kPairTY);
     if (!e && !gbf_domain_alloc(d, &d->tma, sizeof(GbfTmaSet))) {
       GBF_CUDA(cudaMemcpy(d->tma, &h, sizeof(GbfTmaSet), cudaMemcpyHostToDevice));
@@ -301,9 +309,9 @@ int gbf_split_alloc(gbf_domain* d) {
 }
 
 int gbf_split_init_state(const gbf_model& m, const double* P_dev, const double* S_dev, float* dPf, float* Sf,
-                         double* M1, double* M2, bool df, cudaStream_t st) {
+                         double* M1, double* M2, int mr, cudaStream_t st) {
   const size_t n = gbf_geo(m).n;
-  k_split_init<<<gbf_grid_for(n, kThreads, 4), kThreads, 0, st>>>(m, P_dev, S_dev, dPf, Sf, M1, M2, df ? 1 : 0);
+  k_split_init<<<gbf_grid_for(n, kThreads, 4), kThreads, 0, st>>>(m, P_dev, S_dev, dPf, Sf, M1, M2, mr);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? GBF_OK : gbf_cuda_check(e, "gbf_split_init_state");
 }
@@ -326,7 +334,7 @@ int gbf_split_upload(gbf_domain* d, const double* P1, const double* S2, cudaMemc
   }
   d->cur = 0;
   k_split_init<<<gbf_grid_for(n, kThreads, 4), kThreads, 0, d->stream>>>(
-      d->m, P, S, d->Pf[0], d->Sf[0], d->M1, d->M2, d->precision == GBF_PREC_SPLIT_DF);
+      d->m, P, S, d->Pf[0], d->Sf[0], d->M1, d->M2, gbf_mass_rep(d->precision));
   GBF_CUDA(cudaGetLastError());
   // the next-state buffer's faces are rewritten every step; start them equal
   GBF_CUDA(cudaMemcpyAsync(d->Pf[1], d->Pf[0], n * sizeof(float), cudaMemcpyDeviceToDevice, d->stream));
@@ -358,7 +366,7 @@ int gbf_split_step(gbf_domain* d) {
     d->mass_count++;
   }
   const GbfSplitConsts C = gbf_split_consts(d->m);
-  int s = gbf_split_launch_domain(d->m, C, G, d->precision == GBF_PREC_SPLIT_DF, mass_out, d->stream, &d->timer,
+  int s = gbf_split_launch_domain(d->m, C, G, gbf_mass_rep(d->precision), mass_out, d->stream, &d->timer,
                                   (const GbfTmaSet*)d->tma, d->cur);
   if (s) return s;
   d->cur = nxt;

@@ -27,8 +27,18 @@ struct GbfSplitConsts {
   // the FP32 rounding of phi
   double m_d[2], dtsrc_m_d[2];
   float2 m_df[2], dtsrc_m_df[2];
+  double ro01b1_d, ro02b2_d;  // rho01 beta1, rho02 beta2 (the defect form's row densities)
 };
 GbfSplitConsts gbf_split_consts(const gbf_model& m);
+
+// How the split forms hold the per-cell phase masses M1, M2: FP64, FP32
+// pairs, or FP32 defects over the mass of the FP32 state at the row's
+// hydrostatic density (4 bytes; gbf_split_tile.cuh).
+enum { kMassF64 = 0, kMassDF = 1, kMassDefect = 2 };
+__host__ __device__ inline int gbf_mass_rep(int precision) {
+  return precision == GBF_PREC_SPLIT_DEFECT ? kMassDefect : precision == GBF_PREC_SPLIT_DF ? kMassDF : kMassF64;
+}
+__host__ __device__ inline int gbf_mass_bytes(int mr) { return mr == kMassDefect ? 4 : 8; }
 
 // Arrays of one grid's split-precision step.
 struct GbfSplitGrid {
@@ -39,7 +49,7 @@ struct GbfSplitGrid {
   const float* K;   // NULL: media table
   const float* phi;
   const int* media;
-  double* M1;       // FP64, or float2 pairs in the same 8 bytes
+  double* M1;       // FP64, float2 pairs in the same 8 bytes, or FP32 defects (4 bytes)
   double* M2;
   double* mass_partials;  // NULL: no phase-mass sums
   unsigned* status;
@@ -56,9 +66,9 @@ int gbf_split_state_to_f64(const gbf_model& m, const float* dPf, const float* Sf
                            cudaStream_t st);
 // FP32 state and wide masses of one grid from FP64 device arrays.
 int gbf_split_init_state(const gbf_model& m, const double* P_dev, const double* S_dev, float* dPf, float* Sf,
-                         double* M1, double* M2, bool df, cudaStream_t st);
+                         double* M1, double* M2, int mr, cudaStream_t st);
 struct GbfTmaSet;
 // `maps` (device memory; boxes of the x-pair tile) selects the x-pair TMA
 // tile for state buffer `buf`; without it the plain-load 32x8 tile runs.
-int gbf_split_launch_domain(const gbf_model& m, const GbfSplitConsts& C, const GbfSplitGrid& G, bool df,
+int gbf_split_launch_domain(const gbf_model& m, const GbfSplitConsts& C, const GbfSplitGrid& G, int mr,
                             double* mass_out, cudaStream_t st, GbfTimer* tm, const GbfTmaSet* maps, int buf);

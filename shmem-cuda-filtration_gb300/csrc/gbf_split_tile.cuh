@@ -4,6 +4,8 @@
 
 #include <math.h>
 
+#include <type_traits>
+
 #include "gbf_split.h"
 #include "gbf_tma.h"
 
@@ -120,6 +122,63 @@ template <> struct Wide<true> {
   }
 };
 
+// ------------------------------------------------- per-cell mass storage
+// M1, M2 of the split forms: the phase masses in the wide type (kMassF64,
+// kMassDF: 8 bytes a cell), or FP32 defects (kMassDefect, 4 bytes). The
+// wide type of a form (constants, the source) is FP64 for kMassF64 and FP32
+// pairs otherwise.
+template <int MR>
+using WideOf = Wide<MR != kMassF64>;
+template <int MR>
+struct MassRep {
+  using T = typename WideOf<MR>::T;
+  static __device__ __forceinline__ T load(const double* p, size_t i) { return WideOf<MR>::load(p, i); }
+  static __device__ __forceinline__ void store(double* p, size_t i, T v) { WideOf<MR>::store(p, i, v); }
+};
+template <>
+struct MassRep<kMassDefect> {
+  using T = float;
+  static __device__ __forceinline__ T load(const double* p, size_t i) { return reinterpret_cast<const float*>(p)[i]; }
+  static __device__ __forceinline__ void store(double* p, size_t i, T v) { reinterpret_cast<float*>(p)[i] = v; }
+};
+// Element type of a mass array in shared memory.
+template <int MR>
+using MassElem = typename std::conditional<MR == kMassDefect, float, double>::type;
+
+// The defect form. A cell's phase masses per pore volume are held as
+//   M1 = c1(j) (1 - S) + D1,   M2 = c2(j) S + D2,
+// with S the cell's FP32 saturation, c_a(j) the hydrostatic density of phase
+// a at row j, rho0a (1 + beta_a j H), rounded to FP32 (so c (1 - S) and c S
+// are exact products), and D1, D2 FP32 "defects": the compressibility part
+// rho0a beta_a dP and the Newton residual, small numbers. The residual of the
+// Newton and the mass update then need FP32 only, with rounding errors
+// relative to those small numbers; e_a is the remainder rho0a (1 + beta_a j H)
+// - c_a (FP32). Both follow from FP64 by fixed roundings, so every kernel
+// derives the same values.
+struct GbfDefectRow {
+  float c1, e1, c2, e2;
+};
+__device__ __forceinline__ GbfDefectRow gbf_defect_row(double ro01, double ro01b1, double ro02, double ro02b2,
+                                                      double H, int j) {
+  const double hs = __dmul_rn((double)j, H);
+  const double r1 = __fma_rn(ro01b1, hs, ro01), r2 = __fma_rn(ro02b2, hs, ro02);
+  GbfDefectRow w;
+  w.c1 = __double2float_rn(r1);
+  w.e1 = __double2float_rn(__dsub_rn(r1, (double)w.c1));
+  w.c2 = __double2float_rn(r2);
+  w.e2 = __double2float_rn(__dsub_rn(r2, (double)w.c2));
+  return w;
+}
+// The same from the model (host-side gbf_split_consts forms ro0 beta and H
+// with the same products).
+__device__ __forceinline__ GbfDefectRow gbf_defect_row(const gbf_model& m, int j) {
+  return gbf_defect_row(m.ro01, __dmul_rn(m.ro01, m.beta1), m.ro02, __dmul_rn(m.ro02, m.beta2),
+                        __dmul_rn(__dmul_rn(m.ro01, m.g), m.h2), j);
+}
+__device__ __forceinline__ GbfDefectRow gbf_defect_row(const GbfSplitConsts& C, int j) {
+  return gbf_defect_row(C.ro01_d, C.ro01b1_d, C.ro02_d, C.ro02b2_d, C.H_d, j);
+}
+
 // ------------------------------------------------------------- tile shape
 // A CTA of TX x TY threads owns a TX x TY column tile (one column per thread).
 // The halo plane (TX + 2 columns, TY + 2 rows) is stored with a row pitch PX
@@ -149,23 +208,26 @@ using GbfSplitPlane = GbfSplitPlaneT<kSplitTX, kSplitTY>;
 // Two rings filled by cp.async.bulk.tensor, one mbarrier per stage:
 //  - halo planes: dP, S, K of one x-y plane of the tile with its 1-cell halo,
 //    up to kTmaStages planes ahead of the plane being built;
-//  - interior rows: M1, M2 (8 bytes a cell) and phi of the plane being
-//    updated, RS - 1 planes ahead (RS = 3 where the static shared memory
-//    of the kernel stays within 48 KB, else 2).
+//  - interior rows: M1, M2 (8 bytes a cell, or 4 in the defect form) and
+//    phi of the plane being updated, RS - 1 planes ahead (RS = 3 where the
+//    static shared memory of the kernel stays within 48 KB, else 2).
 // Every array starts on a 128-byte boundary.
 constexpr int kTmaStages = 3;
-template <int TX, int TY>
+template <int TX, int TY, int MR = kMassF64>
 struct GbfRawRing {
   static constexpr int RS = TX >= 64 ? 2 : 3;
   static constexpr int BX = gbf_tma_box_x(TX), HY = TY + 2, N = BX * HY;
   static constexpr int NP = (N + 31) / 32 * 32;
-  static constexpr int MX = gbf_tma_rows_x8(TX), NM = (MX * TY + 15) / 16 * 16;  // 8-byte elements
-  static constexpr int FX = gbf_tma_box_x(TX), NF = (FX * TY + 31) / 32 * 32;   // FP32 elements
+  static constexpr int FX = gbf_tma_box_x(TX), NF = (FX * TY + 31) / 32 * 32;  // FP32 elements
+  // mass rows: 8-byte elements {TX + 2, TY}, or FP32 ones in phi's box
+  static constexpr int MB = (int)sizeof(MassElem<MR>);
+  static constexpr int MX = MB == 8 ? gbf_tma_rows_x8(TX) : FX;
+  static constexpr int NM = MB == 8 ? (MX * TY + 15) / 16 * 16 : NF;
   // bytes that complete one stage of each ring (whole boxes, also where they overhang the grid)
   static constexpr unsigned kHaloBytes = 3u * N * 4u;
-  static constexpr unsigned kRowsBytes = 2u * MX * TY * 8u + (unsigned)FX * TY * 4u;
+  static constexpr unsigned kRowsBytes = 2u * MX * TY * (unsigned)MB + (unsigned)FX * TY * 4u;
   float v[kTmaStages][3][NP];
-  double m1[RS][NM], m2[RS][NM];
+  MassElem<MR> m1[RS][NM], m2[RS][NM];
   float phi[RS][NF];
   unsigned long long bar[kTmaStages], mbar[RS];
 };
@@ -259,12 +321,52 @@ __device__ __forceinline__ float split_Pk(const GbfSplitConsts& C, int md, float
   return Pk;
 }
 
-template <bool DF>
-struct GbfSplitAcc {
-  typename Wide<DF>::T m1, m2;
+// A thread's sums over its cells: phase masses phi T (for the mass balance),
+// largest CFL numbers, non-finite flag.
+template <int MR>
+struct GbfSplitAcc {  // kMassF64, kMassDF: phi T in the wide type
+  using W = WideOf<MR>;
+  typename W::T m1, m2;
   float cfl1, cfl2;  // largest CFL numbers of the thread's cells (when requested)
   unsigned bad;
-  __device__ GbfSplitAcc() : m1(Wide<DF>::f(0.f)), m2(Wide<DF>::f(0.f)), cfl1(0.f), cfl2(0.f), bad(0) {}
+  __device__ GbfSplitAcc() : m1(W::f(0.f)), m2(W::f(0.f)), cfl1(0.f), cfl2(0.f), bad(0) {}
+  __device__ __forceinline__ void masses(double& a, double& b) const {
+    a = W::tod(m1);
+    b = W::tod(m2);
+  }
+};
+template <>
+struct GbfSplitAcc<kMassDefect> {
+  // sum phi S and sum phi as FP32 pairs, the exact errors of the high-part
+  // additions in the low part: TwoSum (Knuth) for sum phi S, which keeps its
+  // relative precision however small it is (the DNAPL of the first steps);
+  // FastTwoSum (Dekker) for sum phi, its high part started at 1, above every
+  // term (phi < 1). Sum phi D1 and sum phi (D2 + rho02 beta2 P_k S) in FP32
+  // (small terms). c1, c2: the densities of the thread's row (a thread keeps
+  // one row j), which turn the sums into phase masses.
+  float sS, lS, sP, lP, b1, b2, c1, c2;
+  float cfl1, cfl2;
+  unsigned bad;
+  __device__ GbfSplitAcc()
+      : sS(0.f), lS(0.f), sP(1.f), lP(0.f), b1(0.f), b2(0.f), c1(0.f), c2(0.f), cfl1(0.f), cfl2(0.f), bad(0) {}
+  // phi = ph + pl (pl: the low part of a media-table porosity)
+  __device__ __forceinline__ void add(float ph, float pl, float S, float D1, float D2q) {
+    const float p = ph * S, pe = fmaf(pl, S, fmaf(ph, S, -p));
+    float s = sS + p;
+    const float bb = s - sS;
+    lS += ((sS - (s - bb)) + (p - bb)) + pe;
+    sS = s;
+    s = sP + ph;
+    lP += (ph - (s - sP)) + pl;
+    sP = s;
+    b1 = fmaf(ph, D1, b1);
+    b2 = fmaf(ph, D2q, b2);
+  }
+  __device__ __forceinline__ void masses(double& a, double& b) const {
+    const double S = (double)sS + (double)lS, P = ((double)sP - 1.0) + (double)lP;
+    a = (double)c1 * (P - S) + (double)b1;
+    b = (double)c2 * S + (double)b2;
+  }
 };
 
 // ------------------------------------------------------- one cell's update
@@ -278,31 +380,35 @@ struct GbfCellIn {
   float dPp, L1p, L2p;
   float phi;
 };
-template <bool DF>
+template <int MR>
 struct GbfCellOut {
   float dPn, Sn;
-  typename Wide<DF>::T M1n, M2n;
+  typename MassRep<MR>::T M1n, M2n;
 };
 
 // The fused a3 + a4 update of N interior cells of one row and plane
 // (cpu.cpp:218-320 in the split form): donor-cell fluxes, FP32 mass
-// increments, wide mass targets (rate source added exactly), the residual
-// split into its exact large part and FP32 small parts, and the FP32
-// increment Newton. Every operation is applied lane by lane in the same
-// order, so that N = 1 and N = 2 (two cells interleaved for instruction-level
-// parallelism) give each cell the same bits; the rare branches (rate source,
-// second Newton iteration) run for all lanes when any lane needs them and
-// select per lane. Lanes with count[n] false are computed but neither added
-// to the mass sums nor checked for non-finite values.
-template <bool DF, int N, bool CFL = false>
+// increments, mass targets (rate source added exactly), the residual, and the
+// FP32 increment Newton. Wide forms: targets T = M + dm in the wide type, the
+// residual split into its exact large part and FP32 small parts. Defect form:
+// the residual and the new defects from FP32 operations on small numbers
+// (rw: the row's densities). Every operation is applied lane by lane in the
+// same order, so that N = 1 and N = 2 (two cells interleaved for
+// instruction-level parallelism) give each cell the same bits; the rare
+// branches (rate source, second Newton iteration) run for all lanes when any
+// lane needs them and select per lane. Lanes with count[n] false are
+// computed but neither added to the mass sums nor checked for non-finite
+// values.
+template <int MR, int N, bool CFL = false>
 __device__ __forceinline__ void split_cells(const GbfSplitConsts& C, const GbfCellIn (&in)[N],
-                                            const typename Wide<DF>::T (&M1)[N],
-                                            const typename Wide<DF>::T (&M2)[N], typename Wide<DF>::T R01,
-                                            typename Wide<DF>::T R02, int md, const int (&ci)[N], int j, int k,
-                                            bool phi_field, bool mass, const bool (&count)[N],
-                                            GbfSplitAcc<DF>& acc, GbfCellOut<DF> (&o)[N]) {
-  using W = Wide<DF>;
+                                            const typename MassRep<MR>::T (&M1)[N],
+                                            const typename MassRep<MR>::T (&M2)[N], typename WideOf<MR>::T R01,
+                                            typename WideOf<MR>::T R02, const GbfDefectRow& rw, int md,
+                                            const int (&ci)[N], int j, int k, bool phi_field, bool mass,
+                                            const bool (&count)[N], GbfSplitAcc<MR>& acc, GbfCellOut<MR> (&o)[N]) {
+  using W = WideOf<MR>;
   using WT = typename W::T;
+  constexpr bool DEF = MR == kMassDefect;
   const bool noflow = C.noflow_bottom && (j == C.ny - 2);
   float Pp[N], dm1[N], dm2[N];
   WT T1[N], T2[N];
@@ -342,16 +448,18 @@ __device__ __forceinline__ void split_cells(const GbfSplitConsts& C, const GbfCe
       acc.cfl1 = fmaxf(acc.cfl1, c1 * dtphi * C.cfl1);
       acc.cfl2 = fmaxf(acc.cfl2, c2 * dtphi * C.cfl2);
     }
-    // mass targets T = M + dm (wide)
-    T1[n] = W::add_f(M1[n], dm1[n]);
-    T2[n] = W::add_f(M2[n], dm2[n]);
+    if constexpr (!DEF) {  // mass targets T = M + dm (wide)
+      T1[n] = W::add_f(M1[n], dm1[n]);
+      T2[n] = W::add_f(M2[n], dm2[n]);
+    }
   }
-  // the rate source, added exactly
-  float srcf[N];
+  // the rate source, added exactly (defect form: its FP32 high and low parts)
+  float srcf[N], srcl[N];
   bool insrc[N], anysrc = false;
 #pragma unroll
   for (int n = 0; n < N; n++) {
     srcf[n] = 0.f;
+    srcl[n] = 0.f;
     insrc[n] = j == 1 && ci[n] >= C.ri0 && ci[n] < C.ri0 + C.rn && k >= C.rk0 && k < C.rk0 + C.rn;
     anysrc |= insrc[n];
   }
@@ -360,18 +468,28 @@ __device__ __forceinline__ void split_cells(const GbfSplitConsts& C, const GbfCe
     for (int n = 0; n < N; n++) {
       const WT src = phi_field ? W::div_f(W::c(C.dtsrc_d, C.dtsrc_df), in[n].phi)
                                : W::c(C.dtsrc_m_d[md], C.dtsrc_m_df[md]);
-      const WT t2 = W::add(T2[n], src);
-      if (insrc[n]) {
-        T2[n] = t2;
-        srcf[n] = W::tof(src);
+      if constexpr (DEF) {
+        if (insrc[n]) {
+          srcf[n] = src.hi;
+          srcl[n] = src.lo;
+        }
+      } else {
+        const WT t2 = W::add(T2[n], src);
+        if (insrc[n]) {
+          T2[n] = t2;
+          srcf[n] = W::tof(src);
+        }
       }
     }
   }
-  // residual r = F(P, S) - T at the stored state, cpu.cpp:305-306, split
-  // into its large part rho0 (1 - S) - M (wide; the products of FP32
+  // residual r = F(P, S) - T at the stored state, cpu.cpp:305-306. Wide
+  // forms: its large part rho0 (1 - S) - M (wide; the products of FP32
   // numbers are exact) and small FP32 parts rho0 beta P' (..) and dm:
   //   r1 = (rho01 - M1 - rho01 S) + rho01 beta1 P' (1 - S) - dm1
   //   r2 = (rho02 S - M2) + rho02 beta2 (P' + P_k) S - dm2 - src
+  // Defect form (M1 = c1 (1 - S) + D1, M2 = c2 S + D2, c = rho0 (1 + beta j H) - e):
+  //   r1 = (rho01 beta1 dP + e1) (1 - S) - D1 - dm1
+  //   r2 = (rho02 beta2 (dP + P_k) + e2) S - D2 - dm2 - src
   // then the FP32 Newton on d = (dp, ds): r + [F(x + d) - F(x)] = 0, the
   // bracket written in increments so that no large terms cancel. The
   // equations are linear up to terms beta (dp ds, P_k'' ds^2): after the
@@ -383,8 +501,13 @@ __device__ __forceinline__ void split_cells(const GbfSplitConsts& C, const GbfCe
   for (int n = 0; n < N; n++) {
     const float S0 = in[n].S0;
     Pk0[n] = split_Pk(C, md, S0, dPk0[n]);
-    r1[n] = W::rho_1mS_minus(R01, M1[n], S0) + C.ro01b1 * Pp[n] * (1.f - S0) - dm1[n];
-    r2[n] = W::rhoS_minus(R02, M2[n], S0) + C.ro02b2 * (Pp[n] + Pk0[n]) * S0 - dm2[n] - srcf[n];
+    if constexpr (DEF) {
+      r1[n] = fmaf(fmaf(C.ro01b1, in[n].dPc, rw.e1), 1.f - S0, -M1[n]) - dm1[n];
+      r2[n] = fmaf(fmaf(C.ro02b2, in[n].dPc + Pk0[n], rw.e2), S0, -M2[n]) - dm2[n] - srcf[n];
+    } else {
+      r1[n] = W::rho_1mS_minus(R01, M1[n], S0) + C.ro01b1 * Pp[n] * (1.f - S0) - dm1[n];
+      r2[n] = W::rhoS_minus(R02, M2[n], S0) + C.ro02b2 * (Pp[n] + Pk0[n]) * S0 - dm2[n] - srcf[n];
+    }
     a0[n] = fmaf(C.beta1, Pp[n], 1.f);
     b0[n] = fmaf(C.beta2, Pp[n] + Pk0[n], 1.f);
     const float J11 = C.ro01b1 * (1.f - S0), J12 = -C.ro01 * a0[n];
@@ -424,21 +547,41 @@ __device__ __forceinline__ void split_cells(const GbfSplitConsts& C, const GbfCe
   for (int n = 0; n < N; n++) {
     o[n].dPn = in[n].dPc + dp[n];
     o[n].Sn = in[n].S0 + ds[n];
-    o[n].M1n = T1[n];
-    // next step's ro2 S2 is taken at P2 = P1, without P_k (cpu.cpp:63 vs :306)
-    o[n].M2n = W::add_f(T2[n], -C.ro02b2 * Pk[n] * o[n].Sn);
-    if (count[n]) {
-      if (mass) {  // phi T in the wide type (phi exact: an FP32 input or a wide table value)
-        if (phi_field) {
-          acc.m1 = W::acc_phi(acc.m1, in[n].phi, T1[n]);
-          acc.m2 = W::acc_phi(acc.m2, in[n].phi, T2[n]);
-        } else {
-          const WT phw = W::c(C.m_d[md], C.m_df[md]);
-          acc.m1 = W::add(acc.m1, W::mul(phw, T1[n]));
-          acc.m2 = W::add(acc.m2, W::mul(phw, T2[n]));
+    if constexpr (DEF) {
+      // new defects: D1 + dm1 + c1 dS and D2 + dm2 + src - c2 dS - rho02 beta2 P_k S,
+      // with dS the stored change of S and c dS against the increment it
+      // balances inside one FMA (exact product, one rounding of a small sum)
+      const float dse = o[n].Sn - in[n].S0;
+      const float q = C.ro02b2 * Pk[n] * o[n].Sn;  // next step's ro2 S2 is taken without P_k (cpu.cpp:63 vs :306)
+      o[n].M1n = M1[n] + fmaf(rw.c1, dse, dm1[n]);
+      float u = fmaf(-rw.c2, dse, dm2[n]);
+      if (anysrc && insrc[n]) u = fmaf(-rw.c2, dse, srcf[n]) + (dm2[n] + srcl[n]);
+      o[n].M2n = M2[n] + (u - q);
+      if (count[n]) {
+        if (mass) {  // phi T with T1 = c1 (1 - S) + D1, T2 = c2 S + D2 + q
+          const float ph = phi_field ? in[n].phi : C.m_df[md].x;
+          const float pl = phi_field ? 0.f : C.m_df[md].y;
+          acc.add(ph, pl, o[n].Sn, o[n].M1n, o[n].M2n + q);
         }
+        if (!isfinite(o[n].dPn) || !isfinite(o[n].Sn)) acc.bad = 1;
       }
-      if (!isfinite(o[n].dPn) || !isfinite(o[n].Sn)) acc.bad = 1;
+    } else {
+      o[n].M1n = T1[n];
+      // next step's ro2 S2 is taken at P2 = P1, without P_k (cpu.cpp:63 vs :306)
+      o[n].M2n = W::add_f(T2[n], -C.ro02b2 * Pk[n] * o[n].Sn);
+      if (count[n]) {
+        if (mass) {  // phi T in the wide type (phi exact: an FP32 input or a wide table value)
+          if (phi_field) {
+            acc.m1 = W::acc_phi(acc.m1, in[n].phi, T1[n]);
+            acc.m2 = W::acc_phi(acc.m2, in[n].phi, T2[n]);
+          } else {
+            const WT phw = W::c(C.m_d[md], C.m_df[md]);
+            acc.m1 = W::add(acc.m1, W::mul(phw, T1[n]));
+            acc.m2 = W::add(acc.m2, W::mul(phw, T2[n]));
+          }
+        }
+        if (!isfinite(o[n].dPn) || !isfinite(o[n].Sn)) acc.bad = 1;
+      }
     }
   }
 }
@@ -452,19 +595,20 @@ __device__ __forceinline__ void split_cells(const GbfSplitConsts& C, const GbfCe
 // call returns false if a bounded wait gave up (the status word then carries
 // GBF_DEV_TIMEOUT). `phases` holds the barrier parities across calls.
 // TMA = false: plain loads, one plane prefetched in registers, two buffers.
-template <bool DF, int TX = kSplitTX, int TY = kSplitTY, bool TMA = false, bool CFL = false>
+template <int MR, int TX = kSplitTX, int TY = kSplitTY, bool TMA = false, bool CFL = false>
 __device__ bool split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i0, int j0, int k0, int k1,
-                           GbfSplitPlaneT<TX, TY, gbf_plane_pitch<TX, TMA>()>* pl, GbfSplitAcc<DF>& acc,
-                           GbfRawRing<TX, TY>* raw = nullptr, const GbfTmaSet* maps = nullptr, int buf = 0,
+                           GbfSplitPlaneT<TX, TY, gbf_plane_pitch<TX, TMA>()>* pl, GbfSplitAcc<MR>& acc,
+                           GbfRawRing<TX, TY, MR>* raw = nullptr, const GbfTmaSet* maps = nullptr, int buf = 0,
                            unsigned* phases = nullptr) {
-  using W = Wide<DF>;
+  using W = WideOf<MR>;
   using WT = typename W::T;
+  using MT = typename MassRep<MR>::T;
   constexpr int PX = gbf_plane_pitch<TX, TMA>();
   using Sh = GbfSplitShape<TX, TY, PX>;
   constexpr int kSplitTX = TX, kSplitThreads = Sh::threads, kSplitHX = Sh::HX, kSplitHN = Sh::HN,
                 kSplitSlots = Sh::slots;
   using GbfSplitPlane = GbfSplitPlaneT<TX, TY, PX>;
-  static_assert(!TMA || PX == GbfRawRing<TX, TY>::BX, "TMA plane pitch equals the box width");
+  static_assert(!TMA || PX == GbfRawRing<TX, TY, MR>::BX, "TMA plane pitch equals the box width");
   const int nx = C.nx, ny = C.ny, nz = C.nz;
   const unsigned pln = (unsigned)nx * (unsigned)ny;  // grids hold < 2^32 cells (checked on the host)
   const int tx = threadIdx.x % kSplitTX, ty = threadIdx.x / kSplitTX;
@@ -526,7 +670,7 @@ __device__ bool split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i
   // tracks the stages in flight (`pend`: bits 0.. halo ring, bits 8.. rows
   // ring) and the barrier parities (`*phases`, same bit layout), so that a
   // give-up can wait out the copies still in flight.
-  using Ring = GbfRawRing<TX, TY>;
+  using Ring = GbfRawRing<TX, TY, MR>;
   constexpr int RS = Ring::RS;
   unsigned pend = 0;
   int h_issue = 0, r_issue = 0;  // next stage to fill, halo and rows rings
@@ -625,6 +769,11 @@ __device__ bool split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i
   int cur = 0;                             // plain loads: buffer of plane k
   int t_cur = 0, t_next = 1, t_rows = 0;   // TMA: buffer/halo stage of planes k, k + 1; rows stage of plane k
   const WT R01 = W::c(C.ro01_d, C.ro01_df), R02 = W::c(C.ro02_d, C.ro02_df);
+  const GbfDefectRow rw = MR == kMassDefect ? gbf_defect_row(C, j) : GbfDefectRow{};
+  if constexpr (MR == kMassDefect) {
+    acc.c1 = rw.c1;
+    acc.c2 = rw.c2;
+  }
   const int mi = ty * Ring::MX + tx + 1, fi = ty * Ring::FX + tx + 1;  // own cell in the rows boxes
   for (int k = k0; k < k1; k++) {
     if constexpr (TMA) {
@@ -654,8 +803,10 @@ __device__ bool split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i
       const unsigned c = (unsigned)(i + j * nx) + (unsigned)k * pln;
       const int md = (!TMA && G.media) ? __ldg(G.media + c) : 0;
       const float phi = TMA ? raw->phi[sr][fi] : (G.phi ? __ldg(G.phi + c) : C.m[md]);
-      const WT M1 = TMA ? W::load(raw->m1[sr], mi) : W::load(G.M1, c);
-      const WT M2 = TMA ? W::load(raw->m2[sr], mi) : W::load(G.M2, c);
+      const MT M1 = TMA ? MassRep<MR>::load(reinterpret_cast<const double*>(raw->m1[sr]), mi)
+                        : MassRep<MR>::load(G.M1, c);
+      const MT M2 = TMA ? MassRep<MR>::load(reinterpret_cast<const double*>(raw->m2[sr]), mi)
+                        : MassRep<MR>::load(G.M2, c);
       GbfCellIn in;
       in.dPc = Pc.dP[hc]; in.S0 = Pc.S[hc]; in.L1c = Pc.L1[hc]; in.L2c = Pc.L2[hc];
       in.dPxm = Pc.dP[hc - 1]; in.dPxp = Pc.dP[hc + 1];
@@ -666,16 +817,16 @@ __device__ bool split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i
       in.dPp = Pn.dP[hc]; in.L1p = Pn.L1[hc]; in.L2p = Pn.L2[hc];
       in.phi = phi;
       const GbfCellIn ins[1] = {in};
-      const WT m1s[1] = {M1}, m2s[1] = {M2};
+      const MT m1s[1] = {M1}, m2s[1] = {M2};
       const int cis[1] = {i};
       const bool cnt[1] = {true};
-      GbfCellOut<DF> os[1];
-      split_cells<DF, 1, CFL>(C, ins, m1s, m2s, R01, R02, md, cis, j, k, G.phi != nullptr,
+      GbfCellOut<MR> os[1];
+      split_cells<MR, 1, CFL>(C, ins, m1s, m2s, R01, R02, rw, md, cis, j, k, G.phi != nullptr,
                               G.mass_partials != nullptr, cnt, acc, os);
       G.dPn[c] = os[0].dPn;
       G.Sn[c] = os[0].Sn;
-      W::store(G.M1, c, os[0].M1n);
-      W::store(G.M2, c, os[0].M2n);
+      MassRep<MR>::store(G.M1, c, os[0].M1n);
+      MassRep<MR>::store(G.M2, c, os[0].M2n);
       dPm = in.dPc;
       L1m = in.L1c;
       L2m = in.L2c;
@@ -694,14 +845,19 @@ __device__ bool split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i
 
 // Split state of one cell from FP64 P, S: dP = P - P_hs(j), S in FP32 and
 // the phase masses ro1 (1 - S2), ro2 S2 with P2 = P1 (cpu.cpp:72-73, 224-225)
-// in the wide type of `df`.
+// in the representation `mr` (defect form: minus c1 (1 - S), c2 S of the
+// FP32 S, products that are exact in FP64).
 __device__ __forceinline__ void gbf_split_init_cell(const gbf_model& m, double p, double s, int j, float& dPf,
-                                                    float& Sf, double* M1, double* M2, size_t c, bool df) {
+                                                    float& Sf, double* M1, double* M2, size_t c, int mr) {
   dPf = (float)(p - gbf_p_hydrostatic(m, j));
   Sf = (float)s;
   const double m1 = m.ro01 * (1. + m.beta1 * (p - m.P_atm)) * (1. - s);
   const double m2 = m.ro02 * (1. + m.beta2 * (p - m.P_atm)) * s;
-  if (df) {
+  if (mr == kMassDefect) {
+    const GbfDefectRow w = gbf_defect_row(m, j);
+    reinterpret_cast<float*>(M1)[c] = (float)(m1 - (double)w.c1 * (1. - (double)Sf));
+    reinterpret_cast<float*>(M2)[c] = (float)(m2 - (double)w.c2 * (double)Sf);
+  } else if (mr == kMassDF) {
     reinterpret_cast<float2*>(M1)[c] = gbf_df_from_double(m1);
     reinterpret_cast<float2*>(M2)[c] = gbf_df_from_double(m2);
   } else {
@@ -775,10 +931,11 @@ __device__ __forceinline__ void split_block_cfl(float c1, float c2, float* out) 
 }
 
 // Deterministic block reduction of the phase-mass partial sums (FP64).
-template <bool DF, int NT = kSplitThreads>
-__device__ __forceinline__ void split_block_mass(const GbfSplitAcc<DF>& acc, double V, double* out2) {
+template <int MR, int NT = kSplitThreads>
+__device__ __forceinline__ void split_block_mass(const GbfSplitAcc<MR>& acc, double V, double* out2) {
   __shared__ double red[2][NT / 32];
-  double a = Wide<DF>::tod(acc.m1), b = Wide<DF>::tod(acc.m2);
+  double a, b;
+  acc.masses(a, b);
   for (int o = 16; o > 0; o >>= 1) {
     a += __shfl_down_sync(0xffffffffu, a, o);
     b += __shfl_down_sync(0xffffffffu, b, o);
@@ -804,31 +961,38 @@ __device__ __forceinline__ void split_block_mass(const GbfSplitAcc<DF>& acc, dou
 // The interior rows of M1, M2 and phi arrive as {TXC, TY} boxes at x0 (no
 // halo). Shared memory exceeds the static 48 KB, so the kernel takes it as
 // dynamic shared memory (GbfPairSmem).
-template <int TXC, int TY>
+template <int TXC, int TY, int MR = kMassF64>
 struct GbfPairRing {
   static_assert(TXC % 32 == 0 && TXC <= 248, "x-pair tile width");
   static constexpr int BX = TXC + 8, HY = TY + 2, N = BX * HY, NP = (N + 31) / 32 * 32;
   static constexpr int NR = TXC * TY;  // interior-row elements per field
   static constexpr int RS = 3;
+  static constexpr unsigned MB = (unsigned)sizeof(MassElem<MR>);
   static constexpr unsigned kHaloBytes = 3u * N * 4u;
-  static constexpr unsigned kRowsBytes = (unsigned)NR * (8u + 8u + 4u);
+  static constexpr unsigned kRowsBytes = (unsigned)NR * (MB + MB + 4u);
   float v[kTmaStages][3][NP];
-  double m1[RS][NR], m2[RS][NR];
+  MassElem<MR> m1[RS][NR], m2[RS][NR];
   float phi[RS][NR];
   unsigned long long bar[kTmaStages], mbar[RS];
 };
-template <int TXC, int TY>
+template <int TXC, int TY, int MR = kMassF64>
 struct GbfPairSmem {
-  GbfPairRing<TXC, TY> ring;
-  float dP[kTmaStages][GbfPairRing<TXC, TY>::NP], S[kTmaStages][GbfPairRing<TXC, TY>::NP];
-  float L1[kTmaStages][GbfPairRing<TXC, TY>::NP], L2[kTmaStages][GbfPairRing<TXC, TY>::NP];
+  using Ring = GbfPairRing<TXC, TY, MR>;
+  Ring ring;
+  float dP[kTmaStages][Ring::NP], S[kTmaStages][Ring::NP];
+  float L1[kTmaStages][Ring::NP], L2[kTmaStages][Ring::NP];
 };
 
 __device__ __forceinline__ float2 gbf_ld2(const float* p) { return *reinterpret_cast<const float2*>(p); }
 __device__ __forceinline__ void gbf_st2(float* p, float a, float b) { *reinterpret_cast<float2*>(p) = make_float2(a, b); }
 
-template <bool DF> struct WidePair;
-template <> struct WidePair<false> {  // FP64 masses: two doubles
+// Address of cell c of a mass array (8 or 4 bytes a cell), as the array's nominal type.
+template <int MR>
+__device__ __forceinline__ double* mass_at(double* p, size_t c) {
+  return reinterpret_cast<double*>(reinterpret_cast<MassElem<MR>*>(p) + c);
+}
+template <int MR> struct WidePair;
+template <> struct WidePair<kMassF64> {  // FP64 masses: two doubles
   static __device__ __forceinline__ void load(const double* p, double& a, double& b) {
     const double2 v = *reinterpret_cast<const double2*>(p);
     a = v.x;
@@ -838,7 +1002,7 @@ template <> struct WidePair<false> {  // FP64 masses: two doubles
     *reinterpret_cast<double2*>(p) = make_double2(a, b);
   }
 };
-template <> struct WidePair<true> {  // FP32-pair masses: four floats
+template <> struct WidePair<kMassDF> {  // FP32-pair masses: four floats
   static __device__ __forceinline__ void load(const double* p, GbfDF& a, GbfDF& b) {
     const float4 v = *reinterpret_cast<const float4*>(p);
     a = {v.x, v.y};
@@ -848,22 +1012,33 @@ template <> struct WidePair<true> {  // FP32-pair masses: four floats
     *reinterpret_cast<float4*>(p) = make_float4(a.hi, a.lo, b.hi, b.lo);
   }
 };
+template <> struct WidePair<kMassDefect> {  // FP32 defects: two floats
+  static __device__ __forceinline__ void load(const double* p, float& a, float& b) {
+    const float2 v = *reinterpret_cast<const float2*>(p);
+    a = v.x;
+    b = v.y;
+  }
+  static __device__ __forceinline__ void store(double* p, float a, float b) {
+    *reinterpret_cast<float2*>(p) = make_float2(a, b);
+  }
+};
 
 // The x-pair z-marching tile: cells x0 .. x0 + TXC - 1 (interior ones only)
 // of rows j0 .. j0 + TY - 1, planes k0 .. k1 - 1. Same staging protocol,
 // bounded waits and give-up as split_tile<..., TMA = true>; each cell is
 // updated by split_cell, so results equal the other tiles' bit for bit.
-template <bool DF, int TXC, int TY, bool CFL = false>
+template <int MR, int TXC, int TY, bool CFL = false>
 __device__ bool split_tile_x2(const GbfSplitConsts& C, const GbfSplitGrid& G, int x0, int j0, int k0, int k1,
-                              GbfPairSmem<TXC, TY>& sm, GbfSplitAcc<DF>& acc, const GbfTmaSet* maps, int buf,
+                              GbfPairSmem<TXC, TY, MR>& sm, GbfSplitAcc<MR>& acc, const GbfTmaSet* maps, int buf,
                               unsigned* phases) {
-  using W = Wide<DF>;
+  using W = WideOf<MR>;
   using WT = typename W::T;
-  using Ring = GbfPairRing<TXC, TY>;
+  using MT = typename MassRep<MR>::T;
+  using Ring = GbfPairRing<TXC, TY, MR>;
   constexpr int THX = TXC / 2, NT = THX * TY, BX = Ring::BX, HY = Ring::HY, RS = Ring::RS;
   constexpr int PCOLS = (TXC + 4) / 2;  // pair columns 1 .. PCOLS of the box (columns 2 .. TXC + 5)
   constexpr int NPAIR = PCOLS * HY, SLOTS = (NPAIR + NT - 1) / NT;
-  GbfPairRing<TXC, TY>& raw = sm.ring;
+  Ring& raw = sm.ring;
   const int nx = C.nx, ny = C.ny;
   const unsigned pln = (unsigned)nx * (unsigned)ny;
   const int tx = threadIdx.x % THX, ty = threadIdx.x / THX;
@@ -970,6 +1145,11 @@ __device__ bool split_tile_x2(const GbfSplitConsts& C, const GbfSplitGrid& G, in
     if (k0 + kTmaStages <= k1) issue(k0 + kTmaStages);
   }
   const WT R01 = W::c(C.ro01_d, C.ro01_df), R02 = W::c(C.ro02_d, C.ro02_df);
+  const GbfDefectRow rw = MR == kMassDefect ? gbf_defect_row(C, j) : GbfDefectRow{};
+  if constexpr (MR == kMassDefect) {
+    acc.c1 = rw.c1;
+    acc.c2 = rw.c2;
+  }
   int t_cur = 0, t_next = 1, t_rows = 0;
   for (int k = k0; k < k1; k++) {
     {
@@ -998,9 +1178,9 @@ __device__ bool split_tile_x2(const GbfSplitConsts& C, const GbfSplitGrid& G, in
       const float2 dp = gbf_ld2(sm.dP[t_next] + hc), ap = gbf_ld2(sm.L1[t_next] + hc),
                    bp = gbf_ld2(sm.L2[t_next] + hc);
       const float2 ph = gbf_ld2(&raw.phi[t_rows][mi]);
-      WT M1a, M1b, M2a, M2b;
-      WidePair<DF>::load(&raw.m1[t_rows][mi], M1a, M1b);
-      WidePair<DF>::load(&raw.m2[t_rows][mi], M2a, M2b);
+      MT M1a, M1b, M2a, M2b;
+      WidePair<MR>::load(reinterpret_cast<const double*>(&raw.m1[t_rows][mi]), M1a, M1b);
+      WidePair<MR>::load(reinterpret_cast<const double*>(&raw.m2[t_rows][mi]), M2a, M2b);
       GbfCellIn in[2];
       // cell a
       in[0].dPc = d0.x; in[0].S0 = s0.x; in[0].L1c = a0.x; in[0].L2c = b0.x;
@@ -1018,24 +1198,24 @@ __device__ bool split_tile_x2(const GbfSplitConsts& C, const GbfSplitGrid& G, in
       in[1].dPm = dPmb; in[1].L1m = L1mb; in[1].L2m = L2mb;
       in[1].dPp = dp.y; in[1].L1p = ap.y; in[1].L2p = bp.y;
       in[1].phi = ph.y;
-      const WT m1s[2] = {M1a, M1b}, m2s[2] = {M2a, M2b};
+      const MT m1s[2] = {M1a, M1b}, m2s[2] = {M2a, M2b};
       const int cis[2] = {ia, ia + 1};
       const bool cnt[2] = {act_a, act_b};
-      GbfCellOut<DF> o[2];
-      split_cells<DF, 2, CFL>(C, in, m1s, m2s, R01, R02, 0, cis, j, k, true, G.mass_partials != nullptr, cnt,
+      GbfCellOut<MR> o[2];
+      split_cells<MR, 2, CFL>(C, in, m1s, m2s, R01, R02, rw, 0, cis, j, k, true, G.mass_partials != nullptr, cnt,
                               acc, o);
       // The x faces i = 0 and i = nx - 1 (rows and planes interior) take the
       // boundary rules' values here: the new S of the x-neighbour and its dP
       // (cpu.cpp:327-331, 366-372), or the hydrostatic side value dP = 0 with
       // GBF_BC_HYDROSTATIC_SIDES; no other boundary rule reads these cells, so
       // the face pass skips them (gbf_boundary_count_no_xfaces).
-      const GbfCellOut<DF> oa = act_a ? o[0] : GbfCellOut<DF>{C.noflow_bottom ? 0.f : o[1].dPn, o[1].Sn, M1a, M2a};
-      const GbfCellOut<DF> ob = act_b ? o[1] : GbfCellOut<DF>{C.noflow_bottom ? 0.f : o[0].dPn, o[0].Sn, M1b, M2b};
+      const GbfCellOut<MR> oa = act_a ? o[0] : GbfCellOut<MR>{C.noflow_bottom ? 0.f : o[1].dPn, o[1].Sn, M1a, M2a};
+      const GbfCellOut<MR> ob = act_b ? o[1] : GbfCellOut<MR>{C.noflow_bottom ? 0.f : o[0].dPn, o[0].Sn, M1b, M2b};
       const unsigned c = (unsigned)(ia + j * nx) + (unsigned)k * pln;  // even: nx and ia are
       gbf_st2(G.dPn + c, oa.dPn, ob.dPn);
       gbf_st2(G.Sn + c, oa.Sn, ob.Sn);
-      WidePair<DF>::store(G.M1 + c, oa.M1n, ob.M1n);
-      WidePair<DF>::store(G.M2 + c, oa.M2n, ob.M2n);
+      WidePair<MR>::store(mass_at<MR>(G.M1, c), oa.M1n, ob.M1n);
+      WidePair<MR>::store(mass_at<MR>(G.M2, c), oa.M2n, ob.M2n);
       dPma = d0.x; L1ma = a0.x; L2ma = b0.x;
       dPmb = d0.y; L1mb = a0.y; L2mb = b0.y;
     }

@@ -51,7 +51,7 @@ def cfl_reference(m, P, S, K, phi):
     return out
 
 
-@pytest.mark.parametrize("form", ["split", "split_df"])
+@pytest.mark.parametrize("form", ["split", "split_df", "split_defect"])
 def test_cfl_matches_definition(gpu_lib, abi, O, oracle, pkg, form):
     from importlib import import_module
     Domain = import_module(pkg.__name__ + ".domain").Domain
@@ -59,7 +59,7 @@ def test_cfl_matches_definition(gpu_lib, abi, O, oracle, pkg, form):
     m.S_wr[:] = [0.1, 0.1]
     oracle.initial(st)
     st["S2"][3:12, 2:9, 6:16] = 0.3  # a DNAPL blob, so that both phases are mobile
-    p = abi.GBF_PREC_SPLIT if form == "split" else abi.GBF_PREC_SPLIT_DF
+    p = {"split": abi.GBF_PREC_SPLIT, "split_df": abi.GBF_PREC_SPLIT_DF, "split_defect": abi.GBF_PREC_SPLIT_DEFECT}[form]
     steps = 12
     dom = Domain(m, None, st.K, st.phi, precision=p)
     assert gpu_lib.gbf_domain_uses_tma(dom.h) == 1

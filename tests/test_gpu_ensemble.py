@@ -8,7 +8,7 @@ from dataclasses import dataclass
 import numpy as np
 import pytest
 
-from gpu_util import p_tol
+from gpu_util import p_tol, mass_order_rtol
 
 pytestmark = pytest.mark.gpu
 
@@ -70,11 +70,12 @@ def mods(pkg):
     return import_module(pkg.__name__ + ".ensemble"), import_module(pkg.__name__ + ".domain")
 
 
-PRECS = ["f64", "split", "split_df"]
+PRECS = ["f64", "split", "split_df", "split_defect"]
 
 
 def prec(abi, name):
-    return {"split": abi.GBF_PREC_SPLIT, "split_df": abi.GBF_PREC_SPLIT_DF, "f64": abi.GBF_PREC_F64}[name]
+    return {"split": abi.GBF_PREC_SPLIT, "split_df": abi.GBF_PREC_SPLIT_DF, "split_defect": abi.GBF_PREC_SPLIT_DEFECT,
+            "f64": abi.GBF_PREC_F64}[name]
 
 
 @pytest.mark.parametrize("p", PRECS)
@@ -105,7 +106,7 @@ def test_ensemble_members_equal_single_domains(gpu_lib, abi, pkg, p):
         for r, (P, S, mh) in enumerate(single):
             assert np.array_equal(ens.download(r, "S2"), S), (shape, r)
             assert np.array_equal(ens.download(r, "P1"), P), (shape, r)
-            np.testing.assert_allclose(mass[:, r, :], mh, rtol=1e-12, atol=0)
+            np.testing.assert_allclose(mass[:, r, :], mh, rtol=mass_order_rtol(p, 1e-12), atol=0)
         ens.close()
 
 
@@ -179,7 +180,7 @@ def test_ensemble_autotune(gpu_lib, abi, pkg):
     ref.close()
 
 
-@pytest.mark.parametrize("p", ["split", "split_df"])
+@pytest.mark.parametrize("p", ["split", "split_df", "split_defect"])
 def test_ensemble_tma_staging_equals_plain_loads(gpu_lib, abi, pkg, p):
     """Persistent ensemble kernel with TMA plane staging (barrier parities
     carried from tile to tile) against plain loads, every tile shape, with a

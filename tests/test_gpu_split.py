@@ -11,17 +11,18 @@ its total carries FP32 rounding (bound 1e-6 there).
 import numpy as np
 import pytest
 
-from gpu_util import rel_l2
+from gpu_util import mass_order_rtol, rel_l2
 from test_gpu_f64 import make_case
 
 pytestmark = pytest.mark.gpu
 
-SPLITS = ["split", "split_df"]
+SPLITS = ["split", "split_df", "split_defect"]
 DS_TOL = 1e-5
 
 
 def prec(abi, name):
-    return {"split": abi.GBF_PREC_SPLIT, "split_df": abi.GBF_PREC_SPLIT_DF, "f64": abi.GBF_PREC_F64}[name]
+    return {"split": abi.GBF_PREC_SPLIT, "split_df": abi.GBF_PREC_SPLIT_DF, "split_defect": abi.GBF_PREC_SPLIT_DEFECT,
+            "f64": abi.GBF_PREC_F64}[name]
 
 
 def domain_cls(pkg):
@@ -142,8 +143,8 @@ def test_tma_staging_equals_plain_loads(gpu_lib, abi, O, oracle, pkg, form):
     finally:
         gpu_lib.gbf_set_tma(prev)
     assert np.array_equal(out[1][0], out[0][0]) and np.array_equal(out[1][1], out[0][1])  # P, S
-    # phase masses: wide per-thread sums; the x-pair tile adds its two cells per plane in turn
-    np.testing.assert_allclose(out[1][2], out[0][2], rtol=1e-13, atol=0)
+    # phase masses: per-thread sums; the x-pair tile adds its two cells per plane in turn
+    np.testing.assert_allclose(out[1][2], out[0][2], rtol=mass_order_rtol(form, 1e-13), atol=0)
 
 
 def test_pinned_transfers_equal_staged(gpu_lib, abi, O, oracle, pkg):
