@@ -69,6 +69,7 @@ __device__ __forceinline__ float* ens_cfl_slot(const EnsCfl& cfl, int member) {
 template <int MR, int TX, int TY, bool TMA, bool CFL>
 __global__ void __launch_bounds__(TX * TY, 1024 / (TX * TY)) k_ens_split_step(const EnsMember* __restrict__ mem,
                                                                              const int4* __restrict__ tiles,
+                                                                             const int* __restrict__ order,
                                                                              int ntiles, int cur,
                                                                              unsigned* counter, double* partials,
                                                                              unsigned* status,
@@ -96,7 +97,8 @@ __global__ void __launch_bounds__(TX * TY, 1024 / (TX * TY)) k_ens_split_step(co
     __syncthreads();
     const int t = s_tile;
     if (t >= ntiles) break;
-    const int4 tl = tiles[t];
+    const int ti = order ? order[t] : t;  // list index (mass-partial slot)
+    const int4 tl = tiles[ti];
     const EnsMember* me = mem + tl.x;
     {  // member constants to shared memory
       const int* src = reinterpret_cast<const int*>(&me->C);
@@ -123,7 +125,7 @@ __global__ void __launch_bounds__(TX * TY, 1024 / (TX * TY)) k_ens_split_step(co
                                                 TMA ? maps + tl.x : nullptr, cur, &phases);
     if (!ok) break;  // a plane wait gave up (status set); the whole CTA stops
     if (acc.bad) atomicOr(status, GBF_DEV_NONFINITE);
-    if (partials) split_block_mass<MR, NT>(acc, Cs.V, partials + 2 * t);
+    if (partials) split_block_mass<MR, NT>(acc, Cs.V, partials + 2 * ti);
     if constexpr (CFL)
       if (Gs.cfl_out) split_block_cfl<NT>(acc.cfl1, acc.cfl2, Gs.cfl_out);
     __syncthreads();
@@ -132,8 +134,9 @@ __global__ void __launch_bounds__(TX * TY, 1024 / (TX * TY)) k_ens_split_step(co
 
 template <int MR, int TXC, int TY, bool CFL>
 __global__ void __launch_bounds__(TXC / 2 * TY, 512 / (TXC / 2 * TY)) k_ens_split_step_x2(
-    const EnsMember* __restrict__ mem, const int4* __restrict__ tiles, int ntiles, int cur, unsigned* counter,
-    double* partials, unsigned* status, const GbfTmaSet* __restrict__ maps, const EnsCfl cfl) {
+    const EnsMember* __restrict__ mem, const int4* __restrict__ tiles, const int* __restrict__ order, int ntiles,
+    int cur, unsigned* counter, double* partials, unsigned* status, const GbfTmaSet* __restrict__ maps,
+    const EnsCfl cfl) {
   extern __shared__ __align__(128) unsigned char dyn[];
   using Smem = GbfPairSmem<TXC, TY, MR>;
   Smem& sm = *reinterpret_cast<Smem*>(dyn);
@@ -157,7 +160,8 @@ __global__ void __launch_bounds__(TXC / 2 * TY, 512 / (TXC / 2 * TY)) k_ens_spli
     __syncthreads();
     const int t = s_tile;
     if (t >= ntiles) break;
-    const int4 tl = tiles[t];
+    const int ti = order ? order[t] : t;  // list index (mass-partial slot)
+    const int4 tl = tiles[ti];
     const EnsMember* me = mem + tl.x;
     {
       const int* src = reinterpret_cast<const int*>(&me->C);
@@ -184,7 +188,7 @@ __global__ void __launch_bounds__(TXC / 2 * TY, 512 / (TXC / 2 * TY)) k_ens_spli
                                                maps + tl.x, cur, &phases);
     if (!ok) break;
     if (acc.bad) atomicOr(status, GBF_DEV_NONFINITE);
-    if (partials) split_block_mass<MR, NT>(acc, Cs.V, partials + 2 * t);
+    if (partials) split_block_mass<MR, NT>(acc, Cs.V, partials + 2 * ti);
     if constexpr (CFL)
       if (Gs.cfl_out) split_block_cfl<NT>(acc.cfl1, acc.cfl2, Gs.cfl_out);
     __syncthreads();
@@ -365,6 +369,7 @@ struct gbf_ensemble {
   EnsMember* d_mem = nullptr;
   std::vector<int4> tiles;
   int4* d_tiles = nullptr;
+  int* d_order = nullptr;  // whole-ensemble processing order of the tiles: longest k ranges first
   std::vector<EnsChunk> props, flux, bnd, all;
   EnsChunk *d_props = nullptr, *d_flux = nullptr, *d_bnd = nullptr, *d_all = nullptr;
   double* d_stage = nullptr;  // packed FP64 P, S of all members (whole-ensemble transfers)
@@ -496,6 +501,13 @@ int build_lists(gbf_ensemble* e) {
   if (split) {
     s |= upload((void**)&e->d_tiles, e->tiles.data(), e->tiles.size() * sizeof(int4));
     e->nparts = (int)e->tiles.size();
+    // longest-processing-time-first order for the whole-ensemble step: the
+    // persistent CTAs end on the short tiles, which shortens the tail
+    std::vector<int> order(e->tiles.size());
+    for (size_t q = 0; q < order.size(); q++) order[q] = (int)q;
+    auto planes = [&](int q) { return (e->tiles[q].w >> 16) - (e->tiles[q].w & 0xffff); };
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return planes(a) > planes(b); });
+    s |= upload((void**)&e->d_order, order.data(), order.size() * sizeof(int));
   } else {
     s |= upload((void**)&e->d_props, e->props.data(), e->props.size() * sizeof(EnsChunk));
     s |= upload((void**)&e->d_flux, e->flux.data(), e->flux.size() * sizeof(EnsChunk));
@@ -557,6 +569,7 @@ int build_lists(gbf_ensemble* e) {
 struct TileRange {
   int t0, nt, cur;
   unsigned* counter;
+  const int* order;  // processing order of tiles [0, nt) (absolute indices; t0 = 0), or NULL: list order
 };
 
 EnsCfl ens_cfl(const gbf_ensemble* e) {
@@ -573,7 +586,7 @@ int launch_split_step_t(gbf_ensemble* e, double* partials, cudaStream_t st, cons
   GBF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TX * TY, 0));
   const int blocks = std::max(1, std::min(tr.nt, per_sm * gbf_num_sms()));
   e->persistent_blocks = blocks;
-  kern<<<blocks, TX * TY, 0, st>>>(e->d_mem, e->d_tiles + tr.t0, tr.nt, tr.cur, tr.counter,
+  kern<<<blocks, TX * TY, 0, st>>>(e->d_mem, e->d_tiles + tr.t0, tr.order, tr.nt, tr.cur, tr.counter,
                                     partials ? partials + 2 * (size_t)tr.t0 : nullptr, e->d_status, e->d_maps,
                                     ens_cfl(e));
   return GBF_OK;
@@ -589,7 +602,7 @@ int launch_split_step_x2(gbf_ensemble* e, double* partials, cudaStream_t st, con
   GBF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TXC / 2 * TY, bytes));
   const int blocks = std::max(1, std::min(tr.nt, std::max(1, per_sm) * gbf_num_sms()));
   e->persistent_blocks = blocks;
-  kern<<<blocks, TXC / 2 * TY, bytes, st>>>(e->d_mem, e->d_tiles + tr.t0, tr.nt, tr.cur, tr.counter,
+  kern<<<blocks, TXC / 2 * TY, bytes, st>>>(e->d_mem, e->d_tiles + tr.t0, tr.order, tr.nt, tr.cur, tr.counter,
                                              partials ? partials + 2 * (size_t)tr.t0 : nullptr, e->d_status,
                                              e->d_maps, ens_cfl(e));
   return GBF_OK;
@@ -622,7 +635,8 @@ int enqueue_step(gbf_ensemble* e, cudaStream_t st) {
   if (e->precision != GBF_PREC_F64) {
     GBF_CUDA(cudaMemsetAsync(e->d_counter, 0, sizeof(unsigned), st));
     ev = gbf_timer_begin(tm, st);
-    if (int s = launch_split_step(e, partials, st, {0, (int)e->tiles.size(), e->cur, e->d_counter})) return s;
+    if (int s = launch_split_step(e, partials, st, {0, (int)e->tiles.size(), e->cur, e->d_counter, e->d_order}))
+      return s;
     gbf_timer_end(tm, GBF_K_ENS_STEP, ev, st);
     ev = gbf_timer_begin(tm, st);
     k_ens_split_boundary<<<(unsigned)e->bnd.size(), kThreads, 0, st>>>(e->d_mem, e->d_bnd, e->cur);
@@ -685,7 +699,7 @@ int enqueue_group_step(gbf_ensemble* e, int r0, int r1, int cur, unsigned* count
   const auto &a = e->starts[r0], &b = e->starts[r1];
   if (e->precision != GBF_PREC_F64) {
     GBF_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned), st));
-    if (int s = launch_split_step(e, nullptr, st, {a.tiles, b.tiles - a.tiles, cur, counter})) return s;
+    if (int s = launch_split_step(e, nullptr, st, {a.tiles, b.tiles - a.tiles, cur, counter, nullptr})) return s;
     k_ens_split_boundary<<<(unsigned)(b.bnd - a.bnd), kThreads, 0, st>>>(e->d_mem, e->d_bnd + a.bnd, cur);
   } else {
     k_ens_f64_props<<<(unsigned)(b.props - a.props), kThreads, 0, st>>>(e->d_mem, e->d_props + a.props, cur);

@@ -189,27 +189,39 @@ __global__ void k_split_to_f64(const gbf_model m, const float* dPf, const float*
 
 }  // namespace
 
-// k planes per CTA: enough CTAs to fill the GPU several times over, long
-// enough runs that the one-plane prologue stays small.
-int gbf_split_kchunk(const GbfSplitConsts& C) {
-  const long long tiles = (long long)tiles_x(C) * tiles_y(C);
-  const long long want = 6LL * gbf_num_sms();
-  int chunks = (int)((want + tiles - 1) / tiles);
-  if (chunks < 1) chunks = 1;
-  int kchunk = (C.nz - 2 + chunks - 1) / chunks;
-  if (kchunk < 16) kchunk = 16;
-  return kchunk;
+// k planes per CTA of a grid of `tiles` column tiles and `nzi` interior
+// planes, run with `slots` CTAs resident at a time: the CTAs run in waves,
+// and the last wave of an uneven count leaves slots idle. Among k ranges of
+// at least 16 planes (or the whole column), take the one with the fewest
+// plane-times: waves x (planes per CTA + about 1.5 for the prologue, which
+// builds the first plane and loads the plane below it). Grids that fill
+// less than one wave may go down to 8 planes per CTA.
+int gbf_split_kchunk_waves(long long tiles, int nzi, long long slots) {
+  if (nzi < 1) return 1;
+  if (slots < 1) slots = 1;
+  const int max_chunks = (nzi + 7) / 8;
+  int best = nzi;
+  double best_cost = 1e300;
+  for (int chunks = 1; chunks <= max_chunks; chunks++) {
+    const int kc = (nzi + chunks - 1) / chunks;
+    const long long ctas = tiles * ((nzi + kc - 1) / kc);
+    if (chunks > 1 && kc < 16 && (kc < 8 || ctas > slots)) continue;
+    const double cost = (double)((ctas + slots - 1) / slots) * (kc + 1.5);
+    if (cost < best_cost - 1e-9) {
+      best_cost = cost;
+      best = kc;
+    }
+  }
+  return best;
 }
 
-// k planes per x-pair CTA, by the same rule.
+// Resident CTAs per SM of the two single-grid tiles (launch bounds and shared memory: the 32x8
+// plain-load tile 4, the x-pair tile 2).
+int gbf_split_kchunk(const GbfSplitConsts& C) {
+  return gbf_split_kchunk_waves((long long)tiles_x(C) * tiles_y(C), C.nz - 2, 4LL * gbf_num_sms());
+}
 int gbf_split_kchunk_x2(const GbfSplitConsts& C) {
-  const long long tiles = (long long)tiles_x2(C) * tiles_y2(C);
-  const long long want = 3LL * gbf_num_sms();  // two CTAs per SM
-  int chunks = (int)((want + tiles - 1) / tiles);
-  if (chunks < 1) chunks = 1;
-  int kchunk = (C.nz - 2 + chunks - 1) / chunks;
-  if (kchunk < 16) kchunk = 16;
-  return kchunk;
+  return gbf_split_kchunk_waves((long long)tiles_x2(C) * tiles_y2(C), C.nz - 2, 2LL * gbf_num_sms());
 }
 
 template <int MR, bool CFL>
