@@ -44,11 +44,14 @@ struct EnsChunk {
   unsigned begin, end;
 };
 
-// Tile shapes (cells in x by rows); the last one is the x-pair TMA tile
-// (split_tile_x2: two cells per thread, TMA staging only).
-enum { kShape32x8 = 0, kShape64x4 = 1, kShape32x4 = 2, kShape64x8x2 = 3, kShapes = 4 };
-const int kShapeTX[kShapes] = {32, 64, 32, 64}, kShapeTY[kShapes] = {8, 4, 4, 8};
-const bool kShapePairs[kShapes] = {false, false, false, true};
+// Tile shapes (cells in x by rows); the last two are x-pair TMA tiles
+// (split_tile_x2: two cells per thread, TMA staging only). 64x8 and 32x16
+// pairs have the same shared memory (halo boxes {72, 10} and {40, 18}: 720
+// elements each); the narrower one covers grids whose nx - 1 is just above a
+// multiple of 64 with fewer idle lanes, and has the smaller halo (1.27x).
+enum { kShape32x8 = 0, kShape64x4 = 1, kShape32x4 = 2, kShape64x8x2 = 3, kShape32x16x2 = 4, kShapes = 5 };
+const int kShapeTX[kShapes] = {32, 64, 32, 64, 32}, kShapeTY[kShapes] = {8, 4, 4, 8, 16};
+const bool kShapePairs[kShapes] = {false, false, false, true, true};
 constexpr int kChunkCells = 16384, kBoundaryChunk = 4096, kThreads = 256;
 
 // ------------------------------------------------------------ split kernels
@@ -612,6 +615,7 @@ template <int MR>
 int launch_split_form(gbf_ensemble* e, double* partials, cudaStream_t st, const TileRange& tr) {
   switch (e->shape) {
     case kShape64x8x2: return launch_split_step_x2<MR, 64, 8>(e, partials, st, tr);
+    case kShape32x16x2: return launch_split_step_x2<MR, 32, 16>(e, partials, st, tr);
     case kShape64x4: return launch_split_step_t<MR, 64, 4>(e, partials, st, tr);
     case kShape32x4: return launch_split_step_t<MR, 32, 4>(e, partials, st, tr);
     default: return launch_split_step_t<MR, 32, 8>(e, partials, st, tr);
@@ -1127,7 +1131,7 @@ int gbf_ensemble_get_tuning(gbf_ensemble* e, int* shape, int* edges, int* kchunk
 }
 
 const char* gbf_ensemble_shape_name(int shape) {
-  static const char* names[kShapes] = {"32x8", "64x4", "32x4", "64x8 pairs"};
+  static const char* names[kShapes] = {"32x8", "64x4", "32x4", "64x8 pairs", "32x16 pairs"};
   return (shape >= 0 && shape < kShapes) ? names[shape] : "";
 }
 

@@ -91,7 +91,7 @@ def test_ensemble_members_equal_single_domains(gpu_lib, abi, pkg, p):
         d.step(steps)
         single.append((d.download("P1"), d.download("S2"), d.mass_history(steps)))
         d.close()
-    shapes = [0] if p == "f64" else [0, 1, 2, 3]  # 3: two cells per thread (TMA staging)
+    shapes = [0] if p == "f64" else [0, 1, 2, 3, 4]  # 3, 4: two cells per thread (TMA staging)
     for shape in shapes:
         ens = E.Ensemble(mems, precision=prec(abi, p))
         if p != "f64":
@@ -190,13 +190,13 @@ def test_ensemble_tma_staging_equals_plain_loads(gpu_lib, abi, pkg, p):
     steps = 12
     prev = gpu_lib.gbf_set_tma(-1)
     try:
-        for shape in (0, 1, 2, 3):
+        for shape in (0, 1, 2, 3, 4):
             res = {}
             for tma in (1, 0):
                 gpu_lib.gbf_set_tma(tma)
                 ens = E.Ensemble(mems, precision=prec(abi, p))
-                if shape == 3 and not tma:  # the x-pair tile has no plain-load form
-                    assert gpu_lib.gbf_ensemble_set_tuning(ens.h, 3, 0, 0) == abi.GBF_ERR_ARG
+                if shape in (3, 4) and not tma:  # the x-pair tiles have no plain-load form
+                    assert gpu_lib.gbf_ensemble_set_tuning(ens.h, shape, 0, 0) == abi.GBF_ERR_ARG
                     gpu_lib.gbf_clear_status()
                     ens.set_tuning(0, 0, 0)
                 else:
@@ -309,9 +309,10 @@ def test_ensemble_without_tma_refuses_pair_tile(gpu_lib, abi, pkg):
     mems.append(Mem(m, K, phi))
     ens = E.Ensemble(mems, precision=abi.GBF_PREC_SPLIT_DF)
     assert gpu_lib.gbf_ensemble_uses_tma(ens.h) == 0
-    assert gpu_lib.gbf_ensemble_set_tuning(ens.h, 3, 0, 0) == abi.GBF_ERR_ARG
-    gpu_lib.gbf_clear_status()
-    assert ens.autotune(1)["tile"] != "64x8 pairs"
+    for shape in (3, 4):
+        assert gpu_lib.gbf_ensemble_set_tuning(ens.h, shape, 0, 0) == abi.GBF_ERR_ARG
+        gpu_lib.gbf_clear_status()
+    assert "pairs" not in ens.autotune(1)["tile"]
     ens.upload_initial()
     ens.step(6)
     assert ens.status() == abi.GBF_OK
