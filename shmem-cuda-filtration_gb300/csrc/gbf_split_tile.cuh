@@ -299,18 +299,17 @@ __device__ __forceinline__ void split_props(const GbfSplitConsts& C, int md, flo
   L2 = K * kr2 * C.nmr2 * fmaf(C.beta2, Pp, 1.f);
 }
 
-// Upwinded flux through one face: the potential x times the mobility of the
-// cell the flow comes from, L_pos for x >= 0 and L_neg otherwise — the
-// reference's ((x + |x|) L_pos + (x - |x|) L_neg) / 2 (cpu.cpp:260-262). In x
-// and z both phases share the potential (P2 = P1), and so the comparison.
-// Donor-cell flux difference of one direction: in through face 1 (from the
-// minus side, a rounded product), out through face 2 (fused into the
-// difference). The rounding is fixed explicitly: two cells of one thread
-// share a face, and a compiler free to merge the two products in one tile
-// shape and not in another would give the shapes different bits.
-__device__ __forceinline__ float split_donor(float x1, float x2, float Lc, float Lm, float Lp) {
-  const float in1 = __fmul_rn(x1, x1 >= 0.f ? Lm : Lc);
-  return fmaf(-x2, x2 >= 0.f ? Lc : Lp, in1);
+// Upwinded flux through one face: the potential x (from the minus to the
+// plus side) times the mobility of the cell the flow comes from, L_minus for
+// x >= 0 and L_plus otherwise — the reference's ((x + |x|) L_minus + (x - |x|)
+// L_plus) / 2 (cpu.cpp:260-262) — as one rounded product. A face's flux is
+// then one value whichever of its two cells computes it: the two cells of a
+// thread's pair share their middle x face, and the flux through the face
+// above a plane is carried to the next plane as the flux through the face
+// below it. In x and z both phases share the potential (P2 = P1), and so the
+// comparison.
+__device__ __forceinline__ float split_face(float x, float Lminus, float Lplus) {
+  return __fmul_rn(x, x >= 0.f ? Lminus : Lplus);
 }
 
 // Brooks-Corey capillary pressure P_d S_e^(-1/lambda) and its S-derivative (cpu.cpp:303-308).
@@ -371,12 +370,13 @@ struct GbfSplitAcc<kMassDefect> {
 
 // ------------------------------------------------------- one cell's update
 // Inputs of one cell at plane k: the cell, its x and y neighbours (y = the
-// vertical j), and its column at planes k - 1 and k + 1.
+// vertical j), its column at plane k + 1, and both phases' fluxes through its
+// face towards plane k - 1 (the previous plane's out-fluxes, split_face).
 struct GbfCellIn {
   float dPc, S0, L1c, L2c;
   float dPxm, dPxp, dPym, dPyp;
   float L1xm, L1xp, L1ym, L1yp, L2xm, L2xp, L2ym, L2yp;
-  float dPm, L1m, L2m;
+  float fz1, fz2;
   float dPp, L1p, L2p;
   float phi;
 };
@@ -384,7 +384,16 @@ template <int MR>
 struct GbfCellOut {
   float dPn, Sn;
   typename MassRep<MR>::T M1n, M2n;
+  float fz1, fz2;  // fluxes through the face towards plane k + 1 (the next plane's fz1, fz2)
 };
+// Both phases' fluxes through the z face between a column's cells at planes
+// k - 1 (dPm, L1m, L2m) and k: the carry a tile starts its first plane with.
+__device__ __forceinline__ void split_zface(const GbfSplitConsts& C, float dPm, float L1m, float L2m, float dPc,
+                                            float L1c, float L2c, float& fz1, float& fz2) {
+  const float z = (dPm - dPc) * C.inv_h3;
+  fz1 = split_face(z, L1m, L1c);
+  fz2 = split_face(z, L2m, L2c);
+}
 
 // The fused a3 + a4 update of N interior cells of one row and plane
 // (cpu.cpp:218-320 in the split form): donor-cell fluxes, FP32 mass
@@ -419,18 +428,23 @@ __device__ __forceinline__ void split_cells(const GbfSplitConsts& C, const GbfCe
     const float x1 = (in[n].dPxm - dPc) * C.inv_h1, x2 = (dPc - in[n].dPxp) * C.inv_h1;
     const float yb1 = (in[n].dPym - dPc) * C.inv_h2;
     const float yb2 = (dPc - in[n].dPyp) * C.inv_h2;
-    const float z1 = (in[n].dPm - dPc) * C.inv_h3, z2 = (dPc - in[n].dPp) * C.inv_h3;
+    const float z2 = (dPc - in[n].dPp) * C.inv_h3;
     Pp[n] = fmaf((float)j, C.H, dPc);  // P - P_atm
     const float gd1 = C.g_ro01_b1 * Pp[n];  // (rho1 - rho01) g
     const float gd2 = fmaf(C.g_ro02_b2, Pp[n], C.g_dro);
     const float y11 = yb1 + gd1, y21 = noflow ? 0.f : yb2 + gd1;
     const float y12 = yb1 + gd2, y22 = noflow ? 0.f : yb2 + gd2;
-    const float f = split_donor(x1, x2, L1c, in[n].L1xm, in[n].L1xp) * C.inv_h1 +
-                    C.kv * split_donor(y11, y21, L1c, in[n].L1ym, in[n].L1yp) * C.inv_h2 +
-                    split_donor(z1, z2, L1c, in[n].L1m, in[n].L1p) * C.inv_h3;
-    const float gs = split_donor(x1, x2, L2c, in[n].L2xm, in[n].L2xp) * C.inv_h1 +
-                     C.kv * split_donor(y12, y22, L2c, in[n].L2ym, in[n].L2yp) * C.inv_h2 +
-                     split_donor(z1, z2, L2c, in[n].L2m, in[n].L2p) * C.inv_h3;
+    // face fluxes, in through the minus face and out through the plus face
+    const float ax1 = split_face(x1, in[n].L1xm, L1c), ax2 = split_face(x2, L1c, in[n].L1xp);
+    const float ay1 = split_face(y11, in[n].L1ym, L1c), ay2 = split_face(y21, L1c, in[n].L1yp);
+    const float az1 = in[n].fz1, az2 = split_face(z2, L1c, in[n].L1p);
+    const float bx1 = split_face(x1, in[n].L2xm, L2c), bx2 = split_face(x2, L2c, in[n].L2xp);
+    const float by1 = split_face(y12, in[n].L2ym, L2c), by2 = split_face(y22, L2c, in[n].L2yp);
+    const float bz1 = in[n].fz2, bz2 = split_face(z2, L2c, in[n].L2p);
+    o[n].fz1 = az2;
+    o[n].fz2 = bz2;
+    const float f = (ax1 - ax2) * C.inv_h1 + C.kv * (ay1 - ay2) * C.inv_h2 + (az1 - az2) * C.inv_h3;
+    const float gs = (bx1 - bx2) * C.inv_h1 + C.kv * (by1 - by2) * C.inv_h2 + (bz1 - bz2) * C.inv_h3;
     const float dtphi = __fdividef(C.dt, in[n].phi);
     dm1[n] = -dtphi * f;  // FP32 mass increments
     dm2[n] = -dtphi * gs;
@@ -438,13 +452,10 @@ __device__ __forceinline__ void split_cells(const GbfSplitConsts& C, const GbfCe
       // CFL number of each phase: the largest face volumetric flux of the cell
       // (mass flux x L_upwind over the reference density) times dt / (phi h)
       // (the mobilities L are <= 0: magnitudes by fabsf)
-      auto face = [](float x, float Lpos, float Lneg) { return fabsf(x * (x >= 0.f ? Lpos : Lneg)); };
-      const float c1 = fmaxf(fmaxf(fmaxf(face(x1, in[n].L1xm, L1c), face(x2, L1c, in[n].L1xp)) * C.inv_h1,
-                                   C.kv * fmaxf(face(y11, in[n].L1ym, L1c), face(y21, L1c, in[n].L1yp)) * C.inv_h2),
-                             fmaxf(face(z1, in[n].L1m, L1c), face(z2, L1c, in[n].L1p)) * C.inv_h3);
-      const float c2 = fmaxf(fmaxf(fmaxf(face(x1, in[n].L2xm, L2c), face(x2, L2c, in[n].L2xp)) * C.inv_h1,
-                                   C.kv * fmaxf(face(y12, in[n].L2ym, L2c), face(y22, L2c, in[n].L2yp)) * C.inv_h2),
-                             fmaxf(face(z1, in[n].L2m, L2c), face(z2, L2c, in[n].L2p)) * C.inv_h3);
+      const float c1 = fmaxf(fmaxf(fmaxf(fabsf(ax1), fabsf(ax2)) * C.inv_h1, C.kv * fmaxf(fabsf(ay1), fabsf(ay2)) * C.inv_h2),
+                             fmaxf(fabsf(az1), fabsf(az2)) * C.inv_h3);
+      const float c2 = fmaxf(fmaxf(fmaxf(fabsf(bx1), fabsf(bx2)) * C.inv_h1, C.kv * fmaxf(fabsf(by1), fabsf(by2)) * C.inv_h2),
+                             fmaxf(fabsf(bz1), fabsf(bz2)) * C.inv_h3);
       acc.cfl1 = fmaxf(acc.cfl1, c1 * dtphi * C.cfl1);
       acc.cfl2 = fmaxf(acc.cfl2, c2 * dtphi * C.cfl2);
     }
@@ -766,6 +777,9 @@ __device__ bool split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i
     fetch(k0 + 1);
     __syncthreads();
   }
+  // flux carry: both phases through the face between planes k0 - 1 and k0
+  float fz1 = 0.f, fz2 = 0.f;
+  if (active) split_zface(C, dPm, L1m, L2m, pl[0].dP[hc], pl[0].L1[hc], pl[0].L2[hc], fz1, fz2);
   int cur = 0;                             // plain loads: buffer of plane k
   int t_cur = 0, t_next = 1, t_rows = 0;   // TMA: buffer/halo stage of planes k, k + 1; rows stage of plane k
   const WT R01 = W::c(C.ro01_d, C.ro01_df), R02 = W::c(C.ro02_d, C.ro02_df);
@@ -813,7 +827,7 @@ __device__ bool split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i
       in.dPym = Pc.dP[hc - kSplitHX]; in.dPyp = Pc.dP[hc + kSplitHX];
       in.L1xm = Pc.L1[hc - 1]; in.L1xp = Pc.L1[hc + 1]; in.L1ym = Pc.L1[hc - kSplitHX]; in.L1yp = Pc.L1[hc + kSplitHX];
       in.L2xm = Pc.L2[hc - 1]; in.L2xp = Pc.L2[hc + 1]; in.L2ym = Pc.L2[hc - kSplitHX]; in.L2yp = Pc.L2[hc + kSplitHX];
-      in.dPm = dPm; in.L1m = L1m; in.L2m = L2m;
+      in.fz1 = fz1; in.fz2 = fz2;
       in.dPp = Pn.dP[hc]; in.L1p = Pn.L1[hc]; in.L2p = Pn.L2[hc];
       in.phi = phi;
       const GbfCellIn ins[1] = {in};
@@ -827,9 +841,8 @@ __device__ bool split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i
       G.Sn[c] = os[0].Sn;
       MassRep<MR>::store(G.M1, c, os[0].M1n);
       MassRep<MR>::store(G.M2, c, os[0].M2n);
-      dPm = in.dPc;
-      L1m = in.L1c;
-      L2m = in.L2c;
+      fz1 = os[0].fz1;
+      fz2 = os[0].fz2;
     }
     if constexpr (!TMA) {
       __syncthreads();
@@ -1144,6 +1157,13 @@ __device__ bool split_tile_x2(const GbfSplitConsts& C, const GbfSplitGrid& G, in
     }
     if (k0 + kTmaStages <= k1) issue(k0 + kTmaStages);
   }
+  // flux carry of both cells: the faces between planes k0 - 1 and k0
+  float fza1 = 0.f, fza2 = 0.f, fzb1 = 0.f, fzb2 = 0.f;
+  if (any) {
+    const float2 d = gbf_ld2(sm.dP[0] + hc), a = gbf_ld2(sm.L1[0] + hc), b = gbf_ld2(sm.L2[0] + hc);
+    split_zface(C, dPma, L1ma, L2ma, d.x, a.x, b.x, fza1, fza2);
+    split_zface(C, dPmb, L1mb, L2mb, d.y, a.y, b.y, fzb1, fzb2);
+  }
   const WT R01 = W::c(C.ro01_d, C.ro01_df), R02 = W::c(C.ro02_d, C.ro02_df);
   const GbfDefectRow rw = MR == kMassDefect ? gbf_defect_row(C, j) : GbfDefectRow{};
   if constexpr (MR == kMassDefect) {
@@ -1187,7 +1207,7 @@ __device__ bool split_tile_x2(const GbfSplitConsts& C, const GbfSplitGrid& G, in
       in[0].dPxm = dl.y; in[0].dPxp = d0.y; in[0].dPym = du.x; in[0].dPyp = dd.x;
       in[0].L1xm = al.y; in[0].L1xp = a0.y; in[0].L1ym = au.x; in[0].L1yp = ad.x;
       in[0].L2xm = bl.y; in[0].L2xp = b0.y; in[0].L2ym = bu.x; in[0].L2yp = bd.x;
-      in[0].dPm = dPma; in[0].L1m = L1ma; in[0].L2m = L2ma;
+      in[0].fz1 = fza1; in[0].fz2 = fza2;
       in[0].dPp = dp.x; in[0].L1p = ap.x; in[0].L2p = bp.x;
       in[0].phi = ph.x;
       // cell b
@@ -1195,7 +1215,7 @@ __device__ bool split_tile_x2(const GbfSplitConsts& C, const GbfSplitGrid& G, in
       in[1].dPxm = d0.x; in[1].dPxp = dr.x; in[1].dPym = du.y; in[1].dPyp = dd.y;
       in[1].L1xm = a0.x; in[1].L1xp = ar.x; in[1].L1ym = au.y; in[1].L1yp = ad.y;
       in[1].L2xm = b0.x; in[1].L2xp = br.x; in[1].L2ym = bu.y; in[1].L2yp = bd.y;
-      in[1].dPm = dPmb; in[1].L1m = L1mb; in[1].L2m = L2mb;
+      in[1].fz1 = fzb1; in[1].fz2 = fzb2;
       in[1].dPp = dp.y; in[1].L1p = ap.y; in[1].L2p = bp.y;
       in[1].phi = ph.y;
       const MT m1s[2] = {M1a, M1b}, m2s[2] = {M2a, M2b};
@@ -1216,8 +1236,8 @@ __device__ bool split_tile_x2(const GbfSplitConsts& C, const GbfSplitGrid& G, in
       gbf_st2(G.Sn + c, oa.Sn, ob.Sn);
       WidePair<MR>::store(mass_at<MR>(G.M1, c), oa.M1n, ob.M1n);
       WidePair<MR>::store(mass_at<MR>(G.M2, c), oa.M2n, ob.M2n);
-      dPma = d0.x; L1ma = a0.x; L2ma = b0.x;
-      dPmb = d0.y; L1mb = a0.y; L2mb = b0.y;
+      fza1 = o[0].fz1; fza2 = o[0].fz2;
+      fzb1 = o[1].fz1; fzb2 = o[1].fz2;
     }
     t_cur = t_next;
     t_next = t_next == kTmaStages - 1 ? 0 : t_next + 1;
