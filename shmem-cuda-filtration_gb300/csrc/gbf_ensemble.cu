@@ -136,7 +136,7 @@ __global__ void __launch_bounds__(TX * TY, 1024 / (TX * TY)) k_ens_split_step(co
 }
 
 template <int MR, int TXC, int TY, bool CFL>
-__global__ void __launch_bounds__(TXC / 2 * TY, 512 / (TXC / 2 * TY)) k_ens_split_step_x2(
+__global__ void __launch_bounds__(TXC / 2 * TY, gbf_pair_ctas(MR) * 256 / (TXC / 2 * TY)) k_ens_split_step_x2(
     const EnsMember* __restrict__ mem, const int4* __restrict__ tiles, const int* __restrict__ order, int ntiles,
     int cur, unsigned* counter, double* partials, unsigned* status, const GbfTmaSet* __restrict__ maps,
     const EnsCfl cfl) {

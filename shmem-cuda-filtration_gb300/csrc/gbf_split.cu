@@ -111,7 +111,7 @@ __global__ void __launch_bounds__(kSplitThreads, 4) k_split_step(const GbfSplitC
 
 // The x-pair tile on one grid: one tile (64 x 8 cells, a k range) per CTA.
 template <int MR, bool CFL>
-__global__ void __launch_bounds__(kPairTX / 2 * kPairTY, 2) k_split_step_x2(const GbfSplitConsts C,
+__global__ void __launch_bounds__(kPairTX / 2 * kPairTY, gbf_pair_ctas(MR)) k_split_step_x2(const GbfSplitConsts C,
                                                                          const GbfSplitGrid G, const int kchunk,
                                                                          const GbfTmaSet* maps, int buf) {
   extern __shared__ __align__(128) unsigned char dyn[];
@@ -216,18 +216,19 @@ int gbf_split_kchunk_waves(long long tiles, int nzi, long long slots) {
 }
 
 // Resident CTAs per SM of the two single-grid tiles (launch bounds and shared memory: the 32x8
-// plain-load tile 4, the x-pair tile 2).
+// plain-load tile 4, the x-pair tile gbf_pair_ctas: 3 in the defect form, else 2).
 int gbf_split_kchunk(const GbfSplitConsts& C) {
   return gbf_split_kchunk_waves((long long)tiles_x(C) * tiles_y(C), C.nz - 2, 4LL * gbf_num_sms());
 }
-int gbf_split_kchunk_x2(const GbfSplitConsts& C) {
-  return gbf_split_kchunk_waves((long long)tiles_x2(C) * tiles_y2(C), C.nz - 2, 2LL * gbf_num_sms());
+int gbf_split_kchunk_x2(const GbfSplitConsts& C, int mr) {
+  return gbf_split_kchunk_waves((long long)tiles_x2(C) * tiles_y2(C), C.nz - 2,
+                                (long long)gbf_pair_ctas(mr) * gbf_num_sms());
 }
 
 template <int MR, bool CFL>
 int launch_x2(const GbfSplitConsts& C, const GbfSplitGrid& G, const GbfTmaSet* maps, int buf, cudaStream_t st,
               unsigned& blocks) {
-  const int kchunk = gbf_split_kchunk_x2(C);
+  const int kchunk = gbf_split_kchunk_x2(C, MR);
   blocks = (unsigned)(tiles_x2(C) * tiles_y2(C) * ((C.nz - 2 + kchunk - 1) / kchunk));
   const int bytes = (int)sizeof(GbfPairSmem<kPairTX, kPairTY, MR>);
   GBF_CUDA(cudaFuncSetAttribute(k_split_step_x2<MR, CFL>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
@@ -271,9 +272,9 @@ int gbf_split_launch_domain(const gbf_model& m, const GbfSplitConsts& C, const G
 }
 
 // Mass-partial slots: the larger of the two tilings' CTA counts.
-unsigned gbf_split_blocks(const gbf_model& m) {
+unsigned gbf_split_blocks(const gbf_model& m, int mr) {
   const GbfSplitConsts C = gbf_split_consts(m);
-  const int kchunk = gbf_split_kchunk(C), kc2 = gbf_split_kchunk_x2(C);
+  const int kchunk = gbf_split_kchunk(C), kc2 = gbf_split_kchunk_x2(C, mr);
   const unsigned a = (unsigned)(tiles_x(C) * tiles_y(C) * ((C.nz - 2 + kchunk - 1) / kchunk));
   const unsigned b = (unsigned)(tiles_x2(C) * tiles_y2(C) * ((C.nz - 2 + kc2 - 1) / kc2));
   return a > b ? a : b;
@@ -293,7 +294,7 @@ int gbf_split_alloc(gbf_domain* d) {
   if (!s) s |= gbf_domain_alloc(d, (void**)&d->M1, n * mb);
   if (!s) s |= gbf_domain_alloc(d, (void**)&d->M2, n * mb);
   // per-block mass partials of the split step kernel
-  if (!s) s |= gbf_domain_alloc(d, (void**)&d->split_partials, 2 * sizeof(double) * gbf_split_blocks(d->m));
+  if (!s) s |= gbf_domain_alloc(d, (void**)&d->split_partials, 2 * sizeof(double) * gbf_split_blocks(d->m, gbf_mass_rep(d->precision)));
   if (s) return GBF_ERR_NOMEM;
   // TMA plane loads: FP32 K and phi fields, no media table, rows of whole 16-byte units
   const gbf_model& m = d->m;

@@ -974,12 +974,17 @@ __device__ __forceinline__ void split_block_mass(const GbfSplitAcc<MR>& acc, dou
 // The interior rows of M1, M2 and phi arrive as {TXC, TY} boxes at x0 (no
 // halo). Shared memory exceeds the static 48 KB, so the kernel takes it as
 // dynamic shared memory (GbfPairSmem).
+// Resident 256-thread x-pair CTAs per SM: three for the defect form (80
+// registers a thread, a 2-stage rows ring: 74 KB of shared memory), two for
+// the wide forms (116-120 registers, 3 stages).
+__host__ __device__ constexpr int gbf_pair_ctas(int MR) { return MR == kMassDefect ? 3 : 2; }
+
 template <int TXC, int TY, int MR = kMassF64>
 struct GbfPairRing {
   static_assert(TXC % 32 == 0 && TXC <= 248, "x-pair tile width");
   static constexpr int BX = TXC + 8, HY = TY + 2, N = BX * HY, NP = (N + 31) / 32 * 32;
   static constexpr int NR = TXC * TY;  // interior-row elements per field
-  static constexpr int RS = 3;
+  static constexpr int RS = gbf_pair_ctas(MR) == 3 ? 2 : 3;
   static constexpr unsigned MB = (unsigned)sizeof(MassElem<MR>);
   static constexpr unsigned kHaloBytes = 3u * N * 4u;
   static constexpr unsigned kRowsBytes = (unsigned)NR * (MB + MB + 4u);
