@@ -1069,7 +1069,10 @@ __device__ bool split_tile_x2(const GbfSplitConsts& C, const GbfSplitGrid& G, in
   const int mi = ty * TXC + 2 * tx;           // own pair in the rows boxes (even)
 
   // halo pairs of this thread: even plane index, global row (rows or columns
-  // outside the grid hold zeros and give finite, unused properties)
+  // outside the grid hold zeros and give finite, unused properties). The
+  // interior pairs of a row go to consecutive threads (a row's THX pairs are
+  // contiguous in shared memory: no bank conflicts), then the left and right
+  // halo pair of every row.
   int hq[SLOTS], hj[SLOTS];
 #pragma unroll
   for (int s = 0; s < SLOTS; s++) {
@@ -1077,7 +1080,15 @@ __device__ bool split_tile_x2(const GbfSplitConsts& C, const GbfSplitGrid& G, in
     hq[s] = -1;
     hj[s] = 0;
     if (q < NPAIR) {
-      const int r = q / PCOLS, c2 = 1 + q % PCOLS;
+      int r, c2;
+      if (q < HY * THX) {
+        r = q / THX;
+        c2 = 2 + q % THX;
+      } else {
+        const int h = q - HY * THX;
+        r = h >> 1;
+        c2 = (h & 1) ? PCOLS : 1;
+      }
       hq[s] = r * BX + 2 * c2;
       hj[s] = j0 - 1 + r;
     }
