@@ -31,18 +31,10 @@ GbfSplitConsts gbf_split_consts(const gbf_model& m) {
     C.rk0 = m.nz / 2 - m.rate_cells / 2;
     src = m.rate / (double)(m.rate_cells * m.rate_cells) / V;
   }
-  C.inv_h1 = (float)(1.0 / m.h1); C.inv_h2 = (float)(1.0 / m.h2); C.inv_h3 = (float)(1.0 / m.h3);
-  C.kv = (float)m.kv;
-  C.dt = (float)m.dt;
   const double H = m.ro01 * m.g * m.h2;
   C.H = (float)H;
   C.ro01 = (float)m.ro01; C.ro02 = (float)m.ro02; C.beta1 = (float)m.beta1; C.beta2 = (float)m.beta2;
   C.cfl1 = (float)(1.0 / m.ro01); C.cfl2 = (float)(1.0 / m.ro02);
-  C.g_ro01_b1 = (float)(m.g * m.ro01 * m.beta1);
-  C.g_ro02_b2 = (float)(m.g * m.ro02 * m.beta2);
-  C.g_dro = (float)(m.g * (m.ro02 - m.ro01));
-  C.neg_inv_mu1 = (float)(-1.0 / m.mu1);
-  C.neg_inv_mu2 = (float)(-1.0 / m.mu2);
   C.nmr1 = (float)(-m.ro01 / m.mu1);
   C.nmr2 = (float)(-m.ro02 / m.mu2);
   C.ro01b1 = (float)(m.ro01 * m.beta1);
@@ -51,9 +43,6 @@ GbfSplitConsts gbf_split_consts(const gbf_model& m) {
     const double lam = m.lambda[md], swr = m.S_wr[md];
     C.K[md] = (float)m.K[md];
     C.m[md] = (float)m.m[md];
-    C.swr[md] = (float)swr;
-    C.inv_1mswr[md] = (float)(1.0 / (1.0 - swr));
-    C.se_a[md] = 1.0f;  // (1 - S_wr) / (1 - S_wr)
     C.se_b[md] = (float)(-1.0 / (1.0 - swr));
     C.e1[md] = (float)((2. + 3. * lam) / lam);
     C.e2[md] = (float)((2. + lam) / lam);
@@ -66,6 +55,12 @@ GbfSplitConsts gbf_split_consts(const gbf_model& m) {
   C.V = V;
   C.ro01b1_d = m.ro01 * m.beta1;
   C.ro02b2_d = m.ro02 * m.beta2;
+  C.gh1 = (float)(m.g * m.ro01 * m.beta1 * m.h2);
+  C.gh2 = (float)(m.g * m.ro02 * m.beta2 * m.h2);
+  C.ghd = (float)(m.g * (m.ro02 - m.ro01) * m.h2);
+  C.wx = (float)(m.dt / (m.h1 * m.h1));
+  C.wy = (float)(m.dt * m.kv / (m.h2 * m.h2));
+  C.wz = (float)(m.dt / (m.h3 * m.h3));
   C.H_df = gbf_df_from_double(H);
   C.beta1_df = gbf_df_from_double(m.beta1);
   C.beta2_df = gbf_df_from_double(m.beta2);

@@ -10,16 +10,19 @@ struct GbfSplitConsts {
   int nx, ny, nz;
   int noflow_bottom;  // GBF_BC_HYDROSTATIC_SIDES: no-flow bottom face and hydrostatic P on the i and k sides
   int ri0, rk0, rn;  // rate-injection patch on the j = 1 layer (rn = 0: none)
-  float inv_h1, inv_h2, inv_h3, kv, dt;
   float H;  // rho01 g h2: hydrostatic pressure step per cell (main.cpp:114)
+  // Face potentials are kept as pressure differences (times h): their
+  // gravity terms g rho01 beta1 h2, g rho02 beta2 h2, g (rho02 - rho01) h2,
+  // and the flux-difference weights dt / h1^2, dt kv / h2^2, dt / h3^2 that
+  // turn the upwinded face products into mass increments (times 1 / phi).
+  float gh1, gh2, ghd;
+  float wx, wy, wz;
   float cfl1, cfl2;  // 1 / rho0 of each phase: face mass flux -> volumetric flux (CFL numbers)
   float ro01, ro02, beta1, beta2;
-  float g_ro01_b1, g_ro02_b2, g_dro;  // g rho01 beta1, g rho02 beta2, g (rho02 - rho01)
-  float neg_inv_mu1, neg_inv_mu2;
   float nmr1, nmr2;      // -rho01 / mu1, -rho02 / mu2
   float ro01b1, ro02b2;  // rho01 beta1, rho02 beta2
-  float K[2], m[2], swr[2], inv_1mswr[2], e1[2], e2[2], m_inv_lam[2], inv_lam_1mswr[2], P_d[2];
-  float se_a[2], se_b[2];  // S_e = se_a + se_b S = (1 - S_wr - S) / (1 - S_wr)
+  float K[2], m[2], e1[2], e2[2], m_inv_lam[2], inv_lam_1mswr[2], P_d[2];
+  float se_b[2];  // S_e = 1 + se_b S = (1 - S_wr - S) / (1 - S_wr)
   double H_d, beta1_d, beta2_d, ro01_d, ro02_d, dtsrc_d, V;
   float2 H_df, beta1_df, beta2_df, ro01_df, ro02_df, dtsrc_df;
   // media-table porosity and dt*src/phi in wide precision: the table values

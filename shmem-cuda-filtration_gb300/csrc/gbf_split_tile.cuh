@@ -290,7 +290,7 @@ __device__ __forceinline__ float split_ex2(float x) {
 __device__ __forceinline__ void split_props(const GbfSplitConsts& C, int md, float K, float dP, float S, int j,
                                             float& L1, float& L2) {
   const float Pp = fmaf((float)j, C.H, dP);  // P - P_atm
-  const float Se = fmaf(S, C.se_b[md], C.se_a[md]);  // (1 - S - S_wr) / (1 - S_wr)
+  const float Se = fmaf(S, C.se_b[md], 1.f);  // (1 - S - S_wr) / (1 - S_wr)
   const float l2 = split_lg2(Se);
   const float kr1 = split_ex2(C.e1[md] * l2);
   const float om = 1.f - Se;
@@ -314,7 +314,7 @@ __device__ __forceinline__ float split_face(float x, float Lminus, float Lplus) 
 
 // Brooks-Corey capillary pressure P_d S_e^(-1/lambda) and its S-derivative (cpu.cpp:303-308).
 __device__ __forceinline__ float split_Pk(const GbfSplitConsts& C, int md, float S, float& dPk_dS) {
-  const float Se = fmaf(S, C.se_b[md], C.se_a[md]);
+  const float Se = fmaf(S, C.se_b[md], 1.f);
   const float Pk = C.P_d[md] * split_ex2(C.m_inv_lam[md] * split_lg2(Se));
   dPk_dS = __fdividef(Pk * C.inv_lam_1mswr[md], Se);
   return Pk;
@@ -390,7 +390,7 @@ struct GbfCellOut {
 // k - 1 (dPm, L1m, L2m) and k: the carry a tile starts its first plane with.
 __device__ __forceinline__ void split_zface(const GbfSplitConsts& C, float dPm, float L1m, float L2m, float dPc,
                                             float L1c, float L2c, float& fz1, float& fz2) {
-  const float z = (dPm - dPc) * C.inv_h3;
+  const float z = dPm - dPc;
   fz1 = split_face(z, L1m, L1c);
   fz2 = split_face(z, L2m, L2c);
 }
@@ -424,14 +424,15 @@ __device__ __forceinline__ void split_cells(const GbfSplitConsts& C, const GbfCe
 #pragma unroll
   for (int n = 0; n < N; n++) {
     const float dPc = in[n].dPc, L1c = in[n].L1c, L2c = in[n].L2c;
-    // face potentials relative to the hydrostatic profile (P2 = P1)
-    const float x1 = (in[n].dPxm - dPc) * C.inv_h1, x2 = (dPc - in[n].dPxp) * C.inv_h1;
-    const float yb1 = (in[n].dPym - dPc) * C.inv_h2;
-    const float yb2 = (dPc - in[n].dPyp) * C.inv_h2;
-    const float z2 = (dPc - in[n].dPp) * C.inv_h3;
+    // face potentials relative to the hydrostatic profile (P2 = P1), times h:
+    // pressure differences, gravity terms scaled by h2
+    const float x1 = in[n].dPxm - dPc, x2 = dPc - in[n].dPxp;
+    const float yb1 = in[n].dPym - dPc;
+    const float yb2 = dPc - in[n].dPyp;
+    const float z2 = dPc - in[n].dPp;
     Pp[n] = fmaf((float)j, C.H, dPc);  // P - P_atm
-    const float gd1 = C.g_ro01_b1 * Pp[n];  // (rho1 - rho01) g
-    const float gd2 = fmaf(C.g_ro02_b2, Pp[n], C.g_dro);
+    const float gd1 = C.gh1 * Pp[n];  // (rho1 - rho01) g h2
+    const float gd2 = fmaf(C.gh2, Pp[n], C.ghd);
     const float y11 = yb1 + gd1, y21 = noflow ? 0.f : yb2 + gd1;
     const float y12 = yb1 + gd2, y22 = noflow ? 0.f : yb2 + gd2;
     // face fluxes, in through the minus face and out through the plus face
@@ -443,21 +444,22 @@ __device__ __forceinline__ void split_cells(const GbfSplitConsts& C, const GbfCe
     const float bz1 = in[n].fz2, bz2 = split_face(z2, L2c, in[n].L2p);
     o[n].fz1 = az2;
     o[n].fz2 = bz2;
-    const float f = (ax1 - ax2) * C.inv_h1 + C.kv * (ay1 - ay2) * C.inv_h2 + (az1 - az2) * C.inv_h3;
-    const float gs = (bx1 - bx2) * C.inv_h1 + C.kv * (by1 - by2) * C.inv_h2 + (bz1 - bz2) * C.inv_h3;
-    const float dtphi = __fdividef(C.dt, in[n].phi);
-    dm1[n] = -dtphi * f;  // FP32 mass increments
-    dm2[n] = -dtphi * gs;
+    // dt times the flux divergence: sum over directions of (in - out) dt / h^2 (kv in y)
+    const float f = (ax1 - ax2) * C.wx + (ay1 - ay2) * C.wy + (az1 - az2) * C.wz;
+    const float gs = (bx1 - bx2) * C.wx + (by1 - by2) * C.wy + (bz1 - bz2) * C.wz;
+    const float rphi = __fdividef(1.f, in[n].phi);
+    dm1[n] = -f * rphi;  // FP32 mass increments
+    dm2[n] = -gs * rphi;
     if (CFL && count[n]) {
       // CFL number of each phase: the largest face volumetric flux of the cell
       // (mass flux x L_upwind over the reference density) times dt / (phi h)
       // (the mobilities L are <= 0: magnitudes by fabsf)
-      const float c1 = fmaxf(fmaxf(fmaxf(fabsf(ax1), fabsf(ax2)) * C.inv_h1, C.kv * fmaxf(fabsf(ay1), fabsf(ay2)) * C.inv_h2),
-                             fmaxf(fabsf(az1), fabsf(az2)) * C.inv_h3);
-      const float c2 = fmaxf(fmaxf(fmaxf(fabsf(bx1), fabsf(bx2)) * C.inv_h1, C.kv * fmaxf(fabsf(by1), fabsf(by2)) * C.inv_h2),
-                             fmaxf(fabsf(bz1), fabsf(bz2)) * C.inv_h3);
-      acc.cfl1 = fmaxf(acc.cfl1, c1 * dtphi * C.cfl1);
-      acc.cfl2 = fmaxf(acc.cfl2, c2 * dtphi * C.cfl2);
+      const float c1 = fmaxf(fmaxf(fmaxf(fabsf(ax1), fabsf(ax2)) * C.wx, fmaxf(fabsf(ay1), fabsf(ay2)) * C.wy),
+                             fmaxf(fabsf(az1), fabsf(az2)) * C.wz);
+      const float c2 = fmaxf(fmaxf(fmaxf(fabsf(bx1), fabsf(bx2)) * C.wx, fmaxf(fabsf(by1), fabsf(by2)) * C.wy),
+                             fmaxf(fabsf(bz1), fabsf(bz2)) * C.wz);
+      acc.cfl1 = fmaxf(acc.cfl1, c1 * rphi * C.cfl1);
+      acc.cfl2 = fmaxf(acc.cfl2, c2 * rphi * C.cfl2);
     }
     if constexpr (!DEF) {  // mass targets T = M + dm (wide)
       T1[n] = W::add_f(M1[n], dm1[n]);
@@ -1138,7 +1140,7 @@ __device__ bool split_tile_x2(const GbfSplitConsts& C, const GbfSplitGrid& G, in
   auto build = [&](int s) {  // plane buffer s from halo stage s
 #pragma unroll
     for (int q = 0; q < SLOTS; q++) {
-      if (hq[q] >= 0) {
+      if ((q + 1) * NT <= NPAIR || hq[q] >= 0) {  // the first slots hold a pair for every thread
         const int e = hq[q];
         const float2 p = gbf_ld2(&raw.v[s][0][e]), sv = gbf_ld2(&raw.v[s][1][e]), kv = gbf_ld2(&raw.v[s][2][e]);
         float l1a, l2a, l1b, l2b;
