@@ -34,6 +34,7 @@ GbfSplitConsts gbf_split_consts(const gbf_model& m) {
   const double H = m.ro01 * m.g * m.h2;
   C.H = (float)H;
   C.ro01 = (float)m.ro01; C.ro02 = (float)m.ro02; C.beta1 = (float)m.beta1; C.beta2 = (float)m.beta2;
+  C.bmax = C.beta1 > C.beta2 ? C.beta1 : C.beta2;
   C.cfl1 = (float)(1.0 / m.ro01); C.cfl2 = (float)(1.0 / m.ro02);
   C.nmr1 = (float)(-m.ro01 / m.mu1);
   C.nmr2 = (float)(-m.ro02 / m.mu2);

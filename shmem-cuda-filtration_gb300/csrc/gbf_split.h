@@ -18,7 +18,7 @@ struct GbfSplitConsts {
   float gh1, gh2, ghd;
   float wx, wy, wz;
   float cfl1, cfl2;  // 1 / rho0 of each phase: face mass flux -> volumetric flux (CFL numbers)
-  float ro01, ro02, beta1, beta2;
+  float ro01, ro02, beta1, beta2, bmax;  // bmax = max(beta1, beta2)
   float nmr1, nmr2;      // -rho01 / mu1, -rho02 / mu2
   float ro01b1, ro02b2;  // rho01 beta1, rho02 beta2
   float K[2], m[2], e1[2], e2[2], m_inv_lam[2], inv_lam_1mswr[2], P_d[2];

@@ -395,6 +395,20 @@ __device__ __forceinline__ void split_zface(const GbfSplitConsts& C, float dPm, 
   fz2 = split_face(z, L2m, L2c);
 }
 
+// Flags of a thread's row and columns, fixed for a tile (the member
+// constants are re-read from shared memory after every barrier, so the tile
+// computes them once): bit 0 the no-flow bottom row (j = ny - 2 with
+// GBF_BC_HYDROSTATIC_SIDES); bit 1 + n lane n's cell lies in the rate
+// source's row and columns (j = 1, i in the patch).
+template <int N>
+__device__ __forceinline__ unsigned split_row_flags(const GbfSplitConsts& C, int j, const int (&ci)[N]) {
+  unsigned f = (C.noflow_bottom && j == C.ny - 2) ? 1u : 0u;
+#pragma unroll
+  for (int n = 0; n < N; n++)
+    if (j == 1 && ci[n] >= C.ri0 && ci[n] < C.ri0 + C.rn) f |= 2u << n;
+  return f;
+}
+
 // The fused a3 + a4 update of N interior cells of one row and plane
 // (cpu.cpp:218-320 in the split form): donor-cell fluxes, FP32 mass
 // increments, mass targets (rate source added exactly), the residual, and the
@@ -413,12 +427,12 @@ __device__ __forceinline__ void split_cells(const GbfSplitConsts& C, const GbfCe
                                             const typename MassRep<MR>::T (&M1)[N],
                                             const typename MassRep<MR>::T (&M2)[N], typename WideOf<MR>::T R01,
                                             typename WideOf<MR>::T R02, const GbfDefectRow& rw, int md,
-                                            const int (&ci)[N], int j, int k, bool phi_field, bool mass,
+                                            unsigned rowf, int j, int k, bool phi_field, bool mass,
                                             const bool (&count)[N], GbfSplitAcc<MR>& acc, GbfCellOut<MR> (&o)[N]) {
   using W = WideOf<MR>;
   using WT = typename W::T;
   constexpr bool DEF = MR == kMassDefect;
-  const bool noflow = C.noflow_bottom && (j == C.ny - 2);
+  const bool noflow = rowf & 1u;
   float Pp[N], dm1[N], dm2[N];
   WT T1[N], T2[N];
 #pragma unroll
@@ -469,11 +483,12 @@ __device__ __forceinline__ void split_cells(const GbfSplitConsts& C, const GbfCe
   // the rate source, added exactly (defect form: its FP32 high and low parts)
   float srcf[N], srcl[N];
   bool insrc[N], anysrc = false;
+  const bool ksrc = (rowf >> 1) != 0u && (unsigned)(k - C.rk0) < (unsigned)C.rn;
 #pragma unroll
   for (int n = 0; n < N; n++) {
     srcf[n] = 0.f;
     srcl[n] = 0.f;
-    insrc[n] = j == 1 && ci[n] >= C.ri0 && ci[n] < C.ri0 + C.rn && k >= C.rk0 && k < C.rk0 + C.rn;
+    insrc[n] = ksrc && ((rowf >> (1 + n)) & 1u);
     anysrc |= insrc[n];
   }
   if (anysrc) {
@@ -528,7 +543,7 @@ __device__ __forceinline__ void split_cells(const GbfSplitConsts& C, const GbfCe
     const float inv = __fdividef(1.f, J11 * J22 - J12 * J21);
     dp[n] = -inv * (J22 * r1[n] - J12 * r2[n]);
     ds[n] = -inv * (J11 * r2[n] - J21 * r1[n]);
-    const float nl = fmaxf(C.beta1, C.beta2) * fabsf(ds[n]) * (fabsf(dp[n]) + 4.f * fabsf(dPk0[n] * ds[n]) + 1.f);
+    const float nl = C.bmax * fabsf(ds[n]) * (fabsf(dp[n]) + 4.f * fabsf(dPk0[n] * ds[n]) + 1.f);
     need[n] = nl > 1e-9f;
     anyneed |= need[n];
     Pk[n] = fmaf(dPk0[n], ds[n], Pk0[n]);
@@ -576,7 +591,7 @@ __device__ __forceinline__ void split_cells(const GbfSplitConsts& C, const GbfCe
           const float pl = phi_field ? 0.f : C.m_df[md].y;
           acc.add(ph, pl, o[n].Sn, o[n].M1n, o[n].M2n + q);
         }
-        if (!isfinite(o[n].dPn) || !isfinite(o[n].Sn)) acc.bad = 1;
+        if (!isfinite(o[n].dPn + o[n].Sn)) acc.bad = 1;  // NaN and infinities carry through the sum
       }
     } else {
       o[n].M1n = T1[n];
@@ -593,7 +608,7 @@ __device__ __forceinline__ void split_cells(const GbfSplitConsts& C, const GbfCe
             acc.m2 = W::add(acc.m2, W::mul(phw, T2[n]));
           }
         }
-        if (!isfinite(o[n].dPn) || !isfinite(o[n].Sn)) acc.bad = 1;
+        if (!isfinite(o[n].dPn + o[n].Sn)) acc.bad = 1;  // NaN and infinities carry through the sum
       }
     }
   }
@@ -786,6 +801,8 @@ __device__ bool split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i
   int t_cur = 0, t_next = 1, t_rows = 0;   // TMA: buffer/halo stage of planes k, k + 1; rows stage of plane k
   const WT R01 = W::c(C.ro01_d, C.ro01_df), R02 = W::c(C.ro02_d, C.ro02_df);
   const GbfDefectRow rw = MR == kMassDefect ? gbf_defect_row(C, j) : GbfDefectRow{};
+  const int cols[1] = {i};
+  const unsigned rowf = split_row_flags<1>(C, j, cols);
   if constexpr (MR == kMassDefect) {
     acc.c1 = rw.c1;
     acc.c2 = rw.c2;
@@ -834,10 +851,9 @@ __device__ bool split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i
       in.phi = phi;
       const GbfCellIn ins[1] = {in};
       const MT m1s[1] = {M1}, m2s[1] = {M2};
-      const int cis[1] = {i};
       const bool cnt[1] = {true};
       GbfCellOut<MR> os[1];
-      split_cells<MR, 1, CFL>(C, ins, m1s, m2s, R01, R02, rw, md, cis, j, k, G.phi != nullptr,
+      split_cells<MR, 1, CFL>(C, ins, m1s, m2s, R01, R02, rw, md, rowf, j, k, G.phi != nullptr,
                               G.mass_partials != nullptr, cnt, acc, os);
       G.dPn[c] = os[0].dPn;
       G.Sn[c] = os[0].Sn;
@@ -1184,6 +1200,9 @@ __device__ bool split_tile_x2(const GbfSplitConsts& C, const GbfSplitGrid& G, in
   }
   const WT R01 = W::c(C.ro01_d, C.ro01_df), R02 = W::c(C.ro02_d, C.ro02_df);
   const GbfDefectRow rw = MR == kMassDefect ? gbf_defect_row(C, j) : GbfDefectRow{};
+  const int cols[2] = {ia, ia + 1};
+  const unsigned rowf = split_row_flags<2>(C, j, cols);
+  const bool hsides = C.noflow_bottom != 0;  // x faces: hydrostatic Dirichlet (dP = 0)
   if constexpr (MR == kMassDefect) {
     acc.c1 = rw.c1;
     acc.c2 = rw.c2;
@@ -1237,18 +1256,17 @@ __device__ bool split_tile_x2(const GbfSplitConsts& C, const GbfSplitGrid& G, in
       in[1].dPp = dp.y; in[1].L1p = ap.y; in[1].L2p = bp.y;
       in[1].phi = ph.y;
       const MT m1s[2] = {M1a, M1b}, m2s[2] = {M2a, M2b};
-      const int cis[2] = {ia, ia + 1};
       const bool cnt[2] = {act_a, act_b};
       GbfCellOut<MR> o[2];
-      split_cells<MR, 2, CFL>(C, in, m1s, m2s, R01, R02, rw, 0, cis, j, k, true, G.mass_partials != nullptr, cnt,
+      split_cells<MR, 2, CFL>(C, in, m1s, m2s, R01, R02, rw, 0, rowf, j, k, true, G.mass_partials != nullptr, cnt,
                               acc, o);
       // The x faces i = 0 and i = nx - 1 (rows and planes interior) take the
       // boundary rules' values here: the new S of the x-neighbour and its dP
       // (cpu.cpp:327-331, 366-372), or the hydrostatic side value dP = 0 with
       // GBF_BC_HYDROSTATIC_SIDES; no other boundary rule reads these cells, so
       // the face pass skips them (gbf_boundary_count_no_xfaces).
-      const GbfCellOut<MR> oa = act_a ? o[0] : GbfCellOut<MR>{C.noflow_bottom ? 0.f : o[1].dPn, o[1].Sn, M1a, M2a};
-      const GbfCellOut<MR> ob = act_b ? o[1] : GbfCellOut<MR>{C.noflow_bottom ? 0.f : o[0].dPn, o[0].Sn, M1b, M2b};
+      const GbfCellOut<MR> oa = act_a ? o[0] : GbfCellOut<MR>{hsides ? 0.f : o[1].dPn, o[1].Sn, M1a, M2a};
+      const GbfCellOut<MR> ob = act_b ? o[1] : GbfCellOut<MR>{hsides ? 0.f : o[0].dPn, o[0].Sn, M1b, M2b};
       const unsigned c = (unsigned)(ia + j * nx) + (unsigned)k * pln;  // even: nx and ia are
       gbf_st2(G.dPn + c, oa.dPn, ob.dPn);
       gbf_st2(G.Sn + c, oa.Sn, ob.Sn);
