@@ -18,12 +18,12 @@ def domain_cls(pkg):
     return import_module(pkg.__name__ + ".domain").Domain
 
 
-@pytest.mark.parametrize("prec", ["f64", "split_df"])
+@pytest.mark.parametrize("prec", ["f64", "split_df", "split_defect"])
 def test_reference_checkpoint_restores_into_domain(gpu_lib, abi, pkg, O, oracle, tmp_path, prec):
     m, steps, path = golden_file(abi, tmp_path)
     rc, step, got, media = read(gpu_lib, m, path)
     assert rc == abi.GBF_OK
-    p = abi.GBF_PREC_F64 if prec == "f64" else abi.GBF_PREC_SPLIT_DF
+    p = {"f64": abi.GBF_PREC_F64, "split_df": abi.GBF_PREC_SPLIT_DF, "split_defect": abi.GBF_PREC_SPLIT_DEFECT}[prec]
     dom = domain_cls(pkg)(m, media, precision=p)
     assert dom.restore(path) == steps
     more = 10

@@ -19,7 +19,7 @@ def numbers(text):
     return np.array([float(x) for x in NUM.findall(text)])
 
 
-@pytest.mark.parametrize("prec", ["f64", "split_df"])
+@pytest.mark.parametrize("prec", ["f64", "split_df", "split_defect"])
 def test_domain_plot_files_match_oracle(gpu_lib, abi, pkg, O, oracle, tmp_path, prec):
     from importlib import import_module
     Domain = import_module(pkg.__name__ + ".domain").Domain
@@ -37,7 +37,7 @@ def test_domain_plot_files_match_oracle(gpu_lib, abi, pkg, O, oracle, tmp_path, 
     arrs = [st[k] for k in ("P1", "S2", "u2x", "u2y", "u2z")]
     assert gpu_lib.gbf_write_plots(str(tmp_path / "ref").encode(), ctypes.byref(m), t,
                                    *[a.ctypes.data for a in arrs], media.ctypes.data) == abi.GBF_OK
-    p = abi.GBF_PREC_F64 if prec == "f64" else abi.GBF_PREC_SPLIT_DF
+    p = {"f64": abi.GBF_PREC_F64, "split_df": abi.GBF_PREC_SPLIT_DF, "split_defect": abi.GBF_PREC_SPLIT_DEFECT}[prec]
     dom = Domain(m, media, precision=p)
     dom.upload(P0, S0)
     dom.step(steps)

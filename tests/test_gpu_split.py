@@ -102,6 +102,42 @@ def test_split_matches_fp64_gpu_at_96_cubed(gpu_lib, abi, pkg, form):
     dut.close()
 
 
+@pytest.mark.parametrize("form", ["split_df", "split_defect"])
+def test_split_long_run_against_fp64_gpu(gpu_lib, abi, pkg, form):
+    """300 steps of a 48^3 heterogeneous rate-injection grid at the reference
+    ini's compressibilities (1e-4, 1e-8), where the defects carry a large
+    compressibility part: neither the FP32 state nor the masses drift from the
+    FP64 GPU path (pinned to the oracle). Every step's phase masses within
+    1e-9, max|dS| <= 1e-5 and rel-L2(P) <= 1e-6 at the end."""
+    from importlib import import_module
+    wl = import_module(pkg.__name__ + ".workloads")
+    Domain = domain_cls(pkg)
+    mem = wl.config1(gpu_lib, n=48, seed=77)
+    mem.model.beta1, mem.model.beta2 = 1e-4, 1e-8
+    mem.model.rate = 2.0
+    wl.set_stable_dt(gpu_lib, mem, 0.5)
+    mem.model.newton_tol = 1e-11
+    steps = 300
+    P0, S0 = mem.initial_state()
+    out = {}
+    for name, p in (("f64", abi.GBF_PREC_F64), (form, prec(abi, form))):
+        d = Domain(mem.model, mem.media, mem.K, mem.phi, precision=p)
+        d.set_outputs(abi.GBF_OUT_MASS, steps)
+        d.upload(P0, S0)
+        d.step(steps)
+        assert d.status() == abi.GBF_OK
+        out[name] = (d.download("P1"), d.download("S2"), d.mass_history(steps))
+        d.close()
+    Pr, Sr, mr = out["f64"]
+    Pd, Sd, md = out[form]
+    assert Sr.max() > 1e-3
+    assert np.abs(Sd - Sr).max() <= DS_TOL
+    assert rel_l2(Pd, Pr) <= 1e-6
+    for ph in range(2):
+        drift = np.abs(md[:, ph] - mr[:, ph]) / np.abs(mr[:, ph])
+        assert drift.max() <= 1e-9, (ph, drift.max())
+
+
 def test_split_nonfinite_status(gpu_lib, abi, O, oracle, pkg):
     Domain = domain_cls(pkg)
     m = abi.reference_model(40, 12, 12, 0.01)
