@@ -36,6 +36,7 @@ struct EnsMember {
   double *M1, *M2;
   double *L1, *L2, *ro1, *ro2, *lnSe;
   int part_begin, part_end;  // this member's slots in the partial-sum array
+  double k1v;                // defect form: water-mass part left out of the tiles' sums (gbf_defect_k1)
   unsigned long long off;    // first cell of this member in the packed all-members layout
 };
 
@@ -298,7 +299,7 @@ __global__ void k_ens_mass_tail(const EnsMember* __restrict__ mem, const double*
   }
   const unsigned step = *count;
   if (threadIdx.x == 0 && step < (unsigned)cap) {
-    hist[2 * ((size_t)step * nmem + blockIdx.x)] = red[0][0];
+    hist[2 * ((size_t)step * nmem + blockIdx.x)] = red[0][0] + me.k1v;
     hist[2 * ((size_t)step * nmem + blockIdx.x) + 1] = red[1][0];
   }
 }
@@ -788,6 +789,9 @@ int gbf_ensemble_create(int n, const gbf_model* models, const gbf_cells* host_ce
       if (hc.phi && !(s |= ens_alloc(e, (void**)&me.cells.phi, nc * sizeof(float))))
         cudaMemcpy((void*)me.cells.phi, hc.phi, nc * sizeof(float), cudaMemcpyHostToDevice);
     }
+    me.k1v = 0.0;
+    if (split && !s && gbf_mass_rep(precision) == kMassDefect)
+      s |= gbf_defect_k1(m, me.cells.phi, me.cells.media, &me.k1v, nullptr);
     if (split) {
       for (int b = 0; b < 2; b++) {
         s |= ens_alloc(e, (void**)&me.dPf[b], nc * sizeof(float));

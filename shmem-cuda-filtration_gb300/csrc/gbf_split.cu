@@ -151,7 +151,35 @@ __global__ void __launch_bounds__(kThreads) k_split_boundary(const gbf_model m, 
   }
 }
 
-__global__ void k_split_mass_tail(const double* partials, int nblocks, double* out) {
+// Per interior row j: c1(j) times the sum of the row's interior porosities
+// (FP64), one block per row.
+__global__ void k_defect_k1_rows(const gbf_model m, const float* phi, const int* media, double* rows) {
+  __shared__ double red[256];
+  const int nx = m.nx, ny = m.ny, nz = m.nz, j = 1 + blockIdx.x;
+  const size_t n = (size_t)(nx - 2) * (nz - 2);
+  double a = 0.;
+  for (size_t t = threadIdx.x; t < n; t += blockDim.x) {
+    const int i = 1 + (int)(t % (nx - 2)), k = 1 + (int)(t / (nx - 2));
+    const size_t c = (size_t)i + (size_t)j * nx + (size_t)k * nx * ny;
+    a += phi ? (double)phi[c] : m.m[media ? media[c] : 0];
+  }
+  red[threadIdx.x] = a;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) rows[blockIdx.x] = (double)gbf_defect_row(m, j).c1 * red[0];
+}
+__global__ void k_defect_k1_sum(const double* rows, int nrows, double V, double* out) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double a = 0.;
+    for (int q = 0; q < nrows; q++) a += rows[q];
+    *out = a * V;
+  }
+}
+
+__global__ void k_split_mass_tail(const double* partials, int nblocks, double* out, double k1v) {
   __shared__ double red[2][256];
   double a = 0., b = 0.;
   for (int q = threadIdx.x; q < nblocks; q += blockDim.x) { a += partials[2 * q]; b += partials[2 * q + 1]; }
@@ -162,7 +190,7 @@ __global__ void k_split_mass_tail(const double* partials, int nblocks, double* o
     if (threadIdx.x < o) { red[0][threadIdx.x] += red[0][threadIdx.x + o]; red[1][threadIdx.x] += red[1][threadIdx.x + o]; }
     __syncthreads();
   }
-  if (threadIdx.x == 0) { out[0] = red[0][0]; out[1] = red[1][0]; }
+  if (threadIdx.x == 0) { out[0] = red[0][0] + k1v; out[1] = red[1][0]; }
 }
 
 __global__ void k_split_init(const gbf_model m, const double* P, const double* S, float* dPf, float* Sf,
@@ -243,7 +271,8 @@ int launch_form(const GbfSplitConsts& C, const GbfSplitGrid& G, const GbfTmaSet*
 }
 
 int gbf_split_launch_domain(const gbf_model& m, const GbfSplitConsts& C, const GbfSplitGrid& G, int mr,
-                            double* mass_out, cudaStream_t st, GbfTimer* tm, const GbfTmaSet* maps, int buf) {
+                            double* mass_out, cudaStream_t st, GbfTimer* tm, const GbfTmaSet* maps, int buf,
+                            double k1v) {
   const int kchunk = gbf_split_kchunk(C);
   const int nkc = (C.nz - 2 + kchunk - 1) / kchunk;
   unsigned blocks = (unsigned)(tiles_x(C) * tiles_y(C) * nkc);
@@ -260,7 +289,7 @@ int gbf_split_launch_domain(const gbf_model& m, const GbfSplitConsts& C, const G
   gbf_timer_end(tm, GBF_K_SPLIT_BOUNDARY, e, st);
   if (G.mass_partials && mass_out) {
     e = gbf_timer_begin(tm, st);
-    k_split_mass_tail<<<1, 256, 0, st>>>(G.mass_partials, (int)blocks, mass_out);
+    k_split_mass_tail<<<1, 256, 0, st>>>(G.mass_partials, (int)blocks, mass_out, mr == kMassDefect ? k1v : 0.0);
     gbf_timer_end(tm, GBF_K_MASS_TAIL, e, st);
   }
   cudaError_t err = cudaGetLastError();
@@ -289,6 +318,10 @@ int gbf_split_alloc(gbf_domain* d) {
   const int mb = gbf_mass_bytes(gbf_mass_rep(d->precision));
   if (!s) s |= gbf_domain_alloc(d, (void**)&d->M1, n * mb);
   if (!s) s |= gbf_domain_alloc(d, (void**)&d->M2, n * mb);
+  // the defect form's water-mass part left out of the tiles' sums
+  d->defect_k1v = 0.0;
+  if (!s && gbf_mass_rep(d->precision) == kMassDefect)
+    s |= gbf_defect_k1(d->m, d->cells.phi, d->cells.media, &d->defect_k1v, nullptr);  // after the cells' copies
   // per-block mass partials of the split step kernel
   if (!s) s |= gbf_domain_alloc(d, (void**)&d->split_partials, 2 * sizeof(double) * gbf_split_blocks(d->m, gbf_mass_rep(d->precision)));
   if (s) return GBF_ERR_NOMEM;
@@ -314,6 +347,20 @@ int gbf_split_alloc(gbf_domain* d) {
       gbf_clear_status();
     }
   }
+  return GBF_OK;
+}
+
+int gbf_defect_k1(const gbf_model& m, const float* phi_dev, const int* media_dev, double* k1v_host,
+                  cudaStream_t st) {
+  const int nrows = m.ny - 2;
+  double* rows = nullptr;
+  GBF_CUDA(cudaMallocAsync((void**)&rows, (nrows + 1) * sizeof(double), st));
+  k_defect_k1_rows<<<nrows, 256, 0, st>>>(m, phi_dev, media_dev, rows);
+  k_defect_k1_sum<<<1, 32, 0, st>>>(rows, nrows, m.h1 * m.h2 * m.h3, rows + nrows);
+  GBF_CUDA(cudaGetLastError());
+  GBF_CUDA(cudaMemcpyAsync(k1v_host, rows + nrows, sizeof(double), cudaMemcpyDeviceToHost, st));
+  GBF_CUDA(cudaStreamSynchronize(st));
+  GBF_CUDA(cudaFreeAsync(rows, st));
   return GBF_OK;
 }
 
@@ -376,7 +423,7 @@ int gbf_split_step(gbf_domain* d) {
   }
   const GbfSplitConsts C = gbf_split_consts(d->m);
   int s = gbf_split_launch_domain(d->m, C, G, gbf_mass_rep(d->precision), mass_out, d->stream, &d->timer,
-                                  (const GbfTmaSet*)d->tma, d->cur);
+                                  (const GbfTmaSet*)d->tma, d->cur, d->defect_k1v);
   if (s) return s;
   d->cur = nxt;
   d->steps++;

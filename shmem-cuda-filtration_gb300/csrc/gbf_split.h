@@ -70,8 +70,14 @@ int gbf_split_state_to_f64(const gbf_model& m, const float* dPf, const float* Sf
 // FP32 state and wide masses of one grid from FP64 device arrays.
 int gbf_split_init_state(const gbf_model& m, const double* P_dev, const double* S_dev, float* dPf, float* Sf,
                          double* M1, double* M2, int mr, cudaStream_t st);
+// V sum over interior cells of c1(j) phi (the defect form's water mass of a
+// fully water-saturated grid at the row densities): the part of the phase-1
+// mass the tiles' sums leave out. Written to *k1v_host; 0 for other forms.
+int gbf_defect_k1(const gbf_model& m, const float* phi_dev, const int* media_dev, double* k1v_host,
+                  cudaStream_t st);
 struct GbfTmaSet;
 // `maps` (device memory; boxes of the x-pair tile) selects the x-pair TMA
 // tile for state buffer `buf`; without it the plain-load 32x8 tile runs.
 int gbf_split_launch_domain(const gbf_model& m, const GbfSplitConsts& C, const GbfSplitGrid& G, int mr,
-                            double* mass_out, cudaStream_t st, GbfTimer* tm, const GbfTmaSet* maps, int buf);
+                            double* mass_out, cudaStream_t st, GbfTimer* tm, const GbfTmaSet* maps, int buf,
+                            double k1v);

@@ -336,34 +336,31 @@ struct GbfSplitAcc {  // kMassF64, kMassDF: phi T in the wide type
 };
 template <>
 struct GbfSplitAcc<kMassDefect> {
-  // sum phi S and sum phi as FP32 pairs, the exact errors of the high-part
-  // additions in the low part: TwoSum (Knuth) for sum phi S, which keeps its
-  // relative precision however small it is (the DNAPL of the first steps);
-  // FastTwoSum (Dekker) for sum phi, its high part started at 1, above every
-  // term (phi < 1). Sum phi D1 and sum phi (D2 + rho02 beta2 P_k S) in FP32
-  // (small terms). c1, c2: the densities of the thread's row (a thread keeps
-  // one row j), which turn the sums into phase masses.
-  float sS, lS, sP, lP, b1, b2, c1, c2;
+  // sum phi S as an FP32 pair: TwoSum (Knuth) into the high part, the exact
+  // errors (and those of the products phi S) into the low part, so that it
+  // keeps its relative precision however small it is (the DNAPL of the first
+  // steps); sum phi D1 and sum phi (D2 + rho02 beta2 P_k S) in FP32 (small
+  // terms). c1, c2: the densities of the thread's row (a thread keeps one row
+  // j). The phase masses are -c1 sum phi S + sum phi D1 (the grid's
+  // c1-weighted porosity sum, gbf_defect_k1, is added once per grid) and
+  // c2 sum phi S + sum phi (D2 + ...).
+  float sS, lS, b1, b2, c1, c2;
   float cfl1, cfl2;
   unsigned bad;
-  __device__ GbfSplitAcc()
-      : sS(0.f), lS(0.f), sP(1.f), lP(0.f), b1(0.f), b2(0.f), c1(0.f), c2(0.f), cfl1(0.f), cfl2(0.f), bad(0) {}
+  __device__ GbfSplitAcc() : sS(0.f), lS(0.f), b1(0.f), b2(0.f), c1(0.f), c2(0.f), cfl1(0.f), cfl2(0.f), bad(0) {}
   // phi = ph + pl (pl: the low part of a media-table porosity)
   __device__ __forceinline__ void add(float ph, float pl, float S, float D1, float D2q) {
     const float p = ph * S, pe = fmaf(pl, S, fmaf(ph, S, -p));
-    float s = sS + p;
+    const float s = sS + p;
     const float bb = s - sS;
     lS += ((sS - (s - bb)) + (p - bb)) + pe;
     sS = s;
-    s = sP + ph;
-    lP += (ph - (s - sP)) + pl;
-    sP = s;
     b1 = fmaf(ph, D1, b1);
     b2 = fmaf(ph, D2q, b2);
   }
   __device__ __forceinline__ void masses(double& a, double& b) const {
-    const double S = (double)sS + (double)lS, P = ((double)sP - 1.0) + (double)lP;
-    a = (double)c1 * (P - S) + (double)b1;
+    const double S = (double)sS + (double)lS;
+    a = (double)b1 - (double)c1 * S;
     b = (double)c2 * S + (double)b2;
   }
 };
