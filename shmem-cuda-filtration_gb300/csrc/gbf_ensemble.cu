@@ -50,9 +50,14 @@ struct EnsChunk {
 // pairs have the same shared memory (halo boxes {72, 10} and {40, 18}: 720
 // elements each); the narrower one covers grids whose nx - 1 is just above a
 // multiple of 64 with fewer idle lanes, and has the smaller halo (1.27x).
-enum { kShape32x8 = 0, kShape64x4 = 1, kShape32x4 = 2, kShape64x8x2 = 3, kShape32x16x2 = 4, kShapes = 5 };
-const int kShapeTX[kShapes] = {32, 64, 32, 64, 32}, kShapeTY[kShapes] = {8, 4, 4, 8, 16};
-const bool kShapePairs[kShapes] = {false, false, false, true, true};
+enum { kShape32x8 = 0, kShape64x4 = 1, kShape32x4 = 2, kShape64x8x2 = 3, kShape32x16x2 = 4, kShapeMixedx2 = 5,
+       kShapes = 6 };
+const int kShapeTX[kShapes] = {32, 64, 32, 64, 32, 32}, kShapeTY[kShapes] = {8, 4, 4, 8, 16, 16};
+const bool kShapePairs[kShapes] = {false, false, false, true, true, true};
+// The mixed shape's second tile: 48 x 10 cells, for the last 48 columns of a
+// grid whose nx is 16 more than a multiple of 32 (nx >= 48).
+constexpr int kWideTX = 48, kWideTY = 10;
+bool mixed_wide_tail(int nx) { return nx >= 48 && nx % 32 > 0 && nx % 32 <= 16; }
 constexpr int kChunkCells = 16384, kBoundaryChunk = 4096, kThreads = 256;
 
 // ------------------------------------------------------------ split kernels
@@ -136,14 +141,44 @@ __global__ void __launch_bounds__(TX * TY, 1024 / (TX * TY)) k_ens_split_step(co
   }
 }
 
+// Per tile: the member's constants to shared memory, its arrays to Gs.
+template <int NT, bool CFL>
+__device__ __forceinline__ void ens_tile_setup(const EnsMember* me, int member, int cur, double* partials,
+                                               unsigned* status, const EnsCfl& cfl, GbfSplitConsts& Cs,
+                                               GbfSplitGrid& Gs) {
+  const int* src = reinterpret_cast<const int*>(&me->C);
+  int* dst = reinterpret_cast<int*>(&Cs);
+  for (int q = threadIdx.x; q < (int)(sizeof(GbfSplitConsts) / sizeof(int)); q += NT) dst[q] = src[q];
+  if (threadIdx.x == 0) {
+    Gs.dP = me->dPf[cur];
+    Gs.S = me->Sf[cur];
+    Gs.dPn = me->dPf[cur ^ 1];
+    Gs.Sn = me->Sf[cur ^ 1];
+    Gs.K = me->cells.K;
+    Gs.phi = me->cells.phi;
+    Gs.media = me->cells.media;
+    Gs.M1 = me->M1;
+    Gs.M2 = me->M2;
+    Gs.mass_partials = partials;
+    Gs.status = status;
+    Gs.cfl_out = CFL ? ens_cfl_slot(cfl, member) : nullptr;
+  }
+}
+
+// Tiles of the x-pair shapes carry their kind in bit 30 of the x origin:
+// 0 the shape's own tile, 1 (mixed shape) a 48x10 tile.
+constexpr int kTileKindShift = 30;
+__host__ __device__ constexpr int tile_x0(int y) { return y & ((1 << kTileKindShift) - 1); }
+__host__ __device__ constexpr int tile_kind(int y) { return y >> kTileKindShift; }
+
 template <int MR, int TXC, int TY, bool CFL>
 __global__ void __launch_bounds__(TXC / 2 * TY, gbf_pair_ctas(MR) * 256 / (TXC / 2 * TY)) k_ens_split_step_x2(
     const EnsMember* __restrict__ mem, const int4* __restrict__ tiles, const int* __restrict__ order, int ntiles,
     int cur, unsigned* counter, double* partials, unsigned* status, const GbfTmaSet* __restrict__ maps,
     const EnsCfl cfl) {
   extern __shared__ __align__(128) unsigned char dyn[];
-  using Smem = GbfPairSmem<TXC, TY, MR>;
-  Smem& sm = *reinterpret_cast<Smem*>(dyn);
+  using Cta = GbfPairCta<TXC, TY, MR>;
+  Cta& cta = *reinterpret_cast<Cta*>(dyn);
   __shared__ GbfSplitConsts Cs;
   __shared__ GbfSplitGrid Gs;
   __shared__ int s_tile;
@@ -153,11 +188,7 @@ __global__ void __launch_bounds__(TXC / 2 * TY, gbf_pair_ctas(MR) * 256 / (TXC /
     if (threadIdx.x == 0) atomicOr(status, GBF_DEV_TIMEOUT);
     return;
   }
-  if (threadIdx.x == 0) {
-    for (int s = 0; s < kTmaStages; s++) gbf_mbar_init(&sm.ring.bar[s], 1);
-    for (int s = 0; s < Smem::Ring::RS; s++) gbf_mbar_init(&sm.ring.mbar[s], 1);
-    gbf_mbar_fence_init();
-  }
+  if (threadIdx.x == 0) gbf_pair_bars_init(cta.bars);
   __syncthreads();
   for (;;) {
     if (threadIdx.x == 0) s_tile = (int)atomicAdd(counter, 1u);
@@ -166,35 +197,68 @@ __global__ void __launch_bounds__(TXC / 2 * TY, gbf_pair_ctas(MR) * 256 / (TXC /
     if (t >= ntiles) break;
     const int ti = order ? order[t] : t;  // list index (mass-partial slot)
     const int4 tl = tiles[ti];
-    const EnsMember* me = mem + tl.x;
-    {
-      const int* src = reinterpret_cast<const int*>(&me->C);
-      int* dst = reinterpret_cast<int*>(&Cs);
-      for (int q = threadIdx.x; q < (int)(sizeof(GbfSplitConsts) / sizeof(int)); q += NT) dst[q] = src[q];
-    }
-    if (threadIdx.x == 0) {
-      Gs.dP = me->dPf[cur];
-      Gs.S = me->Sf[cur];
-      Gs.dPn = me->dPf[cur ^ 1];
-      Gs.Sn = me->Sf[cur ^ 1];
-      Gs.K = me->cells.K;
-      Gs.phi = me->cells.phi;
-      Gs.media = me->cells.media;
-      Gs.M1 = me->M1;
-      Gs.M2 = me->M2;
-      Gs.mass_partials = partials;
-      Gs.status = status;
-      Gs.cfl_out = CFL ? ens_cfl_slot(cfl, tl.x) : nullptr;
-    }
+    ens_tile_setup<NT, CFL>(mem + tl.x, tl.x, cur, partials, status, cfl, Cs, Gs);
     __syncthreads();
     GbfSplitAcc<MR> acc;
-    const bool ok = split_tile_x2<MR, TXC, TY, CFL>(Cs, Gs, tl.y, tl.z, tl.w & 0xffff, tl.w >> 16, sm, acc,
-                                               maps + tl.x, cur, &phases);
+    const bool ok = split_tile_x2<MR, TXC, TY, CFL>(Cs, Gs, tile_x0(tl.y), tl.z, tl.w & 0xffff, tl.w >> 16,
+                                                   cta.bars, cta.body, acc, maps + tl.x, cur, &phases);
     if (!ok) break;
     if (acc.bad) atomicOr(status, GBF_DEV_NONFINITE);
     if (partials) split_block_mass<MR, NT>(acc, Cs.V, partials + 2 * ti);
     if constexpr (CFL)
       if (Gs.cfl_out) split_block_cfl<NT>(acc.cfl1, acc.cfl2, Gs.cfl_out);
+    __syncthreads();
+  }
+}
+
+// The mixed x-pair shape: 32x16 tiles, and 48x10 tiles for the last 48
+// columns of members whose nx is 16 more than a multiple of 32 (fewer idle
+// lanes than a half-empty 32-wide tile). One set of barriers serves both
+// shapes' rings, which share the shared memory (a union); `maps` holds two
+// sets per member (32x16, 48x10 boxes).
+template <int MR, bool CFL>
+__global__ void __launch_bounds__(256, gbf_pair_ctas(MR)) k_ens_split_step_x2m(
+    const EnsMember* __restrict__ mem, const int4* __restrict__ tiles, const int* __restrict__ order, int ntiles,
+    int cur, unsigned* counter, double* partials, unsigned* status, const GbfTmaSet* __restrict__ maps,
+    const EnsCfl cfl) {
+  extern __shared__ __align__(128) unsigned char dyn[];
+  using Cta = GbfPairCtaMixed<MR>;
+  Cta& cta = *reinterpret_cast<Cta*>(dyn);
+  __shared__ GbfSplitConsts Cs;
+  __shared__ GbfSplitGrid Gs;
+  __shared__ int s_tile;
+  constexpr int NT = 256;
+  unsigned phases = 0;
+  if (gbf_smem_u32(dyn) & 127u) {  // the TMA destinations need it; never expected to fire
+    if (threadIdx.x == 0) atomicOr(status, GBF_DEV_TIMEOUT);
+    return;
+  }
+  if (threadIdx.x == 0) gbf_pair_bars_init(cta.bars);
+  __syncthreads();
+  for (;;) {
+    if (threadIdx.x == 0) s_tile = (int)atomicAdd(counter, 1u);
+    __syncthreads();
+    const int t = s_tile;
+    if (t >= ntiles) break;
+    const int ti = order ? order[t] : t;
+    const int4 tl = tiles[ti];
+    ens_tile_setup<NT, CFL>(mem + tl.x, tl.x, cur, partials, status, cfl, Cs, Gs);
+    __syncthreads();
+    GbfSplitAcc<MR> acc;
+    const int x0 = tile_x0(tl.y), k0 = tl.w & 0xffff, k1 = tl.w >> 16;
+    const bool ok = tile_kind(tl.y)
+                        ? split_tile_x2<MR, 48, 10, CFL, NT>(Cs, Gs, x0, tl.z, k0, k1, cta.bars, cta.b, acc,
+                                                             maps + 2 * tl.x + 1, cur, &phases)
+                        : split_tile_x2<MR, 32, 16, CFL, NT>(Cs, Gs, x0, tl.z, k0, k1, cta.bars, cta.a, acc,
+                                                             maps + 2 * tl.x, cur, &phases);
+    if (!ok) break;
+    if (acc.bad) atomicOr(status, GBF_DEV_NONFINITE);
+    if (partials) split_block_mass<MR, NT>(acc, Cs.V, partials + 2 * ti);
+    if constexpr (CFL)
+      if (Gs.cfl_out) split_block_cfl<NT>(acc.cfl1, acc.cfl2, Gs.cfl_out);
+    // the next tile's copies may land where this tile's threads wrote (the
+    // other shape's plane buffers): order the generic writes before them
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
   }
 }
@@ -467,14 +531,20 @@ int build_lists(gbf_ensemble* e) {
     if (split) {
       me.part_begin = (int)e->tiles.size();
       const int kc = kchunk_for(e, m);
-      // tiles start at i0 = 1 + t TX, or at x0 = t TX for the x-pair shape
+      // tiles start at i0 = 1 + t TX, or at x0 = t TX for the x-pair shapes;
+      // the mixed shape ends a row of 32-wide tiles with a 48x10 tile where
+      // that covers the last columns with fewer idle lanes
       const int first = kShapePairs[e->shape] ? 0 : 1;
-      for (int k0 = 1; k0 < m.nz - 1; k0 += kc)
+      const bool wide = e->shape == kShapeMixedx2 && mixed_wide_tail(m.nx);
+      const int x_end = wide ? (m.nx / 32 - 1) * 32 : m.nx - 1;  // end of the TX-wide tiles' origins
+      for (int k0 = 1; k0 < m.nz - 1; k0 += kc) {
+        const int k1 = std::min(k0 + kc, m.nz - 1);
         for (int j0 = 1; j0 < m.ny - 1; j0 += TY)
-          for (int i0 = first; i0 < m.nx - 1; i0 += TX) {
-            const int k1 = std::min(k0 + kc, m.nz - 1);
-            e->tiles.push_back(make_int4(r, i0, j0, k0 | (k1 << 16)));
-          }
+          for (int i0 = first; i0 < x_end; i0 += TX) e->tiles.push_back(make_int4(r, i0, j0, k0 | (k1 << 16)));
+        if (wide)
+          for (int j0 = 1; j0 < m.ny - 1; j0 += kWideTY)
+            e->tiles.push_back(make_int4(r, x_end | (1 << kTileKindShift), j0, k0 | (k1 << 16)));
+      }
       me.part_end = (int)e->tiles.size();
     } else {
       for (unsigned b = 0; b < g.n; b += kChunkCells) e->props.push_back({r, b, (unsigned)std::min<size_t>(g.n, b + kChunkCells)});
@@ -534,20 +604,30 @@ int build_lists(gbf_ensemble* e) {
   if (kShapePairs[e->shape] && !tma) return gbf_fail(GBF_ERR_ARG, "the x-pair tile needs TMA staging");
   const int mb = gbf_mass_bytes(gbf_mass_rep(e->precision));  // bytes of a mass element
   if (tma && !s) {
-    std::vector<GbfTmaSet> maps(e->n);
+    const bool mixed = e->shape == kShapeMixedx2;
+    std::vector<GbfTmaSet> maps(mixed ? 2 * e->n : e->n);
     int enc = GBF_OK;
+    // split_tile_x2 boxes: halo {tx + 8, ty + 2}, rows {tx, ty}
+    auto pair_maps = [&](GbfTmaSet& q, const EnsMember& me, const gbf_model& m, int tx, int ty) {
+      for (int b = 0; b < 2; b++) {
+        enc |= gbf_tma_encode_box(&q.dP[b], me.dPf[b], 4, m.nx, m.ny, m.nz, tx + 8, ty + 2);
+        enc |= gbf_tma_encode_box(&q.S[b], me.Sf[b], 4, m.nx, m.ny, m.nz, tx + 8, ty + 2);
+      }
+      enc |= gbf_tma_encode_box(&q.K, me.cells.K, 4, m.nx, m.ny, m.nz, tx + 8, ty + 2);
+      enc |= gbf_tma_encode_box(&q.M1, me.M1, mb, m.nx, m.ny, m.nz, tx, ty);
+      enc |= gbf_tma_encode_box(&q.M2, me.M2, mb, m.nx, m.ny, m.nz, tx, ty);
+      enc |= gbf_tma_encode_box(&q.phi, me.cells.phi, 4, m.nx, m.ny, m.nz, tx, ty);
+    };
     for (int r = 0; r < e->n && !enc; r++) {
       const EnsMember& me = e->h_mem[r];
       const gbf_model& m = e->models[r];
-      if (kShapePairs[e->shape]) {  // split_tile_x2 boxes: halo {TX + 8, TY + 2}, rows {TX, TY}
-        for (int b = 0; b < 2; b++) {
-          enc |= gbf_tma_encode_box(&maps[r].dP[b], me.dPf[b], 4, m.nx, m.ny, m.nz, TX + 8, TY + 2);
-          enc |= gbf_tma_encode_box(&maps[r].S[b], me.Sf[b], 4, m.nx, m.ny, m.nz, TX + 8, TY + 2);
-        }
-        enc |= gbf_tma_encode_box(&maps[r].K, me.cells.K, 4, m.nx, m.ny, m.nz, TX + 8, TY + 2);
-        enc |= gbf_tma_encode_box(&maps[r].M1, me.M1, mb, m.nx, m.ny, m.nz, TX, TY);
-        enc |= gbf_tma_encode_box(&maps[r].M2, me.M2, mb, m.nx, m.ny, m.nz, TX, TY);
-        enc |= gbf_tma_encode_box(&maps[r].phi, me.cells.phi, 4, m.nx, m.ny, m.nz, TX, TY);
+      if (mixed) {  // [2 r]: 32x16 boxes, [2 r + 1]: 48x10 boxes
+        pair_maps(maps[2 * r], me, m, TX, TY);
+        pair_maps(maps[2 * r + 1], me, m, kWideTX, kWideTY);
+        continue;
+      }
+      if (kShapePairs[e->shape]) {
+        pair_maps(maps[r], me, m, TX, TY);
         continue;
       }
       for (int b = 0; b < 2; b++) {
@@ -600,7 +680,7 @@ template <int MR, int TXC, int TY>
 int launch_split_step_x2(gbf_ensemble* e, double* partials, cudaStream_t st, const TileRange& tr) {
   if (!e->d_maps) return gbf_fail(GBF_ERR_STATE, "x-pair tile without TMA maps");
   auto kern = (partials && ens_cfl(e).hist) ? k_ens_split_step_x2<MR, TXC, TY, true> : k_ens_split_step_x2<MR, TXC, TY, false>;
-  const int bytes = (int)sizeof(GbfPairSmem<TXC, TY, MR>);
+  const int bytes = (int)sizeof(GbfPairCta<TXC, TY, MR>);
   GBF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
   int per_sm = 0;
   GBF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TXC / 2 * TY, bytes));
@@ -613,8 +693,25 @@ int launch_split_step_x2(gbf_ensemble* e, double* partials, cudaStream_t st, con
 }
 
 template <int MR>
+int launch_split_step_x2m(gbf_ensemble* e, double* partials, cudaStream_t st, const TileRange& tr) {
+  if (!e->d_maps) return gbf_fail(GBF_ERR_STATE, "x-pair tile without TMA maps");
+  auto kern = (partials && ens_cfl(e).hist) ? k_ens_split_step_x2m<MR, true> : k_ens_split_step_x2m<MR, false>;
+  const int bytes = (int)sizeof(GbfPairCtaMixed<MR>);
+  GBF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  int per_sm = 0;
+  GBF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, bytes));
+  const int blocks = std::max(1, std::min(tr.nt, std::max(1, per_sm) * gbf_num_sms()));
+  e->persistent_blocks = blocks;
+  kern<<<blocks, 256, bytes, st>>>(e->d_mem, e->d_tiles + tr.t0, tr.order, tr.nt, tr.cur, tr.counter,
+                                   partials ? partials + 2 * (size_t)tr.t0 : nullptr, e->d_status, e->d_maps,
+                                   ens_cfl(e));
+  return GBF_OK;
+}
+
+template <int MR>
 int launch_split_form(gbf_ensemble* e, double* partials, cudaStream_t st, const TileRange& tr) {
   switch (e->shape) {
+    case kShapeMixedx2: return launch_split_step_x2m<MR>(e, partials, st, tr);
     case kShape64x8x2: return launch_split_step_x2<MR, 64, 8>(e, partials, st, tr);
     case kShape32x16x2: return launch_split_step_x2<MR, 32, 16>(e, partials, st, tr);
     case kShape64x4: return launch_split_step_t<MR, 64, 4>(e, partials, st, tr);
@@ -1135,7 +1232,7 @@ int gbf_ensemble_get_tuning(gbf_ensemble* e, int* shape, int* edges, int* kchunk
 }
 
 const char* gbf_ensemble_shape_name(int shape) {
-  static const char* names[kShapes] = {"32x8", "64x4", "32x4", "64x8 pairs", "32x16 pairs"};
+  static const char* names[kShapes] = {"32x8", "64x4", "32x4", "64x8 pairs", "32x16 pairs", "32x16 + 48x10 pairs"};
   return (shape >= 0 && shape < kShapes) ? names[shape] : "";
 }
 

@@ -111,8 +111,8 @@ __global__ void __launch_bounds__(kPairTX / 2 * kPairTY, gbf_pair_ctas(MR)) k_sp
                                                                          const GbfSplitGrid G, const int kchunk,
                                                                          const GbfTmaSet* maps, int buf) {
   extern __shared__ __align__(128) unsigned char dyn[];
-  using Smem = GbfPairSmem<kPairTX, kPairTY, MR>;
-  Smem& sm = *reinterpret_cast<Smem*>(dyn);
+  using Cta = GbfPairCta<kPairTX, kPairTY, MR>;
+  Cta& cta = *reinterpret_cast<Cta*>(dyn);
   if (gbf_smem_u32(dyn) & 127u) {  // the TMA destinations need it; never expected to fire
     if (threadIdx.x == 0) atomicOr(G.status, GBF_DEV_TIMEOUT);
     return;
@@ -122,16 +122,12 @@ __global__ void __launch_bounds__(kPairTX / 2 * kPairTY, gbf_pair_ctas(MR)) k_sp
   const int tx = b % ntx, ty = (b / ntx) % nty, kc = b / (ntx * nty);
   const int k0 = 1 + kc * kchunk;
   const int k1 = min(k0 + kchunk, C.nz - 1);
-  if (threadIdx.x == 0) {
-    for (int s = 0; s < kTmaStages; s++) gbf_mbar_init(&sm.ring.bar[s], 1);
-    for (int s = 0; s < Smem::Ring::RS; s++) gbf_mbar_init(&sm.ring.mbar[s], 1);
-    gbf_mbar_fence_init();
-  }
+  if (threadIdx.x == 0) gbf_pair_bars_init(cta.bars);
   __syncthreads();
   unsigned phases = 0;
   GbfSplitAcc<MR> acc;
-  split_tile_x2<MR, kPairTX, kPairTY, CFL>(C, G, kPairTX * tx, 1 + kPairTY * ty, k0, k1, sm, acc, maps, buf,
-                                           &phases);
+  split_tile_x2<MR, kPairTX, kPairTY, CFL>(C, G, kPairTX * tx, 1 + kPairTY * ty, k0, k1, cta.bars, cta.body, acc,
+                                           maps, buf, &phases);
   if (acc.bad) atomicOr(G.status, GBF_DEV_NONFINITE);
   if (G.mass_partials) split_block_mass<MR, kPairTX / 2 * kPairTY>(acc, C.V, G.mass_partials + 2 * blockIdx.x);
   if constexpr (CFL) split_block_cfl<kPairTX / 2 * kPairTY>(acc.cfl1, acc.cfl2, G.cfl_out);
@@ -254,7 +250,7 @@ int launch_x2(const GbfSplitConsts& C, const GbfSplitGrid& G, const GbfTmaSet* m
               unsigned& blocks) {
   const int kchunk = gbf_split_kchunk_x2(C, MR);
   blocks = (unsigned)(tiles_x2(C) * tiles_y2(C) * ((C.nz - 2 + kchunk - 1) / kchunk));
-  const int bytes = (int)sizeof(GbfPairSmem<kPairTX, kPairTY, MR>);
+  const int bytes = (int)sizeof(GbfPairCta<kPairTX, kPairTY, MR>);
   GBF_CUDA(cudaFuncSetAttribute(k_split_step_x2<MR, CFL>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
   k_split_step_x2<MR, CFL><<<blocks, kPairTX / 2 * kPairTY, bytes, st>>>(C, G, kchunk, maps, buf);
   return GBF_OK;

@@ -996,7 +996,7 @@ __host__ __device__ constexpr int gbf_pair_ctas(int MR) { return MR == kMassDefe
 
 template <int TXC, int TY, int MR = kMassF64>
 struct GbfPairRing {
-  static_assert(TXC % 32 == 0 && TXC <= 248, "x-pair tile width");
+  static_assert(TXC % 16 == 0 && TXC <= 248, "x-pair tile width");
   static constexpr int BX = TXC + 8, HY = TY + 2, N = BX * HY, NP = (N + 31) / 32 * 32;
   static constexpr int NR = TXC * TY;  // interior-row elements per field
   static constexpr int RS = gbf_pair_ctas(MR) == 3 ? 2 : 3;
@@ -1006,7 +1006,6 @@ struct GbfPairRing {
   float v[kTmaStages][3][NP];
   MassElem<MR> m1[RS][NR], m2[RS][NR];
   float phi[RS][NR];
-  unsigned long long bar[kTmaStages], mbar[RS];
 };
 template <int TXC, int TY, int MR = kMassF64>
 struct GbfPairSmem {
@@ -1015,6 +1014,38 @@ struct GbfPairSmem {
   float dP[kTmaStages][Ring::NP], S[kTmaStages][Ring::NP];
   float L1[kTmaStages][Ring::NP], L2[kTmaStages][Ring::NP];
 };
+// The mbarriers of the two rings (halo planes, interior rows), apart from the
+// ring data: a CTA that runs tiles of two shapes keeps one set of barriers,
+// and their parities, for both.
+template <int MR>
+struct alignas(128) GbfPairBars {
+  static constexpr int RS = gbf_pair_ctas(MR) == 3 ? 2 : 3;
+  unsigned long long bar[kTmaStages], mbar[RS];
+};
+// Dynamic shared memory of an x-pair CTA: barriers, then one shape's rings and
+// plane buffers (every TMA destination on a 128-byte boundary).
+template <int TXC, int TY, int MR>
+struct GbfPairCta {
+  GbfPairBars<MR> bars;
+  GbfPairSmem<TXC, TY, MR> body;
+};
+// The same for a CTA that runs 32x16 and 48x10 x-pair tiles (the 48-wide
+// tile covers a grid's last 48 columns where nx is 16 more than a multiple of
+// 32; its halo box {56, 12} is smaller than {40, 18}).
+template <int MR>
+struct GbfPairCtaMixed {
+  GbfPairBars<MR> bars;
+  union {
+    GbfPairSmem<32, 16, MR> a;
+    GbfPairSmem<48, 10, MR> b;
+  };
+};
+template <int MR>
+__device__ __forceinline__ void gbf_pair_bars_init(GbfPairBars<MR>& b) {
+  for (int s = 0; s < kTmaStages; s++) gbf_mbar_init(&b.bar[s], 1);
+  for (int s = 0; s < GbfPairBars<MR>::RS; s++) gbf_mbar_init(&b.mbar[s], 1);
+  gbf_mbar_fence_init();
+}
 
 __device__ __forceinline__ float2 gbf_ld2(const float* p) { return *reinterpret_cast<const float2*>(p); }
 __device__ __forceinline__ void gbf_st2(float* p, float a, float b) { *reinterpret_cast<float2*>(p) = make_float2(a, b); }
@@ -1059,24 +1090,28 @@ template <> struct WidePair<kMassDefect> {  // FP32 defects: two floats
 // The x-pair z-marching tile: cells x0 .. x0 + TXC - 1 (interior ones only)
 // of rows j0 .. j0 + TY - 1, planes k0 .. k1 - 1. Same staging protocol,
 // bounded waits and give-up as split_tile<..., TMA = true>; each cell is
-// updated by split_cell, so results equal the other tiles' bit for bit.
-template <int MR, int TXC, int TY, bool CFL = false>
+// updated by split_cell, so results equal the other tiles' bit for bit. The
+// CTA has NTB >= TXC / 2 * TY threads; the ones beyond the tile take part in
+// the barriers only.
+template <int MR, int TXC, int TY, bool CFL = false, int NTB = TXC / 2 * TY>
 __device__ bool split_tile_x2(const GbfSplitConsts& C, const GbfSplitGrid& G, int x0, int j0, int k0, int k1,
-                              GbfPairSmem<TXC, TY, MR>& sm, GbfSplitAcc<MR>& acc, const GbfTmaSet* maps, int buf,
-                              unsigned* phases) {
+                              GbfPairBars<MR>& bars, GbfPairSmem<TXC, TY, MR>& sm, GbfSplitAcc<MR>& acc,
+                              const GbfTmaSet* maps, int buf, unsigned* phases) {
   using W = WideOf<MR>;
   using WT = typename W::T;
   using MT = typename MassRep<MR>::T;
   using Ring = GbfPairRing<TXC, TY, MR>;
   constexpr int THX = TXC / 2, NT = THX * TY, BX = Ring::BX, HY = Ring::HY, RS = Ring::RS;
+  static_assert(NT <= NTB && RS == GbfPairBars<MR>::RS, "x-pair CTA shape");
   constexpr int PCOLS = (TXC + 4) / 2;  // pair columns 1 .. PCOLS of the box (columns 2 .. TXC + 5)
   constexpr int NPAIR = PCOLS * HY, SLOTS = (NPAIR + NT - 1) / NT;
   Ring& raw = sm.ring;
+  const bool in_tile = NT == NTB || (int)threadIdx.x < NT;
   const int nx = C.nx, ny = C.ny;
   const unsigned pln = (unsigned)nx * (unsigned)ny;
   const int tx = threadIdx.x % THX, ty = threadIdx.x / THX;
   const int ia = x0 + 2 * tx, j = j0 + ty;
-  const bool row_ok = j <= ny - 2;
+  const bool row_ok = in_tile && j <= ny - 2;
   const bool act_a = row_ok && ia >= 1 && ia <= nx - 2;
   const bool act_b = row_ok && ia + 1 <= nx - 2;
   const bool any = row_ok && ia <= nx - 2;  // the pair lies in the grid's row (cell b at most nx - 1)
@@ -1094,7 +1129,7 @@ __device__ bool split_tile_x2(const GbfSplitConsts& C, const GbfSplitGrid& G, in
     const int q = threadIdx.x + s * NT;
     hq[s] = -1;
     hj[s] = 0;
-    if (q < NPAIR) {
+    if (in_tile && q < NPAIR) {
       int r, c2;
       if (q < HY * THX) {
         r = q / THX;
@@ -1115,10 +1150,10 @@ __device__ bool split_tile_x2(const GbfSplitConsts& C, const GbfSplitGrid& G, in
     const int s = h_issue;
     h_issue = s == kTmaStages - 1 ? 0 : s + 1;
     if (threadIdx.x == 0) {
-      gbf_mbar_expect_tx(&raw.bar[s], Ring::kHaloBytes);
-      gbf_tma_plane(raw.v[s][0], &maps->dP[buf], x0 - 4, j0 - 1, p, &raw.bar[s]);
-      gbf_tma_plane(raw.v[s][1], &maps->S[buf], x0 - 4, j0 - 1, p, &raw.bar[s]);
-      gbf_tma_plane(raw.v[s][2], &maps->K, x0 - 4, j0 - 1, p, &raw.bar[s]);
+      gbf_mbar_expect_tx(&bars.bar[s], Ring::kHaloBytes);
+      gbf_tma_plane(raw.v[s][0], &maps->dP[buf], x0 - 4, j0 - 1, p, &bars.bar[s]);
+      gbf_tma_plane(raw.v[s][1], &maps->S[buf], x0 - 4, j0 - 1, p, &bars.bar[s]);
+      gbf_tma_plane(raw.v[s][2], &maps->K, x0 - 4, j0 - 1, p, &bars.bar[s]);
     }
     pend |= 1u << s;
   };
@@ -1126,15 +1161,15 @@ __device__ bool split_tile_x2(const GbfSplitConsts& C, const GbfSplitGrid& G, in
     const int s = r_issue;
     r_issue = s == RS - 1 ? 0 : s + 1;
     if (threadIdx.x == 0) {
-      gbf_mbar_expect_tx(&raw.mbar[s], Ring::kRowsBytes);
-      gbf_tma_plane(raw.m1[s], &maps->M1, x0, j0, p, &raw.mbar[s]);
-      gbf_tma_plane(raw.m2[s], &maps->M2, x0, j0, p, &raw.mbar[s]);
-      gbf_tma_plane(raw.phi[s], &maps->phi, x0, j0, p, &raw.mbar[s]);
+      gbf_mbar_expect_tx(&bars.mbar[s], Ring::kRowsBytes);
+      gbf_tma_plane(raw.m1[s], &maps->M1, x0, j0, p, &bars.mbar[s]);
+      gbf_tma_plane(raw.m2[s], &maps->M2, x0, j0, p, &bars.mbar[s]);
+      gbf_tma_plane(raw.phi[s], &maps->phi, x0, j0, p, &bars.mbar[s]);
     }
     pend |= 1u << (8 + s);
   };
   auto wait_bit = [&](int bit) -> bool {
-    unsigned long long* b = bit < 8 ? &raw.bar[bit] : &raw.mbar[bit - 8];
+    unsigned long long* b = bit < 8 ? &bars.bar[bit] : &bars.mbar[bit - 8];
     if (!gbf_mbar_wait(b, (*phases >> bit) & 1u, kTmaWaitTries)) return false;
     *phases ^= 1u << bit;
     pend &= ~(1u << bit);
@@ -1143,7 +1178,7 @@ __device__ bool split_tile_x2(const GbfSplitConsts& C, const GbfSplitGrid& G, in
   auto give_up = [&]() {
     for (int bit = 0; bit < 16; bit++)
       if ((pend >> bit) & 1u) {
-        unsigned long long* b = bit < 8 ? &raw.bar[bit] : &raw.mbar[bit - 8];
+        unsigned long long* b = bit < 8 ? &bars.bar[bit] : &bars.mbar[bit - 8];
         gbf_mbar_wait(b, (*phases >> bit) & 1u, kTmaDrainTries);
         *phases ^= 1u << bit;
       }
@@ -1153,7 +1188,7 @@ __device__ bool split_tile_x2(const GbfSplitConsts& C, const GbfSplitGrid& G, in
   auto build = [&](int s) {  // plane buffer s from halo stage s
 #pragma unroll
     for (int q = 0; q < SLOTS; q++) {
-      if ((q + 1) * NT <= NPAIR || hq[q] >= 0) {  // the first slots hold a pair for every thread
+      if ((NT == NTB && (q + 1) * NT <= NPAIR) || hq[q] >= 0) {  // the first slots hold a pair for every thread
         const int e = hq[q];
         const float2 p = gbf_ld2(&raw.v[s][0][e]), sv = gbf_ld2(&raw.v[s][1][e]), kv = gbf_ld2(&raw.v[s][2][e]);
         float l1a, l2a, l1b, l2b;

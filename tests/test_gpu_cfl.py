@@ -91,7 +91,7 @@ def test_ensemble_cfl_equals_single_domains(gpu_lib, abi, pkg):
     E, D = mods(pkg)
     mems = members(abi, gpu_lib)
     steps = 6
-    for shape in (0, 3, 4):
+    for shape in (0, 3, 4, 5):
         ens = E.Ensemble(mems, precision=abi.GBF_PREC_SPLIT_DF)
         ens.set_tuning(shape, 0, 0)
         ens.set_outputs(abi.GBF_OUT_MASS | abi.GBF_OUT_CFL, steps)

@@ -37,8 +37,10 @@ def members(abi, lib):
     """Uneven members: sizes, fields, closures, anisotropy, sources, BCs."""
     out = []
     rng = np.random.default_rng(21)
-    # (72, 14, 10): two x tiles of the 64-wide x-pair tile
-    for r, (nx, ny, nz) in enumerate([(24, 20, 18), (36, 16, 22), (16, 16, 16), (40, 24, 12), (72, 14, 10)]):
+    # (72, 14, 10): two x tiles of the 64-wide x-pair tile, a 32-wide and a
+    # 48-wide one in the mixed shape; (48, 12, 14): one 48x10 tile
+    for r, (nx, ny, nz) in enumerate([(24, 20, 18), (36, 16, 22), (16, 16, 16), (40, 24, 12), (72, 14, 10),
+                                      (48, 12, 14)]):
         m = abi.reference_model(nx, ny, nz, 1.0)
         m.h1 = m.h2 = m.h3 = 0.05
         m.S_wr[:] = [0.1, 0.1]
@@ -91,7 +93,7 @@ def test_ensemble_members_equal_single_domains(gpu_lib, abi, pkg, p):
         d.step(steps)
         single.append((d.download("P1"), d.download("S2"), d.mass_history(steps)))
         d.close()
-    shapes = [0] if p == "f64" else [0, 1, 2, 3, 4]  # 3, 4: two cells per thread (TMA staging)
+    shapes = [0] if p == "f64" else [0, 1, 2, 3, 4, 5]  # 3-5: two cells per thread (TMA staging)
     for shape in shapes:
         ens = E.Ensemble(mems, precision=prec(abi, p))
         if p != "f64":
@@ -190,12 +192,12 @@ def test_ensemble_tma_staging_equals_plain_loads(gpu_lib, abi, pkg, p):
     steps = 12
     prev = gpu_lib.gbf_set_tma(-1)
     try:
-        for shape in (0, 1, 2, 3, 4):
+        for shape in (0, 1, 2, 3, 4, 5):
             res = {}
             for tma in (1, 0):
                 gpu_lib.gbf_set_tma(tma)
                 ens = E.Ensemble(mems, precision=prec(abi, p))
-                if shape in (3, 4) and not tma:  # the x-pair tiles have no plain-load form
+                if shape in (3, 4, 5) and not tma:  # the x-pair tiles have no plain-load form
                     assert gpu_lib.gbf_ensemble_set_tuning(ens.h, shape, 0, 0) == abi.GBF_ERR_ARG
                     gpu_lib.gbf_clear_status()
                     ens.set_tuning(0, 0, 0)
@@ -309,7 +311,7 @@ def test_ensemble_without_tma_refuses_pair_tile(gpu_lib, abi, pkg):
     mems.append(Mem(m, K, phi))
     ens = E.Ensemble(mems, precision=abi.GBF_PREC_SPLIT_DF)
     assert gpu_lib.gbf_ensemble_uses_tma(ens.h) == 0
-    for shape in (3, 4):
+    for shape in (3, 4, 5):
         assert gpu_lib.gbf_ensemble_set_tuning(ens.h, shape, 0, 0) == abi.GBF_ERR_ARG
         gpu_lib.gbf_clear_status()
     assert "pairs" not in ens.autotune(1)["tile"]
