@@ -50,28 +50,37 @@ GBF_HD size_t gbf_boundary_count(const GbfGeo& g) {
 // The first two groups only: every boundary cell but the x faces with j, k
 // interior (which the x-pair split tile writes itself).
 GBF_HD size_t gbf_boundary_count_no_xfaces(const GbfGeo& g) { return 2 * g.pl + 2 * (size_t)g.nx * (g.nz - 2); }
-GBF_HD void gbf_boundary_cell(const GbfGeo& g, size_t id, int& i, int& j, int& k) {
-  size_t a = 2 * g.pl;
+// (i, j, k) of boundary cell `id` in the order above. 32-bit arithmetic:
+// grids hold fewer than 2^31 cells (checked on the host), and 64-bit
+// division is emulated on the GPU.
+GBF_HD void gbf_boundary_cell(const GbfGeo& g, size_t id_, int& i, int& j, int& k) {
+  unsigned id = (unsigned)id_;
+  const unsigned nx = (unsigned)g.nx, pl = (unsigned)g.pl;
+  const unsigned a = 2u * pl;
   if (id < a) {
-    k = id < g.pl ? 0 : g.nz - 1;
-    size_t r = id % g.pl;
-    i = (int)(r % g.nx); j = (int)(r / g.nx);
+    k = id < pl ? 0 : g.nz - 1;
+    const unsigned r = id < pl ? id : id - pl;
+    j = (int)(r / nx);
+    i = (int)(r - (unsigned)j * nx);
     return;
   }
   id -= a;
-  size_t b = 2 * (size_t)g.nx * (g.nz - 2);
-  if (id < b) {
-    size_t face = (size_t)g.nx * (g.nz - 2);
+  const unsigned face = nx * (unsigned)(g.nz - 2);
+  if (id < 2u * face) {
     j = id < face ? 0 : g.ny - 1;
-    size_t r = id % face;
-    i = (int)(r % g.nx); k = 1 + (int)(r / g.nx);
+    const unsigned r = id < face ? id : id - face;
+    const unsigned q = r / nx;
+    k = 1 + (int)q;
+    i = (int)(r - q * nx);
     return;
   }
-  id -= b;
-  size_t face = (size_t)(g.ny - 2) * (g.nz - 2);
-  i = id < face ? 0 : g.nx - 1;
-  size_t r = id % face;
-  j = 1 + (int)(r % (g.ny - 2)); k = 1 + (int)(r / (g.ny - 2));
+  id -= 2u * face;
+  const unsigned ry = (unsigned)(g.ny - 2), face_x = ry * (unsigned)(g.nz - 2);
+  i = id < face_x ? 0 : g.nx - 1;
+  const unsigned r = id < face_x ? id : id - face_x;
+  const unsigned q = r / ry;
+  k = 1 + (int)q;
+  j = 1 + (int)(r - q * ry);
 }
 
 // Top-centre Dirichlet patch of the reference, |I - NX/2| <= source (cpu.cpp:346).
