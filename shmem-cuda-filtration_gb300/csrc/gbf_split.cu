@@ -17,6 +17,8 @@
 // tile; this file holds the single-domain kernels and the host side.
 #include <math.h>
 
+#include <algorithm>
+
 #include "gbf_split_tile.cuh"
 
 GbfSplitConsts gbf_split_consts(const gbf_model& m) {

@@ -958,12 +958,10 @@ __device__ __forceinline__ void split_block_cfl(float c1, float c2, float* out) 
   __syncthreads();  // red is reused by the next tile of a persistent CTA
 }
 
-// Deterministic block reduction of the phase-mass partial sums (FP64).
-template <int MR, int NT = kSplitThreads>
-__device__ __forceinline__ void split_block_mass(const GbfSplitAcc<MR>& acc, double V, double* out2) {
+// Deterministic block reduction of the threads' phase masses (FP64).
+template <int NT>
+__device__ __forceinline__ void split_block_mass_d(double a, double b, double V, double* out2) {
   __shared__ double red[2][NT / 32];
-  double a, b;
-  acc.masses(a, b);
   for (int o = 16; o > 0; o >>= 1) {
     a += __shfl_down_sync(0xffffffffu, a, o);
     b += __shfl_down_sync(0xffffffffu, b, o);
@@ -977,6 +975,12 @@ __device__ __forceinline__ void split_block_mass(const GbfSplitAcc<MR>& acc, dou
     out2[0] = x * V;
     out2[1] = y * V;
   }
+}
+template <int MR, int NT = kSplitThreads>
+__device__ __forceinline__ void split_block_mass(const GbfSplitAcc<MR>& acc, double V, double* out2) {
+  double a, b;
+  acc.masses(a, b);
+  split_block_mass_d<NT>(a, b, V, out2);
 }
 
 // ------------------------------------------------ x-pair tile (TMA only)
