@@ -64,6 +64,17 @@ __device__ __forceinline__ double gbf_donor(double x1, double x2, double Lc, dou
 // Newton for (P1, S2) from the phase masses (cpu.cpp:293-320); the first
 // iteration reuses ln(S_e) of pass 1; stops at round-off (model.newton_tol)
 // or after model.newton_iterations.
+//
+// After a step dx = (dP, dS) the residual is the Taylor remainder of F, which
+// for this system is R1 = -rho01 beta1 dP dS (F1 is bilinear in P, S) and
+// R2 = rho02 beta2 (dP dS + g'' dS^2 / 2) with g(S) = P_k(S) S; the next step
+// would be J^-1 R. When that predicted step is below tol / 1000 relative to
+// S and to P the iteration stops without computing it (relative in S too:
+// near a rate source S can be 1e-10 and its mass must keep round-off
+// accuracy); the usual case
+// at stable time steps, where one step already lands within round-off (with
+// equal compressibilities the dP dS terms cancel in the P component). g'' is
+// taken at the start point with a factor 2 for its change over the step.
 __device__ __forceinline__ void gbf_f64_newton(const gbf_model& m, const GbfDerived& d, int md, double lnSe0,
                                                double roS1, double roS2, double& P1, double& S2) {
   const double tol = m.newton_tol, swr = m.S_wr[md], pd = m.P_d[md];
@@ -83,9 +94,18 @@ __device__ __forceinline__ void gbf_f64_newton(const gbf_model& m, const GbfDeri
     const double inv_det = 1. / (F1P * F2S - F1S * F2P);
     const double dP = inv_det * (F2S * F1 - F1S * F2);
     const double dS = inv_det * (F1P * F2 - F2P * F1);
+    const double S0 = S2;
     P1 -= dP;
     S2 -= dS;
     if (tol > 0. && fabs(dS) <= tol && fabs(dP) <= tol * fabs(P1)) break;
+    if (tol > 0.) {  // the predicted next step, from the remainder
+      const double Pk2 = PkS * (1. - d.m_inv_lam[md]) * d.inv_1mswr[md] / S_e;  // P_k'' = P_k' (1 / lambda + 1) / ((1 - S_wr) S_e)
+      const double g2 = 0.5 * dS * dS * 2. * fabs(Pk2 * S0 + 2. * PkS) * m.ro02 * m.beta2;  // |g'' part of R2|
+      const double R1 = -m.ro01 * m.beta1 * dP * dS, R2 = m.ro02 * m.beta2 * dP * dS;   // the dP dS parts, signed
+      const double eP = fabs(inv_det * (F2S * R1 - F1S * R2)) + fabs(inv_det * F1S) * g2;
+      const double eS = fabs(inv_det * (F1P * R2 - F2P * R1)) + fabs(inv_det * F1P) * g2;
+      if (eS <= 1e-3 * tol * fabs(S2) && eP <= 1e-3 * tol * fabs(P1)) break;  // relative: S may be tiny
+    }
   }
 }
 
