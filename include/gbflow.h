@@ -340,8 +340,9 @@ int gbf_ensemble_set_timing(gbf_ensemble* e, int on);
 int gbf_ensemble_kernel_times(gbf_ensemble* e, double* ms, int* launches, int nkinds);
 int gbf_ensemble_launches_per_step(gbf_ensemble* e);
 /* Tuning: tile shape (0: 32x8, 1: 64x4, 2: 32x4, 3: 64x8 and 4: 32x16 cells
-   with two cells per thread, which need TMA staging: GBF_ERR_ARG without it;
-   -1 keeps it) and the k planes
+   with two cells per thread, 5: 32x16 with a 48x10 tile ending the rows of
+   grids whose nx is 16 more than a multiple of 32 — the last three need TMA
+   staging: GBF_ERR_ARG without it; -1 keeps it) and the k planes
    per tile pass ("fusion depth") of members whose nx == edge (0: whole column).
    gbf_ensemble_autotune times `trial_steps` steps per candidate and keeps the
    fastest; it advances the state, so upload the initial state afterwards. */
