@@ -333,7 +333,8 @@ def run_ours(args, rank, world):
         Pall = torch.empty(cells, dtype=torch.float64, pin_memory=True).numpy()
         Sall = torch.empty(cells, dtype=torch.float64, pin_memory=True).numpy()
         run.download_all(Pall, Sall)
-        run.advance_host(Pall, Sall, 1)  # warm-up: the first call sets up the pipeline's buffers
+        for _ in range(max(1, args.warmup)):  # warm-up calls: the first sets up the pipeline's buffers
+            run.advance_host(Pall, Sall, 1)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
@@ -345,10 +346,11 @@ def run_ours(args, rank, world):
         hostS = torch.empty(members[0].model.shape, dtype=torch.float64, pin_memory=True).numpy()
         run.download(0, "P1", hostP)
         run.download(0, "S2", hostS)
-        run.upload(0, hostP, hostS)  # warm-up round trip
-        run.step(1)
-        run.download(0, "P1", hostP)
-        run.download(0, "S2", hostS)
+        for _ in range(max(1, args.warmup)):  # warm-up round trips
+            run.upload(0, hostP, hostS)
+            run.step(1)
+            run.download(0, "P1", hostP)
+            run.download(0, "S2", hostS)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
