@@ -813,19 +813,28 @@ int enqueue_group_step(gbf_ensemble* e, int r0, int r1, int cur, unsigned* count
   return err == cudaSuccess ? GBF_OK : gbf_cuda_check(err, "gbf_ensemble group step");
 }
 
-// Member groups of the host-resident pipeline: contiguous ranges of about
-// equal cells, at least kPipeCells cells each, at most kPipeGroups groups.
+// Member groups of the host-resident pipeline: contiguous ranges, at least
+// kPipeCells cells each, at most kPipeGroups groups. The first and the last
+// group take a quarter share of the cells and the others a full one: the
+// first group's upload and the last group's download are the only copies
+// that nothing overlaps, so small end groups shorten the pipeline's fill and
+// drain.
 constexpr long long kPipeCells = 4ll << 20;
 constexpr int kPipeGroups = 16;
 std::vector<int> pipe_groups(const gbf_ensemble* e) {
   const long long want = std::max(1ll, std::min<long long>({(long long)kPipeGroups, (long long)e->n,
                                                               e->pipe_groups > 0 ? e->pipe_groups : e->cells / kPipeCells}));
+  // cumulative share of group g's end: (g + 1 - 0.75) / (want - 1.5) for g < want - 1 (want >= 3)
+  auto end_share = [&](long long g) {
+    if (want < 3) return (double)(g + 1) / (double)want;
+    return ((double)g + 0.25) / ((double)want - 1.5);
+  };
   std::vector<int> first = {0};
   long long acc = 0;
   for (int r = 0; r < e->n; r++) {
     acc += (long long)gbf_geo(e->models[r]).n;
-    const long long g = (long long)first.size();  // groups closed so far
-    if (r + 1 < e->n && g < want && acc * want >= g * e->cells) first.push_back(r + 1);
+    const long long g = (long long)first.size() - 1;  // the group member r belongs to
+    if (r + 1 < e->n && g + 1 < want && (double)acc >= end_share(g) * (double)e->cells) first.push_back(r + 1);
   }
   first.push_back(e->n);
   return first;
