@@ -132,7 +132,7 @@ def barrier(world):
 # ------------------------------------------------------------------ workloads
 
 PRECISIONS = {"f64": ("GBF_PREC_F64", "plain FP64", "f64"),
-              "split": ("GBF_PREC_SPLIT", "FP32 state and fluxes, FP64 masses and residual", "f32+f64"),
+              "split": ("GBF_PREC_SPLIT", "FP32 state and fluxes, FP64 masses (FP64 defects)", "f32+f64"),
               "splitdf": ("GBF_PREC_SPLIT_DF", "FP32 state and fluxes, FP32-pair masses and residual",
                           "f32+f32x2"),
               "splitdefect": ("GBF_PREC_SPLIT_DEFECT", "FP32 state and fluxes, phase masses as FP32 defects over "

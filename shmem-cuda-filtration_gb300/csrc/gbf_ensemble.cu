@@ -724,7 +724,7 @@ int launch_split_step(gbf_ensemble* e, double* partials, cudaStream_t st, const 
   switch (gbf_mass_rep(e->precision)) {
     case kMassDefect: return launch_split_form<kMassDefect>(e, partials, st, tr);
     case kMassDF: return launch_split_form<kMassDF>(e, partials, st, tr);
-    default: return launch_split_form<kMassF64>(e, partials, st, tr);
+    default: return launch_split_form<kMassDefect64>(e, partials, st, tr);
   }
 }
 
@@ -896,7 +896,7 @@ int gbf_ensemble_create(int n, const gbf_model* models, const gbf_cells* host_ce
         cudaMemcpy((void*)me.cells.phi, hc.phi, nc * sizeof(float), cudaMemcpyHostToDevice);
     }
     me.k1v = 0.0;
-    if (split && !s && gbf_mass_rep(precision) == kMassDefect)
+    if (split && !s && gbf_is_defect(gbf_mass_rep(precision)))
       s |= gbf_defect_k1(m, me.cells.phi, me.cells.media, &me.k1v, nullptr);
     if (split) {
       for (int b = 0; b < 2; b++) {

@@ -278,7 +278,7 @@ int gbf_split_launch_domain(const gbf_model& m, const GbfSplitConsts& C, const G
   // TMA staging (maps): the x-pair tile; else the plain-load tile
   const int s = mr == kMassDefect ? launch_form<kMassDefect>(C, G, maps, buf, st, blocks, kchunk)
                 : mr == kMassDF   ? launch_form<kMassDF>(C, G, maps, buf, st, blocks, kchunk)
-                                  : launch_form<kMassF64>(C, G, maps, buf, st, blocks, kchunk);
+                                  : launch_form<kMassDefect64>(C, G, maps, buf, st, blocks, kchunk);
   if (s) return s;
   gbf_timer_end(tm, GBF_K_SPLIT_STEP, e, st);
   e = gbf_timer_begin(tm, st);
@@ -287,7 +287,7 @@ int gbf_split_launch_domain(const gbf_model& m, const GbfSplitConsts& C, const G
   gbf_timer_end(tm, GBF_K_SPLIT_BOUNDARY, e, st);
   if (G.mass_partials && mass_out) {
     e = gbf_timer_begin(tm, st);
-    k_split_mass_tail<<<1, 256, 0, st>>>(G.mass_partials, (int)blocks, mass_out, mr == kMassDefect ? k1v : 0.0);
+    k_split_mass_tail<<<1, 256, 0, st>>>(G.mass_partials, (int)blocks, mass_out, gbf_is_defect(mr) ? k1v : 0.0);
     gbf_timer_end(tm, GBF_K_MASS_TAIL, e, st);
   }
   cudaError_t err = cudaGetLastError();
@@ -318,7 +318,7 @@ int gbf_split_alloc(gbf_domain* d) {
   if (!s) s |= gbf_domain_alloc(d, (void**)&d->M2, n * mb);
   // the defect form's water-mass part left out of the tiles' sums
   d->defect_k1v = 0.0;
-  if (!s && gbf_mass_rep(d->precision) == kMassDefect)
+  if (!s && gbf_is_defect(gbf_mass_rep(d->precision)))
     s |= gbf_defect_k1(d->m, d->cells.phi, d->cells.media, &d->defect_k1v, nullptr);  // after the cells' copies
   // per-block mass partials of the split step kernel
   if (!s) s |= gbf_domain_alloc(d, (void**)&d->split_partials, 2 * sizeof(double) * gbf_split_blocks(d->m, gbf_mass_rep(d->precision)));

@@ -141,6 +141,12 @@ struct MassRep<kMassDefect> {
   static __device__ __forceinline__ T load(const double* p, size_t i) { return reinterpret_cast<const float*>(p)[i]; }
   static __device__ __forceinline__ void store(double* p, size_t i, T v) { reinterpret_cast<float*>(p)[i] = v; }
 };
+template <>
+struct MassRep<kMassDefect64> {
+  using T = double;
+  static __device__ __forceinline__ T load(const double* p, size_t i) { return p[i]; }
+  static __device__ __forceinline__ void store(double* p, size_t i, T v) { p[i] = v; }
+};
 // Element type of a mass array in shared memory.
 template <int MR>
 using MassElem = typename std::conditional<MR == kMassDefect, float, double>::type;
@@ -334,29 +340,31 @@ struct GbfSplitAcc {  // kMassF64, kMassDF: phi T in the wide type
     b = W::tod(m2);
   }
 };
-template <>
-struct GbfSplitAcc<kMassDefect> {
-  // sum phi S as an FP32 pair: TwoSum (Knuth) into the high part, the exact
-  // errors (and those of the products phi S) into the low part, so that it
-  // keeps its relative precision however small it is (the DNAPL of the first
-  // steps); sum phi D1 and sum phi (D2 + rho02 beta2 P_k S) in FP32 (small
-  // terms). c1, c2: the densities of the thread's row (a thread keeps one row
-  // j). The phase masses are -c1 sum phi S + sum phi D1 (the grid's
-  // c1-weighted porosity sum, gbf_defect_k1, is added once per grid) and
-  // c2 sum phi S + sum phi (D2 + ...).
-  float sS, lS, b1, b2, c1, c2;
+// The defect forms: sum phi S as an FP32 pair, TwoSum (Knuth) into the high
+// part with the exact errors (and those of the products phi S) in the low
+// part, so that it keeps its relative precision however small it is (the
+// DNAPL of the first steps); sum phi D1 and sum phi (D2 + rho02 beta2 P_k S)
+// in the defects' type DT (FP32: small terms; FP64). c1, c2: the densities of
+// the thread's row (a thread keeps one row j). The phase masses are
+// -c1 sum phi S + sum phi D1 (the grid's c1-weighted porosity sum,
+// gbf_defect_k1, is added once per grid) and c2 sum phi S + sum phi (D2 + ...).
+template <typename DT>
+struct GbfDefectAcc {
+  float sS, lS;
+  DT b1, b2;
+  float c1, c2;
   float cfl1, cfl2;
   unsigned bad;
-  __device__ GbfSplitAcc() : sS(0.f), lS(0.f), b1(0.f), b2(0.f), c1(0.f), c2(0.f), cfl1(0.f), cfl2(0.f), bad(0) {}
+  __device__ GbfDefectAcc() : sS(0.f), lS(0.f), b1(0), b2(0), c1(0.f), c2(0.f), cfl1(0.f), cfl2(0.f), bad(0) {}
   // phi = ph + pl (pl: the low part of a media-table porosity)
-  __device__ __forceinline__ void add(float ph, float pl, float S, float D1, float D2q) {
+  __device__ __forceinline__ void add(float ph, float pl, float S, DT D1, DT D2q) {
     const float p = ph * S, pe = fmaf(pl, S, fmaf(ph, S, -p));
     const float s = sS + p;
     const float bb = s - sS;
     lS += ((sS - (s - bb)) + (p - bb)) + pe;
     sS = s;
-    b1 = fmaf(ph, D1, b1);
-    b2 = fmaf(ph, D2q, b2);
+    b1 += (DT)ph * D1;
+    b2 += (DT)ph * D2q;
   }
   __device__ __forceinline__ void masses(double& a, double& b) const {
     const double S = (double)sS + (double)lS;
@@ -364,6 +372,10 @@ struct GbfSplitAcc<kMassDefect> {
     b = (double)c2 * S + (double)b2;
   }
 };
+template <>
+struct GbfSplitAcc<kMassDefect> : GbfDefectAcc<float> {};
+template <>
+struct GbfSplitAcc<kMassDefect64> : GbfDefectAcc<double> {};
 
 // ------------------------------------------------------- one cell's update
 // Inputs of one cell at plane k: the cell, its x and y neighbours (y = the
@@ -428,7 +440,8 @@ __device__ __forceinline__ void split_cells(const GbfSplitConsts& C, const GbfCe
                                             const bool (&count)[N], GbfSplitAcc<MR>& acc, GbfCellOut<MR> (&o)[N]) {
   using W = WideOf<MR>;
   using WT = typename W::T;
-  constexpr bool DEF = MR == kMassDefect;
+  constexpr bool DEF = gbf_is_defect(MR);
+  using MT = typename MassRep<MR>::T;
   const bool noflow = rowf & 1u;
   float Pp[N], dm1[N], dm2[N];
   WT T1[N], T2[N];
@@ -527,8 +540,8 @@ __device__ __forceinline__ void split_cells(const GbfSplitConsts& C, const GbfCe
     const float S0 = in[n].S0;
     Pk0[n] = split_Pk(C, md, S0, dPk0[n]);
     if constexpr (DEF) {
-      r1[n] = fmaf(fmaf(C.ro01b1, in[n].dPc, rw.e1), 1.f - S0, -M1[n]) - dm1[n];
-      r2[n] = fmaf(fmaf(C.ro02b2, in[n].dPc + Pk0[n], rw.e2), S0, -M2[n]) - dm2[n] - srcf[n];
+      r1[n] = fmaf(fmaf(C.ro01b1, in[n].dPc, rw.e1), 1.f - S0, -(float)M1[n]) - dm1[n];
+      r2[n] = fmaf(fmaf(C.ro02b2, in[n].dPc + Pk0[n], rw.e2), S0, -(float)M2[n]) - dm2[n] - srcf[n];
     } else {
       r1[n] = W::rho_1mS_minus(R01, M1[n], S0) + C.ro01b1 * Pp[n] * (1.f - S0) - dm1[n];
       r2[n] = W::rhoS_minus(R02, M2[n], S0) + C.ro02b2 * (Pp[n] + Pk0[n]) * S0 - dm2[n] - srcf[n];
@@ -578,15 +591,15 @@ __device__ __forceinline__ void split_cells(const GbfSplitConsts& C, const GbfCe
       // balances inside one FMA (exact product, one rounding of a small sum)
       const float dse = o[n].Sn - in[n].S0;
       const float q = C.ro02b2 * Pk[n] * o[n].Sn;  // next step's ro2 S2 is taken without P_k (cpu.cpp:63 vs :306)
-      o[n].M1n = M1[n] + fmaf(rw.c1, dse, dm1[n]);
+      o[n].M1n = M1[n] + (MT)fmaf(rw.c1, dse, dm1[n]);
       float u = fmaf(-rw.c2, dse, dm2[n]);
       if (anysrc && insrc[n]) u = fmaf(-rw.c2, dse, srcf[n]) + (dm2[n] + srcl[n]);
-      o[n].M2n = M2[n] + (u - q);
+      o[n].M2n = M2[n] + (MT)(u - q);
       if (count[n]) {
         if (mass) {  // phi T with T1 = c1 (1 - S) + D1, T2 = c2 S + D2 + q
           const float ph = phi_field ? in[n].phi : C.m_df[md].x;
           const float pl = phi_field ? 0.f : C.m_df[md].y;
-          acc.add(ph, pl, o[n].Sn, o[n].M1n, o[n].M2n + q);
+          acc.add(ph, pl, o[n].Sn, o[n].M1n, o[n].M2n + (MT)q);
         }
         if (!isfinite(o[n].dPn + o[n].Sn)) acc.bad = 1;  // NaN and infinities carry through the sum
       }
@@ -797,10 +810,10 @@ __device__ bool split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i
   int cur = 0;                             // plain loads: buffer of plane k
   int t_cur = 0, t_next = 1, t_rows = 0;   // TMA: buffer/halo stage of planes k, k + 1; rows stage of plane k
   const WT R01 = W::c(C.ro01_d, C.ro01_df), R02 = W::c(C.ro02_d, C.ro02_df);
-  const GbfDefectRow rw = MR == kMassDefect ? gbf_defect_row(C, j) : GbfDefectRow{};
+  const GbfDefectRow rw = gbf_is_defect(MR) ? gbf_defect_row(C, j) : GbfDefectRow{};
   const int cols[1] = {i};
   const unsigned rowf = split_row_flags<1>(C, j, cols);
-  if constexpr (MR == kMassDefect) {
+  if constexpr (gbf_is_defect(MR)) {
     acc.c1 = rw.c1;
     acc.c2 = rw.c2;
   }
@@ -885,6 +898,10 @@ __device__ __forceinline__ void gbf_split_init_cell(const gbf_model& m, double p
     const GbfDefectRow w = gbf_defect_row(m, j);
     reinterpret_cast<float*>(M1)[c] = (float)(m1 - (double)w.c1 * (1. - (double)Sf));
     reinterpret_cast<float*>(M2)[c] = (float)(m2 - (double)w.c2 * (double)Sf);
+  } else if (mr == kMassDefect64) {
+    const GbfDefectRow w = gbf_defect_row(m, j);
+    M1[c] = m1 - (double)w.c1 * (1. - (double)Sf);
+    M2[c] = m2 - (double)w.c2 * (double)Sf;
   } else if (mr == kMassDF) {
     reinterpret_cast<float2*>(M1)[c] = gbf_df_from_double(m1);
     reinterpret_cast<float2*>(M2)[c] = gbf_df_from_double(m2);
@@ -1080,6 +1097,7 @@ template <> struct WidePair<kMassDF> {  // FP32-pair masses: four floats
     *reinterpret_cast<float4*>(p) = make_float4(a.hi, a.lo, b.hi, b.lo);
   }
 };
+template <> struct WidePair<kMassDefect64> : WidePair<kMassF64> {};  // FP64 defects: two doubles
 template <> struct WidePair<kMassDefect> {  // FP32 defects: two floats
   static __device__ __forceinline__ void load(const double* p, float& a, float& b) {
     const float2 v = *reinterpret_cast<const float2*>(p);
@@ -1235,11 +1253,11 @@ __device__ bool split_tile_x2(const GbfSplitConsts& C, const GbfSplitGrid& G, in
     split_zface(C, dPmb, L1mb, L2mb, d.y, a.y, b.y, fzb1, fzb2);
   }
   const WT R01 = W::c(C.ro01_d, C.ro01_df), R02 = W::c(C.ro02_d, C.ro02_df);
-  const GbfDefectRow rw = MR == kMassDefect ? gbf_defect_row(C, j) : GbfDefectRow{};
+  const GbfDefectRow rw = gbf_is_defect(MR) ? gbf_defect_row(C, j) : GbfDefectRow{};
   const int cols[2] = {ia, ia + 1};
   const unsigned rowf = split_row_flags<2>(C, j, cols);
   const bool hsides = C.noflow_bottom != 0;  // x faces: hydrostatic Dirichlet (dP = 0)
-  if constexpr (MR == kMassDefect) {
+  if constexpr (gbf_is_defect(MR)) {
     acc.c1 = rw.c1;
     acc.c2 = rw.c2;
   }
