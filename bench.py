@@ -323,8 +323,10 @@ def run_ours(args, rank, world):
             "kernel_times_ms": {k: {"total_ms": v[0], "launches": v[1]} for k, v in ktimes.items()},
             "binding_resource": ("FP64 pipe (ncu: 85% of FP64-pipe cycles active in the flux/Newton pass; "
                                  "GB300 DFMA 1.2 TFLOP/s)") if "f64" in kname else
-                                ("instruction issue (ncu: 66-80% issue active at DRAM traffic equal to the "
-                                 "algorithmic bytes)"),
+                                ("FP64 pipe (estimate: about 11 FP64 operations a cell for the FP64 mass "
+                                 "defects and their sums at GB300's 0.6e12 DFMA/s)") if p == "split" else
+                                ("instruction issue (ncu: 66-80% issue active; DRAM traffic 1.14x the "
+                                 "algorithmic bytes on config 4, halo rows re-read)"),
             "ms_per_step_with_kernel_events": ms_k / args.steps}
 
     # e2e through the C ABI with pinned host buffers: H2D state, one step, D2H P and S
