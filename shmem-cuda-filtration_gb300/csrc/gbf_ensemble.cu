@@ -283,6 +283,24 @@ __global__ void __launch_bounds__(kThreads) k_ens_split_boundary(const EnsMember
   }
 }
 
+// The face pass after the x-pair tiles: each block takes kThreads / 32 row
+// segments of one member (gbf_split_face_segment), one per warp.
+__global__ void __launch_bounds__(kThreads) k_ens_split_faces(const EnsMember* __restrict__ mem,
+                                                              const EnsChunk* __restrict__ chunks, int cur) {
+  const EnsChunk ch = chunks[blockIdx.x];
+  const unsigned w = ch.begin + (threadIdx.x >> 5);
+  if (w >= ch.end) return;
+  const EnsMember* me = mem + ch.member;
+  const gbf_model& m = me->m;
+  const GbfGeo g = gbf_geo(m);
+  const int segs = (m.nx + kFaceSeg - 1) / kFaceSeg;
+  const int r = (int)w / segs, seg = (int)w - r * segs;
+  int j, k;
+  gbf_face_row(g, r, j, k);
+  gbf_split_face_segment(m, g, me->dPf[cur], me->Sf[cur], me->dPf[cur ^ 1], me->Sf[cur ^ 1], me->C.H, j, k,
+                         seg * kFaceSeg, (int)(threadIdx.x & 31));
+}
+
 // ------------------------------------------------------------- FP64 kernels
 
 __device__ __forceinline__ GbfF64Step ens_f64_step(const EnsMember& me, int cur) {
@@ -553,9 +571,15 @@ int build_lists(gbf_ensemble* e) {
       for (unsigned b = 0; b < nint; b += kChunkCells) e->flux.push_back({r, b, (unsigned)std::min<size_t>(nint, b + kChunkCells)});
       me.part_end = (int)e->flux.size();
     }
-    // the x-pair split tile writes the x faces itself
-    const size_t nb = (split && kShapePairs[e->shape]) ? gbf_boundary_count_no_xfaces(g) : gbf_boundary_count(g);
-    for (unsigned b = 0; b < nb; b += kBoundaryChunk) e->bnd.push_back({r, b, (unsigned)std::min<size_t>(nb, b + kBoundaryChunk)});
+    if (split && kShapePairs[e->shape]) {
+      // the x-pair tile writes the x faces itself; the face pass takes the
+      // other face cells as row segments, kThreads / 32 per block
+      const unsigned items = (unsigned)(gbf_face_rows(g) * ((m.nx + kFaceSeg - 1) / kFaceSeg));
+      for (unsigned b = 0; b < items; b += kThreads / 32) e->bnd.push_back({r, b, std::min(items, b + kThreads / 32)});
+    } else {
+      const size_t nb = gbf_boundary_count(g);
+      for (unsigned b = 0; b < nb; b += kBoundaryChunk) e->bnd.push_back({r, b, (unsigned)std::min<size_t>(nb, b + kBoundaryChunk)});
+    }
     for (unsigned b = 0; b < g.n; b += kChunkCells) e->all.push_back({r, b, (unsigned)std::min<size_t>(g.n, b + kChunkCells)});
   }
   mark(e->n);
@@ -741,7 +765,10 @@ int enqueue_step(gbf_ensemble* e, cudaStream_t st) {
       return s;
     gbf_timer_end(tm, GBF_K_ENS_STEP, ev, st);
     ev = gbf_timer_begin(tm, st);
-    k_ens_split_boundary<<<(unsigned)e->bnd.size(), kThreads, 0, st>>>(e->d_mem, e->d_bnd, e->cur);
+    if (kShapePairs[e->shape])
+      k_ens_split_faces<<<(unsigned)e->bnd.size(), kThreads, 0, st>>>(e->d_mem, e->d_bnd, e->cur);
+    else
+      k_ens_split_boundary<<<(unsigned)e->bnd.size(), kThreads, 0, st>>>(e->d_mem, e->d_bnd, e->cur);
     gbf_timer_end(tm, GBF_K_ENS_BOUNDARY, ev, st);
   } else {
     ev = gbf_timer_begin(tm, st);
@@ -802,7 +829,10 @@ int enqueue_group_step(gbf_ensemble* e, int r0, int r1, int cur, unsigned* count
   if (e->precision != GBF_PREC_F64) {
     GBF_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned), st));
     if (int s = launch_split_step(e, nullptr, st, {a.tiles, b.tiles - a.tiles, cur, counter, nullptr})) return s;
-    k_ens_split_boundary<<<(unsigned)(b.bnd - a.bnd), kThreads, 0, st>>>(e->d_mem, e->d_bnd + a.bnd, cur);
+    if (kShapePairs[e->shape])
+      k_ens_split_faces<<<(unsigned)(b.bnd - a.bnd), kThreads, 0, st>>>(e->d_mem, e->d_bnd + a.bnd, cur);
+    else
+      k_ens_split_boundary<<<(unsigned)(b.bnd - a.bnd), kThreads, 0, st>>>(e->d_mem, e->d_bnd + a.bnd, cur);
   } else {
     k_ens_f64_props<<<(unsigned)(b.props - a.props), kThreads, 0, st>>>(e->d_mem, e->d_props + a.props, cur);
     k_ens_f64_flux_newton<<<(unsigned)(b.flux - a.flux), kThreads, 0, st>>>(e->d_mem, e->d_flux + a.flux, cur,

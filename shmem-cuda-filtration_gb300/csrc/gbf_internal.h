@@ -50,6 +50,21 @@ GBF_HD size_t gbf_boundary_count(const GbfGeo& g) {
 // The first two groups only: every boundary cell but the x faces with j, k
 // interior (which the x-pair split tile writes itself).
 GBF_HD size_t gbf_boundary_count_no_xfaces(const GbfGeo& g) { return 2 * g.pl + 2 * (size_t)g.nx * (g.nz - 2); }
+// The same cells as rows of nx cells at (j, k), "face rows":
+//   r in [0, 2 ny)                  k = 0 (r < ny) or nz - 1, j = r mod ny
+//   r in [2 ny, 2 ny + 2 (nz - 2))  j = 0 or ny - 1, k = 1 + (r - 2 ny) mod (nz - 2)
+GBF_HD int gbf_face_rows(const GbfGeo& g) { return 2 * g.ny + 2 * (g.nz - 2); }
+GBF_HD void gbf_face_row(const GbfGeo& g, int r, int& j, int& k) {
+  if (r < 2 * g.ny) {
+    k = r < g.ny ? 0 : g.nz - 1;
+    j = r < g.ny ? r : r - g.ny;
+    return;
+  }
+  r -= 2 * g.ny;
+  const int nk = g.nz - 2;
+  j = r < nk ? 0 : g.ny - 1;
+  k = 1 + (r < nk ? r : r - nk);
+}
 // (i, j, k) of boundary cell `id` in the order above. 32-bit arithmetic:
 // grids hold fewer than 2^31 cells (checked on the host), and 64-bit
 // division is emulated on the GPU.

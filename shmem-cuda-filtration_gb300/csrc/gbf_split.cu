@@ -282,6 +282,8 @@ int gbf_split_launch_domain(const gbf_model& m, const GbfSplitConsts& C, const G
   if (s) return s;
   gbf_timer_end(tm, GBF_K_SPLIT_STEP, e, st);
   e = gbf_timer_begin(tm, st);
+  // one cell per thread (row segments, as the ensembles' face pass walks
+  // them, measured 8.6 -> 10.4 us on 256^3: too few warps for a latency-bound pass)
   const size_t nb = maps ? gbf_boundary_count_no_xfaces(gbf_geo(m)) : gbf_boundary_count(gbf_geo(m));
   k_split_boundary<<<gbf_grid_for(nb, kThreads, 4), kThreads, 0, st>>>(m, G, C.H, nb);
   gbf_timer_end(tm, GBF_K_SPLIT_BOUNDARY, e, st);

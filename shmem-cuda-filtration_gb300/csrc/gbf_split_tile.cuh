@@ -952,6 +952,38 @@ __device__ __forceinline__ float gbf_split_sweep_dP(const gbf_model& m, const Gb
   return has_add ? base + add : base;
 }
 
+// One row segment of the face pass after the x-pair tile: a warp writes the
+// new S and dP of cells i0 .. i0 + kFaceSeg - 1 (those below nx) of face row
+// (j, k) (gbf_face_row), kFaceRound a lane. The rules read interior cells of
+// the new state and boundary cells of the previous one, never a cell that
+// this pass writes, so every value is read before any is written: a lane's
+// loads are in flight together. j and k are the same for the whole warp, so
+// only the row's end cells branch apart.
+constexpr int kFaceRound = 4, kFaceSeg = 32 * kFaceRound;
+__device__ __forceinline__ void gbf_split_face_segment(const gbf_model& m, const GbfGeo& g, const float* dP,
+                                                       const float* S, float* dPn, float* Sn, float H, int j, int k,
+                                                       int i0, int lane) {
+  float sv[kFaceRound], pv[kFaceRound];
+#pragma unroll
+  for (int u = 0; u < kFaceRound; u++) {
+    const int i = i0 + lane + 32 * u;
+    sv[u] = pv[u] = 0.f;
+    if (i < g.nx) {
+      sv[u] = gbf_sweep_S<float>(m, g, Sn, S, i, j, k);
+      pv[u] = gbf_split_sweep_dP(m, g, dPn, dP, i, j, k, H);
+    }
+  }
+  const size_t row = gbf_idx(g, 0, j, k);
+#pragma unroll
+  for (int u = 0; u < kFaceRound; u++) {
+    const int i = i0 + lane + 32 * u;
+    if (i < g.nx) {
+      Sn[row + i] = sv[u];
+      dPn[row + i] = pv[u];
+    }
+  }
+}
+
 // Block maximum of the threads' CFL numbers (warp shuffles, then one thread
 // over the warps' maxima), max-combined into out[2] with atomicMax on the
 // bit patterns (non-negative floats order like their bits; NaN left out).
@@ -1318,7 +1350,7 @@ __device__ bool split_tile_x2(const GbfSplitConsts& C, const GbfSplitGrid& G, in
       // boundary rules' values here: the new S of the x-neighbour and its dP
       // (cpu.cpp:327-331, 366-372), or the hydrostatic side value dP = 0 with
       // GBF_BC_HYDROSTATIC_SIDES; no other boundary rule reads these cells, so
-      // the face pass skips them (gbf_boundary_count_no_xfaces).
+      // the face pass skips them (gbf_boundary_count_no_xfaces, gbf_face_row).
       const GbfCellOut<MR> oa = act_a ? o[0] : GbfCellOut<MR>{hsides ? 0.f : o[1].dPn, o[1].Sn, M1a, M2a};
       const GbfCellOut<MR> ob = act_b ? o[1] : GbfCellOut<MR>{hsides ? 0.f : o[0].dPn, o[0].Sn, M1b, M2b};
       const unsigned c = (unsigned)(ia + j * nx) + (unsigned)k * pln;  // even: nx and ia are
