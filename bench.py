@@ -5,7 +5,8 @@
 
 Workloads are <config>_<precision>: config0..config4 (the benchmark
 configurations as seeded synthetic inputs, see workloads.py) and f64, split
-(FP64 masses), splitdf (FP32-pair masses), splitdefect (FP32 mass defects).
+(masses at FP64 precision: FP32-pair defects), splitdf (FP32-pair masses), splitdefect
+(FP32 mass defects).
 The default, config4_splitdefect, is the combined
 precision + batching form on the 256-member ensemble; the same line also
 reports plain FP64 and the other split forms on the same members.
@@ -132,7 +133,8 @@ def barrier(world):
 # ------------------------------------------------------------------ workloads
 
 PRECISIONS = {"f64": ("GBF_PREC_F64", "plain FP64", "f64"),
-              "split": ("GBF_PREC_SPLIT", "FP32 state and fluxes, FP64 masses (FP64 defects)", "f32+f64"),
+              "split": ("GBF_PREC_SPLIT", "FP32 state and fluxes, phase masses at FP64 precision (FP32-pair "
+                        "defects over the state's mass at the row's hydrostatic density)", "f32+f32x2"),
               "splitdf": ("GBF_PREC_SPLIT_DF", "FP32 state and fluxes, FP32-pair masses and residual",
                           "f32+f32x2"),
               "splitdefect": ("GBF_PREC_SPLIT_DEFECT", "FP32 state and fluxes, phase masses as FP32 defects over "
@@ -323,8 +325,6 @@ def run_ours(args, rank, world):
             "kernel_times_ms": {k: {"total_ms": v[0], "launches": v[1]} for k, v in ktimes.items()},
             "binding_resource": ("FP64 pipe (ncu: 85% of FP64-pipe cycles active in the flux/Newton pass; "
                                  "GB300 DFMA 1.2 TFLOP/s)") if "f64" in kname else
-                                ("FP64 pipe (estimate: about 11 FP64 operations a cell for the FP64 mass "
-                                 "defects and their sums at GB300's 0.6e12 DFMA/s)") if p == "split" else
                                 ("instruction issue (ncu: 66-80% issue active; DRAM traffic 1.14x the "
                                  "algorithmic bytes on config 4, halo rows re-read)"),
             "ms_per_step_with_kernel_events": ms_k / args.steps}

@@ -42,8 +42,9 @@ enum { GBF_BC_REFERENCE = 0,           /* reference Border_S2/Border_P1 rules   
        GBF_BC_HYDROSTATIC_SIDES = 1 }; /* Dirichlet hydrostatic P on i/k sides,
                                           no-flow bottom face for both phases          */
 enum { GBF_PREC_F64 = 0,               /* plain FP64 state and arithmetic               */
-       GBF_PREC_SPLIT = 1,             /* FP32 P,S,K,fluxes; FP64 phase masses, held as FP64
-                                          defects over the state's exact FP32-product mass */
+       GBF_PREC_SPLIT = 1,             /* FP32 P,S,K,fluxes; phase masses at least as precise
+                                          as FP64: FP32-pair defects over the state's exact
+                                          FP32-product mass (FP32 pipes only)            */
        GBF_PREC_SPLIT_DF = 2,          /* as SPLIT, masses and residual as FP32 pairs
                                           (about 48 significant bits, FP32 pipes only)  */
        GBF_PREC_SPLIT_DEFECT = 3 };    /* as SPLIT, each phase mass held as its FP32
@@ -185,8 +186,9 @@ int gbf_boundary_f64_noalloc(const gbf_model* m, gbf_arrays d_arrays, void* stre
  * One grid whose state lives in HBM between steps. `precision` is
  * GBF_PREC_F64 (plain FP64: two passes per step — properties, then fluxes,
  * mass update and Newton fused — plus a face pass for the boundaries) or
- * GBF_PREC_SPLIT (FP32 P, S, K, phi and fluxes; FP64 per-cell phase masses,
- * as FP64 defects), GBF_PREC_SPLIT_DF (the masses and residual as FP32 pairs)
+ * GBF_PREC_SPLIT (FP32 P, S, K, phi and fluxes; per-cell phase masses at
+ * least as precise as FP64, as FP32-pair defects), GBF_PREC_SPLIT_DF (the
+ * masses and residual as FP32 pairs)
  * or GBF_PREC_SPLIT_DEFECT (the masses as FP32 defects). All
  * calls are ordered on the domain's
  * stream; gbf_domain_step only enqueues work.

@@ -748,7 +748,7 @@ int launch_split_step(gbf_ensemble* e, double* partials, cudaStream_t st, const 
   switch (gbf_mass_rep(e->precision)) {
     case kMassDefect: return launch_split_form<kMassDefect>(e, partials, st, tr);
     case kMassDF: return launch_split_form<kMassDF>(e, partials, st, tr);
-    default: return launch_split_form<kMassDefect64>(e, partials, st, tr);
+    default: return launch_split_form<kMassDefectDF>(e, partials, st, tr);
   }
 }
 

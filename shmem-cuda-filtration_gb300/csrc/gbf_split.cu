@@ -278,7 +278,7 @@ int gbf_split_launch_domain(const gbf_model& m, const GbfSplitConsts& C, const G
   // TMA staging (maps): the x-pair tile; else the plain-load tile
   const int s = mr == kMassDefect ? launch_form<kMassDefect>(C, G, maps, buf, st, blocks, kchunk)
                 : mr == kMassDF   ? launch_form<kMassDF>(C, G, maps, buf, st, blocks, kchunk)
-                                  : launch_form<kMassDefect64>(C, G, maps, buf, st, blocks, kchunk);
+                                  : launch_form<kMassDefectDF>(C, G, maps, buf, st, blocks, kchunk);
   if (s) return s;
   gbf_timer_end(tm, GBF_K_SPLIT_STEP, e, st);
   e = gbf_timer_begin(tm, st);

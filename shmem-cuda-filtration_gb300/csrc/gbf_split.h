@@ -36,13 +36,14 @@ GbfSplitConsts gbf_split_consts(const gbf_model& m);
 
 // How the split forms hold the per-cell phase masses M1, M2 (gbf_split_tile.cuh):
 // kMassDF FP32 pairs; kMassDefect FP32 defects over the mass of the FP32
-// state at the row's hydrostatic density (4 bytes); kMassDefect64 the same
-// defects in FP64 (GBF_PREC_SPLIT: FP64 masses). kMassF64 (the masses
-// themselves in FP64) is the wide arithmetic's FP64 flavour, not a form.
-enum { kMassF64 = 0, kMassDF = 1, kMassDefect = 2, kMassDefect64 = 3 };
-__host__ __device__ constexpr bool gbf_is_defect(int mr) { return mr == kMassDefect || mr == kMassDefect64; }
+// state at the row's hydrostatic density (4 bytes); kMassDefectDF the same
+// defects as FP32 pairs (8 bytes; GBF_PREC_SPLIT: masses at least as precise
+// as FP64). kMassF64 (the masses themselves in FP64) is the wide
+// arithmetic's FP64 flavour, not a form.
+enum { kMassF64 = 0, kMassDF = 1, kMassDefect = 2, kMassDefectDF = 3 };
+__host__ __device__ constexpr bool gbf_is_defect(int mr) { return mr == kMassDefect || mr == kMassDefectDF; }
 __host__ __device__ inline int gbf_mass_rep(int precision) {
-  return precision == GBF_PREC_SPLIT_DEFECT ? kMassDefect : precision == GBF_PREC_SPLIT_DF ? kMassDF : kMassDefect64;
+  return precision == GBF_PREC_SPLIT_DEFECT ? kMassDefect : precision == GBF_PREC_SPLIT_DF ? kMassDF : kMassDefectDF;
 }
 __host__ __device__ inline int gbf_mass_bytes(int mr) { return mr == kMassDefect ? 4 : 8; }
 

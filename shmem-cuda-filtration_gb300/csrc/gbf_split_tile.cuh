@@ -124,9 +124,9 @@ template <> struct Wide<true> {
 
 // ------------------------------------------------- per-cell mass storage
 // M1, M2 of the split forms: the phase masses in the wide type (kMassF64,
-// kMassDF: 8 bytes a cell), or FP32 defects (kMassDefect, 4 bytes). The
-// wide type of a form (constants, the source) is FP64 for kMassF64 and FP32
-// pairs otherwise.
+// kMassDF: 8 bytes a cell), or defects (below) in FP32 (kMassDefect, 4
+// bytes) or FP32 pairs (kMassDefectDF, 8 bytes). The wide type of a form
+// (constants, the source) is FP64 for kMassF64 and FP32 pairs otherwise.
 template <int MR>
 using WideOf = Wide<MR != kMassF64>;
 template <int MR>
@@ -142,11 +142,17 @@ struct MassRep<kMassDefect> {
   static __device__ __forceinline__ void store(double* p, size_t i, T v) { reinterpret_cast<float*>(p)[i] = v; }
 };
 template <>
-struct MassRep<kMassDefect64> {
-  using T = double;
-  static __device__ __forceinline__ T load(const double* p, size_t i) { return p[i]; }
-  static __device__ __forceinline__ void store(double* p, size_t i, T v) { p[i] = v; }
+struct MassRep<kMassDefectDF> {
+  using T = GbfDF;
+  static __device__ __forceinline__ T load(const double* p, size_t i) { return Wide<true>::load(p, i); }
+  static __device__ __forceinline__ void store(double* p, size_t i, T v) { Wide<true>::store(p, i, v); }
 };
+// A defect's FP32 value (the high part of a pair: |lo| <= ulp(hi) / 2) and
+// a defect plus an FP32 increment, in each defect storage.
+__device__ __forceinline__ float defect_f(float d) { return d; }
+__device__ __forceinline__ float defect_f(GbfDF d) { return d.hi; }
+__device__ __forceinline__ float defect_add(float d, float x) { return d + x; }
+__device__ __forceinline__ GbfDF defect_add(GbfDF d, float x) { return Wide<true>::add_f(d, x); }
 // Element type of a mass array in shared memory.
 template <int MR>
 using MassElem = typename std::conditional<MR == kMassDefect, float, double>::type;
@@ -155,12 +161,14 @@ using MassElem = typename std::conditional<MR == kMassDefect, float, double>::ty
 //   M1 = c1(j) (1 - S) + D1,   M2 = c2(j) S + D2,
 // with S the cell's FP32 saturation, c_a(j) the hydrostatic density of phase
 // a at row j, rho0a (1 + beta_a j H), rounded to FP32 (so c (1 - S) and c S
-// are exact products), and D1, D2 FP32 "defects": the compressibility part
-// rho0a beta_a dP and the Newton residual, small numbers. The residual of the
-// Newton and the mass update then need FP32 only, with rounding errors
-// relative to those small numbers; e_a is the remainder rho0a (1 + beta_a j H)
-// - c_a (FP32). Both follow from FP64 by fixed roundings, so every kernel
-// derives the same values.
+// are exact products), and D1, D2 "defects" (FP32, or FP32 pairs): the
+// compressibility part rho0a beta_a dP and the Newton residual, small
+// numbers. The residual of the Newton and the mass update then need FP32
+// only, with rounding errors relative to those small numbers; e_a is the
+// remainder rho0a (1 + beta_a j H) - c_a (FP32). Both follow from FP64 by
+// fixed roundings, so every kernel derives the same values. Pair defects
+// round at about 2^-48 |D| per update: with |D| / M <= 1e-2, finer than an
+// FP64 mass's own rounding (2^-53 M).
 struct GbfDefectRow {
   float c1, e1, c2, e2;
 };
@@ -344,7 +352,7 @@ struct GbfSplitAcc {  // kMassF64, kMassDF: phi T in the wide type
 // part with the exact errors (and those of the products phi S) in the low
 // part, so that it keeps its relative precision however small it is (the
 // DNAPL of the first steps); sum phi D1 and sum phi (D2 + rho02 beta2 P_k S)
-// in the defects' type DT (FP32: small terms; FP64). c1, c2: the densities of
+// in the defects' type DT (FP32: small terms). c1, c2: the densities of
 // the thread's row (a thread keeps one row j). The phase masses are
 // -c1 sum phi S + sum phi D1 (the grid's c1-weighted porosity sum,
 // gbf_defect_k1, is added once per grid) and c2 sum phi S + sum phi (D2 + ...).
@@ -374,8 +382,34 @@ struct GbfDefectAcc {
 };
 template <>
 struct GbfSplitAcc<kMassDefect> : GbfDefectAcc<float> {};
+// Pair defects: sum phi D1 and sum phi (D2 + ...) as FP32 pairs (each
+// product's rounding error kept, TwoSum into the high part).
 template <>
-struct GbfSplitAcc<kMassDefect64> : GbfDefectAcc<double> {};
+struct GbfSplitAcc<kMassDefectDF> {
+  float sS, lS;
+  GbfDF b1, b2;
+  float c1, c2;
+  float cfl1, cfl2;
+  unsigned bad;
+  __device__ GbfSplitAcc()
+      : sS(0.f), lS(0.f), b1{0.f, 0.f}, b2{0.f, 0.f}, c1(0.f), c2(0.f), cfl1(0.f), cfl2(0.f), bad(0) {}
+  __device__ __forceinline__ void add(float ph, float pl, float S, GbfDF D1, GbfDF D2q) {
+    const float p = ph * S, pe = fmaf(pl, S, fmaf(ph, S, -p));
+    const float s = sS + p;
+    const float bb = s - sS;
+    lS += ((sS - (s - bb)) + (p - bb)) + pe;
+    sS = s;
+    b1 = Wide<true>::acc_phi(b1, ph, D1);
+    b2 = Wide<true>::acc_phi(b2, ph, D2q);
+    b1.lo = fmaf(pl, D1.hi, b1.lo);
+    b2.lo = fmaf(pl, D2q.hi, b2.lo);
+  }
+  __device__ __forceinline__ void masses(double& a, double& b) const {
+    const double S = (double)sS + (double)lS;
+    a = Wide<true>::tod(b1) - (double)c1 * S;
+    b = (double)c2 * S + Wide<true>::tod(b2);
+  }
+};
 
 // ------------------------------------------------------- one cell's update
 // Inputs of one cell at plane k: the cell, its x and y neighbours (y = the
@@ -540,8 +574,8 @@ __device__ __forceinline__ void split_cells(const GbfSplitConsts& C, const GbfCe
     const float S0 = in[n].S0;
     Pk0[n] = split_Pk(C, md, S0, dPk0[n]);
     if constexpr (DEF) {
-      r1[n] = fmaf(fmaf(C.ro01b1, in[n].dPc, rw.e1), 1.f - S0, -(float)M1[n]) - dm1[n];
-      r2[n] = fmaf(fmaf(C.ro02b2, in[n].dPc + Pk0[n], rw.e2), S0, -(float)M2[n]) - dm2[n] - srcf[n];
+      r1[n] = fmaf(fmaf(C.ro01b1, in[n].dPc, rw.e1), 1.f - S0, -defect_f(M1[n])) - dm1[n];
+      r2[n] = fmaf(fmaf(C.ro02b2, in[n].dPc + Pk0[n], rw.e2), S0, -defect_f(M2[n])) - dm2[n] - srcf[n];
     } else {
       r1[n] = W::rho_1mS_minus(R01, M1[n], S0) + C.ro01b1 * Pp[n] * (1.f - S0) - dm1[n];
       r2[n] = W::rhoS_minus(R02, M2[n], S0) + C.ro02b2 * (Pp[n] + Pk0[n]) * S0 - dm2[n] - srcf[n];
@@ -591,15 +625,15 @@ __device__ __forceinline__ void split_cells(const GbfSplitConsts& C, const GbfCe
       // balances inside one FMA (exact product, one rounding of a small sum)
       const float dse = o[n].Sn - in[n].S0;
       const float q = C.ro02b2 * Pk[n] * o[n].Sn;  // next step's ro2 S2 is taken without P_k (cpu.cpp:63 vs :306)
-      o[n].M1n = M1[n] + (MT)fmaf(rw.c1, dse, dm1[n]);
+      o[n].M1n = defect_add(M1[n], fmaf(rw.c1, dse, dm1[n]));
       float u = fmaf(-rw.c2, dse, dm2[n]);
       if (anysrc && insrc[n]) u = fmaf(-rw.c2, dse, srcf[n]) + (dm2[n] + srcl[n]);
-      o[n].M2n = M2[n] + (MT)(u - q);
+      o[n].M2n = defect_add(M2[n], u - q);
       if (count[n]) {
         if (mass) {  // phi T with T1 = c1 (1 - S) + D1, T2 = c2 S + D2 + q
           const float ph = phi_field ? in[n].phi : C.m_df[md].x;
           const float pl = phi_field ? 0.f : C.m_df[md].y;
-          acc.add(ph, pl, o[n].Sn, o[n].M1n, o[n].M2n + (MT)q);
+          acc.add(ph, pl, o[n].Sn, o[n].M1n, defect_add(o[n].M2n, q));
         }
         if (!isfinite(o[n].dPn + o[n].Sn)) acc.bad = 1;  // NaN and infinities carry through the sum
       }
@@ -898,10 +932,10 @@ __device__ __forceinline__ void gbf_split_init_cell(const gbf_model& m, double p
     const GbfDefectRow w = gbf_defect_row(m, j);
     reinterpret_cast<float*>(M1)[c] = (float)(m1 - (double)w.c1 * (1. - (double)Sf));
     reinterpret_cast<float*>(M2)[c] = (float)(m2 - (double)w.c2 * (double)Sf);
-  } else if (mr == kMassDefect64) {
+  } else if (mr == kMassDefectDF) {
     const GbfDefectRow w = gbf_defect_row(m, j);
-    M1[c] = m1 - (double)w.c1 * (1. - (double)Sf);
-    M2[c] = m2 - (double)w.c2 * (double)Sf;
+    reinterpret_cast<float2*>(M1)[c] = gbf_df_from_double(m1 - (double)w.c1 * (1. - (double)Sf));
+    reinterpret_cast<float2*>(M2)[c] = gbf_df_from_double(m2 - (double)w.c2 * (double)Sf);
   } else if (mr == kMassDF) {
     reinterpret_cast<float2*>(M1)[c] = gbf_df_from_double(m1);
     reinterpret_cast<float2*>(M2)[c] = gbf_df_from_double(m2);
@@ -1129,7 +1163,7 @@ template <> struct WidePair<kMassDF> {  // FP32-pair masses: four floats
     *reinterpret_cast<float4*>(p) = make_float4(a.hi, a.lo, b.hi, b.lo);
   }
 };
-template <> struct WidePair<kMassDefect64> : WidePair<kMassF64> {};  // FP64 defects: two doubles
+template <> struct WidePair<kMassDefectDF> : WidePair<kMassDF> {};  // pair defects: four floats
 template <> struct WidePair<kMassDefect> {  // FP32 defects: two floats
   static __device__ __forceinline__ void load(const double* p, float& a, float& b) {
     const float2 v = *reinterpret_cast<const float2*>(p);

@@ -26,8 +26,8 @@ def p_tol(model) -> float:
 
 def mass_order_rtol(form: str, wide: float) -> float:
     """Tolerance between phase-mass sums of one state taken in different orders
-    (other tilings, single domain vs ensemble). The wide split forms sum phi T
-    in FP64 or FP32 pairs; the defect form sums phi D in FP32, so its sums move
+    (other tilings, single domain vs ensemble). The other split forms sum phi T
+    or phi D in FP32 pairs; the FP32 defect form sums phi D in FP32, so its sums move
     by about 2^-24 |sum phi D| / |mass| (D / M up to 1e-5 at compressibility
     1e-4: about 1e-12)."""
     return 2e-11 if form == "split_defect" else wide

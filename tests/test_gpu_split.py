@@ -102,7 +102,7 @@ def test_split_matches_fp64_gpu_at_96_cubed(gpu_lib, abi, pkg, form):
     dut.close()
 
 
-@pytest.mark.parametrize("form", ["split_df", "split_defect"])
+@pytest.mark.parametrize("form", ["split", "split_df", "split_defect"])
 def test_split_long_run_against_fp64_gpu(gpu_lib, abi, pkg, form):
     """300 steps of a 48^3 heterogeneous rate-injection grid at the reference
     ini's compressibilities (1e-4, 1e-8), where the defects carry a large
