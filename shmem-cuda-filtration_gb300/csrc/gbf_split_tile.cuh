@@ -38,10 +38,10 @@ __device__ __forceinline__ GbfDF df_mul(GbfDF a, GbfDF b) {
 }
 // a / b for an FP32 divisor: one correction of the FP32 quotient.
 __device__ __forceinline__ GbfDF df_div_f(GbfDF a, float b) {
-  float q1 = a.hi / b;
-  float p = q1 * b, pe = fmaf(q1, b, -p);
-  float r = ((a.hi - p) - pe) + a.lo;
-  return df_fast_two_sum(q1, r / b);
+  const float q1 = __fdiv_rn(a.hi, b);
+  const float p = __fmul_rn(q1, b), pe = __fmaf_rn(q1, b, -p);
+  const float r = __fadd_rn(__fsub_rn(__fsub_rn(a.hi, p), pe), a.lo);
+  return df_fast_two_sum(q1, __fdiv_rn(r, b));
 }
 __host__ __device__ __forceinline__ float2 gbf_df_from_double(double d) {
   float h = (float)d;
@@ -103,16 +103,17 @@ template <> struct Wide<true> {
   // high part plus the low part's product) and the large terms cancelled
   // by TwoSum before any rounding: rho (1 - S) - M of cpu.cpp:305.
   static __device__ __forceinline__ float rho_1mS_minus(T rho, T M, float S) {
-    const GbfDF a = df_two_sum(rho.hi, -M.hi);          // rho - M (high parts, exact)
-    const float p = rho.hi * S, pe = fmaf(rho.hi, S, -p);  // rho.hi S, exact
+    const GbfDF a = df_two_sum(rho.hi, -M.hi);                 // rho - M (high parts, exact)
+    const float p = __fmul_rn(rho.hi, S), pe = __fmaf_rn(rho.hi, S, -p);  // rho.hi S, exact
     const GbfDF b = df_two_sum(a.hi, -p);
-    return b.hi + (b.lo + ((a.lo - pe) + (rho.lo - M.lo) - rho.lo * S));
+    return __fadd_rn(b.hi, __fadd_rn(b.lo, __fmaf_rn(-rho.lo, S, __fadd_rn(__fsub_rn(a.lo, pe),
+                                                                            __fsub_rn(rho.lo, M.lo)))));
   }
   // rho S - M rounded to FP32 (cpu.cpp:306 without the small beta terms).
   static __device__ __forceinline__ float rhoS_minus(T rho, T M, float S) {
-    const float p = rho.hi * S, pe = fmaf(rho.hi, S, -p);
+    const float p = __fmul_rn(rho.hi, S), pe = __fmaf_rn(rho.hi, S, -p);
     const GbfDF b = df_two_sum(p, -M.hi);
-    return b.hi + (b.lo + ((pe - M.lo) + rho.lo * S));
+    return __fadd_rn(b.hi, __fadd_rn(b.lo, __fmaf_rn(rho.lo, S, __fsub_rn(pe, M.lo))));
   }
   // acc + phi v, the product's rounding error kept
   static __device__ __forceinline__ T acc_phi(T acc, float phi, T v) {
@@ -298,6 +299,58 @@ __device__ __forceinline__ float split_ex2(float x) {
   return y;
 }
 
+// ----------------------------------------------------------- lane vectors
+// The per-cell arithmetic below runs on N = 1 lane (float: the 32-wide tiles)
+// or N = 2 lanes (float2: the two cells of an x-pair thread, on Blackwell's
+// paired FP32 instructions, one instruction for both cells). Every operation
+// is rounded explicitly (__fadd_rn, __fmul_rn, __fmaf_rn and their x2 forms,
+// which round each lane as the scalar ones do), so that both widths give each
+// cell the same bits. The assembler fuses a paired product that feeds a
+// paired add into one paired FMA whatever the rounding suffix (measured on
+// GB300), so the code below never lets a paired product (vmul) feed an add:
+// a product and a sum are written as one explicit FMA (vfma, the same in
+// both widths), and a product that must stay exactly rounded (a face flux
+// carried to the next plane, the products of TwoSum) is taken lane by lane
+// with the scalar __fmul_rn, which is never fused. Paired products feed
+// multiplications, FMA operands and comparisons only.
+template <int N> struct Lanes;
+template <> struct Lanes<1> {
+  using F = float;
+  static __device__ __forceinline__ F splat(float x) { return x; }
+  static __device__ __forceinline__ float get(F a, int) { return a; }
+  template <class Fn> static __device__ __forceinline__ F make(Fn f) { return f(0); }
+};
+template <> struct Lanes<2> {
+  using F = float2;
+  static __device__ __forceinline__ F splat(float x) { return make_float2(x, x); }
+  static __device__ __forceinline__ float get(F a, int n) { return n ? a.y : a.x; }
+  template <class Fn> static __device__ __forceinline__ F make(Fn f) { return make_float2(f(0), f(1)); }
+};
+__device__ __forceinline__ float vadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float vsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float vmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float vfma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ float vneg(float a) { return -a; }
+__device__ __forceinline__ float vabs(float a) { return fabsf(a); }
+__device__ __forceinline__ float2 vneg(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 vabs(float2 a) { return make_float2(fabsf(a.x), fabsf(a.y)); }
+__device__ __forceinline__ float2 vadd(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 vsub(float2 a, float2 b) { return __fadd2_rn(a, vneg(b)); }
+__device__ __forceinline__ float2 vmul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+// Lane by lane exactly rounded products (never fused into a later add).
+__device__ __forceinline__ float vmul_exact(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float2 vmul_exact(float2 a, float2 b) {
+  return make_float2(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y));
+}
+__device__ __forceinline__ float2 vfma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+
+// 1 / x (PTX rcp.approx, flush-to-zero; about 1 ulp).
+__device__ __forceinline__ float split_rcp(float x) {
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
 // Mobility x density of both phases at one cell (FP32): Brooks-Corey kr
 // (cpu.cpp:60-62) from one log2 and two exp2, Xi = -K kr / mu, densities at
 // P2 = P1 (cpu.cpp:63, 72-73).
@@ -328,9 +381,9 @@ __device__ __forceinline__ float split_face(float x, float Lminus, float Lplus) 
 
 // Brooks-Corey capillary pressure P_d S_e^(-1/lambda) and its S-derivative (cpu.cpp:303-308).
 __device__ __forceinline__ float split_Pk(const GbfSplitConsts& C, int md, float S, float& dPk_dS) {
-  const float Se = fmaf(S, C.se_b[md], 1.f);
-  const float Pk = C.P_d[md] * split_ex2(C.m_inv_lam[md] * split_lg2(Se));
-  dPk_dS = __fdividef(Pk * C.inv_lam_1mswr[md], Se);
+  const float Se = __fmaf_rn(S, C.se_b[md], 1.f);
+  const float Pk = __fmul_rn(C.P_d[md], split_ex2(__fmul_rn(C.m_inv_lam[md], split_lg2(Se))));
+  dPk_dS = __fmul_rn(__fmul_rn(Pk, C.inv_lam_1mswr[md]), split_rcp(Se));
   return Pk;
 }
 
@@ -348,40 +401,59 @@ struct GbfSplitAcc {  // kMassF64, kMassDF: phi T in the wide type
     b = W::tod(m2);
   }
 };
-// The defect forms: sum phi S as an FP32 pair, TwoSum (Knuth) into the high
-// part with the exact errors (and those of the products phi S) in the low
-// part, so that it keeps its relative precision however small it is (the
-// DNAPL of the first steps); sum phi D1 and sum phi (D2 + rho02 beta2 P_k S)
-// in the defects' type DT (FP32: small terms). c1, c2: the densities of
-// the thread's row (a thread keeps one row j). The phase masses are
-// -c1 sum phi S + sum phi D1 (the grid's c1-weighted porosity sum,
-// gbf_defect_k1, is added once per grid) and c2 sum phi S + sum phi (D2 + ...).
-template <typename DT>
-struct GbfDefectAcc {
-  float sS, lS;
-  DT b1, b2;
+// The FP32 defect form, per lane (.x: a thread's first cell, .y: the second
+// cell of an x-pair thread): sum phi S as an FP32 pair, TwoSum (Knuth) into
+// the high part with the exact errors (and those of the products phi S) in
+// the low part, so that it keeps its relative precision however small it is
+// (the DNAPL of the first steps); sum phi D1 and sum phi (D2 + rho02 beta2
+// P_k S) in FP32 (small terms). c1, c2: the densities of the thread's row (a
+// thread keeps one row j). The phase masses are -c1 sum phi S + sum phi D1
+// (the grid's c1-weighted porosity sum, gbf_defect_k1, is added once per
+// grid) and c2 sum phi S + sum phi (D2 + ...).
+template <>
+struct GbfSplitAcc<kMassDefect> {
+  float2 sS, lS;  // per lane
+  float b1, b2;   // both lanes
   float c1, c2;
   float cfl1, cfl2;
   unsigned bad;
-  __device__ GbfDefectAcc() : sS(0.f), lS(0.f), b1(0), b2(0), c1(0.f), c2(0.f), cfl1(0.f), cfl2(0.f), bad(0) {}
-  // phi = ph + pl (pl: the low part of a media-table porosity)
-  __device__ __forceinline__ void add(float ph, float pl, float S, DT D1, DT D2q) {
-    const float p = ph * S, pe = fmaf(pl, S, fmaf(ph, S, -p));
-    const float s = sS + p;
-    const float bb = s - sS;
-    lS += ((sS - (s - bb)) + (p - bb)) + pe;
+  __device__ GbfSplitAcc()
+      : sS{0.f, 0.f}, lS{0.f, 0.f}, b1(0.f), b2(0.f), c1(0.f), c2(0.f), cfl1(0.f), cfl2(0.f), bad(0) {}
+  // phi = ph + pl (pl: the low part of a media-table porosity, has_pl)
+  template <class F>
+  static __device__ __forceinline__ void step(F& sS, F& lS, F ph, F pl, F S, bool has_pl) {
+    const F p = vmul_exact(ph, S);  // TwoSum needs it rounded in every use
+    F pe = vfma(ph, S, vneg(p));
+    if (has_pl) pe = vfma(pl, S, pe);
+    const F s = vadd(sS, p);
+    const F bb = vsub(s, sS);
+    lS = vadd(lS, vadd(vadd(vsub(sS, vsub(s, bb)), vsub(p, bb)), pe));
     sS = s;
-    b1 += (DT)ph * D1;
-    b2 += (DT)ph * D2q;
+  }
+  __device__ __forceinline__ void add(float2 ph, float2 pl, float2 S, float2 D1, float2 D2q, bool has_pl) {
+    step(sS, lS, ph, pl, S, has_pl);
+    b1 = __fmaf_rn(ph.y, D1.y, __fmaf_rn(ph.x, D1.x, b1));
+    b2 = __fmaf_rn(ph.y, D2q.y, __fmaf_rn(ph.x, D2q.x, b2));
+  }
+  __device__ __forceinline__ void add(float ph, float pl, float S, float D1, float D2q, bool has_pl) {
+    step(sS.x, lS.x, ph, pl, S, has_pl);
+    b1 = __fmaf_rn(ph, D1, b1);
+    b2 = __fmaf_rn(ph, D2q, b2);
+  }
+  __device__ __forceinline__ void add_lane(int n, float ph, float pl, float S, float D1, float D2q, bool has_pl) {
+    if (n)
+      step(sS.y, lS.y, ph, pl, S, has_pl);
+    else
+      step(sS.x, lS.x, ph, pl, S, has_pl);
+    b1 = __fmaf_rn(ph, D1, b1);
+    b2 = __fmaf_rn(ph, D2q, b2);
   }
   __device__ __forceinline__ void masses(double& a, double& b) const {
-    const double S = (double)sS + (double)lS;
-    a = (double)b1 - (double)c1 * S;
-    b = (double)c2 * S + (double)b2;
+    const double S = __dadd_rn(__dadd_rn((double)sS.x, (double)lS.x), __dadd_rn((double)sS.y, (double)lS.y));
+    a = __dsub_rn((double)b1, __dmul_rn((double)c1, S));
+    b = __dadd_rn(__dmul_rn((double)c2, S), (double)b2);
   }
 };
-template <>
-struct GbfSplitAcc<kMassDefect> : GbfDefectAcc<float> {};
 // Pair defects: sum phi D1 and sum phi (D2 + ...) as FP32 pairs (each
 // product's rounding error kept, TwoSum into the high part).
 template <>
@@ -405,9 +477,9 @@ struct GbfSplitAcc<kMassDefectDF> {
     b2.lo = fmaf(pl, D2q.hi, b2.lo);
   }
   __device__ __forceinline__ void masses(double& a, double& b) const {
-    const double S = (double)sS + (double)lS;
-    a = Wide<true>::tod(b1) - (double)c1 * S;
-    b = (double)c2 * S + Wide<true>::tod(b2);
+    const double S = __dadd_rn((double)sS, (double)lS);
+    a = __dsub_rn(Wide<true>::tod(b1), __dmul_rn((double)c1, S));
+    b = __dadd_rn(__dmul_rn((double)c2, S), Wide<true>::tod(b2));
   }
 };
 
@@ -458,13 +530,14 @@ __device__ __forceinline__ unsigned split_row_flags(const GbfSplitConsts& C, int
 // FP32 increment Newton. Wide forms: targets T = M + dm in the wide type, the
 // residual split into its exact large part and FP32 small parts. Defect form:
 // the residual and the new defects from FP32 operations on small numbers
-// (rw: the row's densities). Every operation is applied lane by lane in the
-// same order, so that N = 1 and N = 2 (two cells interleaved for
-// instruction-level parallelism) give each cell the same bits; the rare
-// branches (rate source, second Newton iteration) run for all lanes when any
-// lane needs them and select per lane. Lanes with count[n] false are
-// computed but neither added to the mass sums nor checked for non-finite
-// values.
+// (rw: the row's densities). The arithmetic runs on lane vectors (Lanes<N>:
+// one instruction for both cells of an x-pair thread where the two cells do
+// the same operation) with explicit roundings, so that N = 1 and N = 2 give
+// each cell the same bits; the x faces (a pair's middle face is one value),
+// the upwind selections, the MUFU functions and the rare branches (rate
+// source, second Newton iteration) run lane by lane. Lanes with count[n]
+// false are computed but neither added to the mass sums nor checked for
+// non-finite values.
 template <int MR, int N, bool CFL = false>
 __device__ __forceinline__ void split_cells(const GbfSplitConsts& C, const GbfCellIn (&in)[N],
                                             const typename MassRep<MR>::T (&M1)[N],
@@ -474,54 +547,100 @@ __device__ __forceinline__ void split_cells(const GbfSplitConsts& C, const GbfCe
                                             const bool (&count)[N], GbfSplitAcc<MR>& acc, GbfCellOut<MR> (&o)[N]) {
   using W = WideOf<MR>;
   using WT = typename W::T;
+  using L = Lanes<N>;
+  using F = typename L::F;
   constexpr bool DEF = gbf_is_defect(MR);
-  using MT = typename MassRep<MR>::T;
   const bool noflow = rowf & 1u;
-  float Pp[N], dm1[N], dm2[N];
-  WT T1[N], T2[N];
+  auto sp = [](float x) { return L::splat(x); };
+  // the upwinded face flux of split_face on lane vectors
+  // upwind mobility of a face with potential x (split_face), and the face
+  // flux as a paired product (FMA operands only) or exactly rounded
+  auto upw = [](F x, F Lm, F Lp) {
+    return L::make([&](int n) { return L::get(x, n) >= 0.f ? L::get(Lm, n) : L::get(Lp, n); });
+  };
+  auto vface = [&](F x, F Lm, F Lp) { return vmul(x, upw(x, Lm, Lp)); };
+  auto vface_exact = [&](F x, F Lm, F Lp) { return vmul_exact(x, upw(x, Lm, Lp)); };
+  const F dPc = L::make([&](int n) { return in[n].dPc; });
+  const F S0 = L::make([&](int n) { return in[n].S0; });
+  const F L1c = L::make([&](int n) { return in[n].L1c; });
+  const F L2c = L::make([&](int n) { return in[n].L2c; });
+  // x faces lane by lane (the pair's middle face is one value for both
+  // cells): flux differences in - out of both phases
+  float ax1[N], ax2[N], bx1[N], bx2[N], dx1[N], dx2[N];
 #pragma unroll
   for (int n = 0; n < N; n++) {
-    const float dPc = in[n].dPc, L1c = in[n].L1c, L2c = in[n].L2c;
-    // face potentials relative to the hydrostatic profile (P2 = P1), times h:
-    // pressure differences, gravity terms scaled by h2
-    const float x1 = in[n].dPxm - dPc, x2 = dPc - in[n].dPxp;
-    const float yb1 = in[n].dPym - dPc;
-    const float yb2 = dPc - in[n].dPyp;
-    const float z2 = dPc - in[n].dPp;
-    Pp[n] = fmaf((float)j, C.H, dPc);  // P - P_atm
-    const float gd1 = C.gh1 * Pp[n];  // (rho1 - rho01) g h2
-    const float gd2 = fmaf(C.gh2, Pp[n], C.ghd);
-    const float y11 = yb1 + gd1, y21 = noflow ? 0.f : yb2 + gd1;
-    const float y12 = yb1 + gd2, y22 = noflow ? 0.f : yb2 + gd2;
-    // face fluxes, in through the minus face and out through the plus face
-    const float ax1 = split_face(x1, in[n].L1xm, L1c), ax2 = split_face(x2, L1c, in[n].L1xp);
-    const float ay1 = split_face(y11, in[n].L1ym, L1c), ay2 = split_face(y21, L1c, in[n].L1yp);
-    const float az1 = in[n].fz1, az2 = split_face(z2, L1c, in[n].L1p);
-    const float bx1 = split_face(x1, in[n].L2xm, L2c), bx2 = split_face(x2, L2c, in[n].L2xp);
-    const float by1 = split_face(y12, in[n].L2ym, L2c), by2 = split_face(y22, L2c, in[n].L2yp);
-    const float bz1 = in[n].fz2, bz2 = split_face(z2, L2c, in[n].L2p);
-    o[n].fz1 = az2;
-    o[n].fz2 = bz2;
-    // dt times the flux divergence: sum over directions of (in - out) dt / h^2 (kv in y)
-    const float f = (ax1 - ax2) * C.wx + (ay1 - ay2) * C.wy + (az1 - az2) * C.wz;
-    const float gs = (bx1 - bx2) * C.wx + (by1 - by2) * C.wy + (bz1 - bz2) * C.wz;
-    const float rphi = __fdividef(1.f, in[n].phi);
-    dm1[n] = -f * rphi;  // FP32 mass increments
-    dm2[n] = -gs * rphi;
-    if (CFL && count[n]) {
-      // CFL number of each phase: the largest face volumetric flux of the cell
-      // (mass flux x L_upwind over the reference density) times dt / (phi h)
-      // (the mobilities L are <= 0: magnitudes by fabsf)
-      const float c1 = fmaxf(fmaxf(fmaxf(fabsf(ax1), fabsf(ax2)) * C.wx, fmaxf(fabsf(ay1), fabsf(ay2)) * C.wy),
-                             fmaxf(fabsf(az1), fabsf(az2)) * C.wz);
-      const float c2 = fmaxf(fmaxf(fmaxf(fabsf(bx1), fabsf(bx2)) * C.wx, fmaxf(fabsf(by1), fabsf(by2)) * C.wy),
-                             fmaxf(fabsf(bz1), fabsf(bz2)) * C.wz);
-      acc.cfl1 = fmaxf(acc.cfl1, c1 * rphi * C.cfl1);
-      acc.cfl2 = fmaxf(acc.cfl2, c2 * rphi * C.cfl2);
-    }
-    if constexpr (!DEF) {  // mass targets T = M + dm (wide)
-      T1[n] = W::add_f(M1[n], dm1[n]);
-      T2[n] = W::add_f(M2[n], dm2[n]);
+    const float x1 = __fsub_rn(in[n].dPxm, in[n].dPc), x2 = __fsub_rn(in[n].dPc, in[n].dPxp);
+    ax1[n] = split_face(x1, in[n].L1xm, in[n].L1c);
+    ax2[n] = split_face(x2, in[n].L1c, in[n].L1xp);
+    bx1[n] = split_face(x1, in[n].L2xm, in[n].L2c);
+    bx2[n] = split_face(x2, in[n].L2c, in[n].L2xp);
+    dx1[n] = __fsub_rn(ax1[n], ax2[n]);
+    dx2[n] = __fsub_rn(bx1[n], bx2[n]);
+  }
+  // y and z face potentials relative to the hydrostatic profile (P2 = P1),
+  // times h: pressure differences, gravity terms scaled by h2
+  const F Pp = vfma(sp((float)j), sp(C.H), dPc);  // P - P_atm
+  const F gd2 = vfma(sp(C.gh2), Pp, sp(C.ghd));     // (rho2 - rho01) g h2
+  const F yb1 = vsub(L::make([&](int n) { return in[n].dPym; }), dPc);
+  const F yb2 = vsub(dPc, L::make([&](int n) { return in[n].dPyp; }));
+  const F z2 = vsub(dPc, L::make([&](int n) { return in[n].dPp; }));
+  // + (rho1 - rho01) g h2 = gh1 Pp
+  const F y11 = vfma(sp(C.gh1), Pp, yb1), y12 = vadd(yb1, gd2);
+  const F y21 = noflow ? sp(0.f) : vfma(sp(C.gh1), Pp, yb2), y22 = noflow ? sp(0.f) : vadd(yb2, gd2);
+  // face fluxes, in through the minus face and out through the plus face:
+  // the plus face's upwinded product, the minus face's inside the FMA of the
+  // difference; the z face's out-flux exactly rounded (carried to the next
+  // plane as its in-flux)
+  const F L1ym = L::make([&](int n) { return in[n].L1ym; }), L2ym = L::make([&](int n) { return in[n].L2ym; });
+  const F ay2 = vface(y21, L1c, L::make([&](int n) { return in[n].L1yp; }));
+  const F by2 = vface(y22, L2c, L::make([&](int n) { return in[n].L2yp; }));
+  const F az2 = vface_exact(z2, L1c, L::make([&](int n) { return in[n].L1p; }));
+  const F bz2 = vface_exact(z2, L2c, L::make([&](int n) { return in[n].L2p; }));
+  const F az1 = L::make([&](int n) { return in[n].fz1; });
+  const F bz1 = L::make([&](int n) { return in[n].fz2; });
+#pragma unroll
+  for (int n = 0; n < N; n++) {
+    o[n].fz1 = L::get(az2, n);
+    o[n].fz2 = L::get(bz2, n);
+  }
+  const F dy1 = vfma(y11, upw(y11, L1ym, L1c), vneg(ay2));  // ay1 - ay2
+  const F dy2 = vfma(y12, upw(y12, L2ym, L2c), vneg(by2));
+  // dt times the flux divergence: sum over directions of (in - out) dt / h^2
+  // (kv in y), then the FP32 mass increments -(..) / phi
+  const F f = vfma(vsub(az1, az2), sp(C.wz),
+                   vfma(dy1, sp(C.wy), vmul(L::make([&](int n) { return dx1[n]; }), sp(C.wx))));
+  const F gs = vfma(vsub(bz1, bz2), sp(C.wz),
+                    vfma(dy2, sp(C.wy), vmul(L::make([&](int n) { return dx2[n]; }), sp(C.wx))));
+  const F nrphi = L::make([&](int n) { return split_rcp(-in[n].phi); });  // -1 / phi
+  const F dm1 = vmul(f, nrphi), dm2 = vmul(gs, nrphi);  // FMA addends only
+  if (CFL) {
+#pragma unroll
+    for (int n = 0; n < N; n++)
+      if (count[n]) {
+        // CFL number of each phase: the largest face volumetric flux of the
+        // cell (mass flux x L_upwind over the reference density) times
+        // dt / (phi h) (the mobilities L are <= 0: magnitudes by fabsf)
+        const float ay1 = split_face(L::get(y11, n), in[n].L1ym, in[n].L1c);
+        const float ay2n = split_face(L::get(y21, n), in[n].L1c, in[n].L1yp);
+        const float by1 = split_face(L::get(y12, n), in[n].L2ym, in[n].L2c);
+        const float by2n = split_face(L::get(y22, n), in[n].L2c, in[n].L2yp);
+        const float c1 = fmaxf(fmaxf(__fmul_rn(fmaxf(fabsf(ax1[n]), fabsf(ax2[n])), C.wx),
+                                     __fmul_rn(fmaxf(fabsf(ay1), fabsf(ay2n)), C.wy)),
+                               __fmul_rn(fmaxf(fabsf(L::get(az1, n)), fabsf(L::get(az2, n))), C.wz));
+        const float c2 = fmaxf(fmaxf(__fmul_rn(fmaxf(fabsf(bx1[n]), fabsf(bx2[n])), C.wx),
+                                     __fmul_rn(fmaxf(fabsf(by1), fabsf(by2n)), C.wy)),
+                               __fmul_rn(fmaxf(fabsf(L::get(bz1, n)), fabsf(L::get(bz2, n))), C.wz));
+        const float rphi = -L::get(nrphi, n);
+        acc.cfl1 = fmaxf(acc.cfl1, __fmul_rn(__fmul_rn(c1, rphi), C.cfl1));
+        acc.cfl2 = fmaxf(acc.cfl2, __fmul_rn(__fmul_rn(c2, rphi), C.cfl2));
+      }
+  }
+  WT T1[N], T2[N];
+  if constexpr (!DEF) {  // mass targets T = M + dm (wide)
+#pragma unroll
+    for (int n = 0; n < N; n++) {
+      T1[n] = W::add_f(M1[n], __fmul_rn(L::get(f, n), L::get(nrphi, n)));  // exactly rounded dm
+      T2[n] = W::add_f(M2[n], __fmul_rn(L::get(gs, n), L::get(nrphi, n)));
     }
   }
   // the rate source, added exactly (defect form: its FP32 high and low parts)
@@ -567,92 +686,163 @@ __device__ __forceinline__ void split_cells(const GbfSplitConsts& C, const GbfCe
   // equations are linear up to terms beta (dp ds, P_k'' ds^2): after the
   // first (linear) iteration the residual is about rho0 beta |dp ds|; a
   // second iteration runs when that could move S by more than 1e-9.
-  float r1[N], r2[N], a0[N], b0[N], Pk0[N], dPk0[N], dp[N], ds[N], Pk[N];
+  // Capillary pressure P_d S_e^(-1/lambda) and its S-derivative (split_Pk).
+  const F Se = vfma(S0, sp(C.se_b[md]), sp(1.f));
+  const F lSe = L::make([&](int n) { return split_lg2(L::get(Se, n)); });
+  const F exS = vmul(sp(C.m_inv_lam[md]), lSe);
+  const F eS = L::make([&](int n) { return split_ex2(L::get(exS, n)); });
+  const F Pk0 = vmul(sp(C.P_d[md]), eS);  // FMA operands only; its sums below are FMAs
+  const F dPk0 = vmul(vmul(Pk0, sp(C.inv_lam_1mswr[md])), L::make([&](int n) { return split_rcp(L::get(Se, n)); }));
+  const F PpPk = vfma(sp(C.P_d[md]), eS, Pp);  // P' + P_k
+  const F omS = vsub(sp(1.f), S0);
+  F r1, r2;
+  if constexpr (DEF) {
+    const F D1 = L::make([&](int n) { return defect_f(M1[n]); });
+    const F D2 = L::make([&](int n) { return defect_f(M2[n]); });
+    // - dm = + f / phi inside the FMA
+    r1 = vfma(vneg(f), nrphi, vfma(vfma(sp(C.ro01b1), dPc, sp(rw.e1)), omS, vneg(D1)));
+    r2 = vsub(vfma(vneg(gs), nrphi,
+                   vfma(vfma(sp(C.ro02b2), vfma(sp(C.P_d[md]), eS, dPc), sp(rw.e2)), S0, vneg(D2))),
+              L::make([&](int n) { return srcf[n]; }));
+  } else {
+    r1 = L::make([&](int n) {
+      return __fmaf_rn(-L::get(f, n), L::get(nrphi, n),
+                       __fmaf_rn(__fmul_rn(C.ro01b1, L::get(Pp, n)), L::get(omS, n),
+                                 W::rho_1mS_minus(R01, M1[n], in[n].S0)));
+    });
+    r2 = L::make([&](int n) {
+      return __fsub_rn(__fmaf_rn(-L::get(gs, n), L::get(nrphi, n),
+                                 __fmaf_rn(__fmul_rn(C.ro02b2, L::get(PpPk, n)), in[n].S0,
+                                           W::rhoS_minus(R02, M2[n], in[n].S0))),
+                       srcf[n]);
+    });
+  }
+  const F a0 = vfma(sp(C.beta1), Pp, sp(1.f));
+  const F b0 = vfma(sp(C.beta2), PpPk, sp(1.f));
+  const F J11 = vmul(sp(C.ro01b1), omS), mJ12 = vmul(sp(C.ro01), a0);  // J12 = -mJ12
+  const F J21 = vmul(sp(C.ro02b2), S0), J22 = vmul(sp(C.ro02), vfma(vmul(sp(C.beta2), dPk0), S0, b0));
+  const F ninv = L::make([&](int n) { return split_rcp(-L::get(vfma(J11, J22, vmul(mJ12, J21)), n)); });
+  const F tp = vfma(J22, r1, vmul(mJ12, r2));       // J22 r1 - J12 r2
+  const F ts = vfma(J11, r2, vneg(vmul(J21, r1)));  // J11 r2 - J21 r1
+  const F dp = vmul(ninv, tp), ds = vmul(ninv, ts);  // the first step (FMA operands only)
+  const F nl = vmul(vmul(sp(C.bmax), vabs(ds)), vadd(vfma(sp(4.f), vabs(vmul(dPk0, ds)), vabs(dp)), sp(1.f)));
+  F Pk = vfma(dPk0, ds, Pk0);
   bool need[N], anyneed = false;
 #pragma unroll
   for (int n = 0; n < N; n++) {
-    const float S0 = in[n].S0;
-    Pk0[n] = split_Pk(C, md, S0, dPk0[n]);
-    if constexpr (DEF) {
-      r1[n] = fmaf(fmaf(C.ro01b1, in[n].dPc, rw.e1), 1.f - S0, -defect_f(M1[n])) - dm1[n];
-      r2[n] = fmaf(fmaf(C.ro02b2, in[n].dPc + Pk0[n], rw.e2), S0, -defect_f(M2[n])) - dm2[n] - srcf[n];
-    } else {
-      r1[n] = W::rho_1mS_minus(R01, M1[n], S0) + C.ro01b1 * Pp[n] * (1.f - S0) - dm1[n];
-      r2[n] = W::rhoS_minus(R02, M2[n], S0) + C.ro02b2 * (Pp[n] + Pk0[n]) * S0 - dm2[n] - srcf[n];
-    }
-    a0[n] = fmaf(C.beta1, Pp[n], 1.f);
-    b0[n] = fmaf(C.beta2, Pp[n] + Pk0[n], 1.f);
-    const float J11 = C.ro01b1 * (1.f - S0), J12 = -C.ro01 * a0[n];
-    const float J21 = C.ro02b2 * S0, J22 = C.ro02 * fmaf(C.beta2 * dPk0[n], S0, b0[n]);
-    const float inv = __fdividef(1.f, J11 * J22 - J12 * J21);
-    dp[n] = -inv * (J22 * r1[n] - J12 * r2[n]);
-    ds[n] = -inv * (J11 * r2[n] - J21 * r1[n]);
-    const float nl = C.bmax * fabsf(ds[n]) * (fabsf(dp[n]) + 4.f * fabsf(dPk0[n] * ds[n]) + 1.f);
-    need[n] = nl > 1e-9f;
+    need[n] = L::get(nl, n) > 1e-9f;
     anyneed |= need[n];
-    Pk[n] = fmaf(dPk0[n], ds[n], Pk0[n]);
   }
+  // the new state: the first step inside one FMA each
+  F dPn = vfma(ninv, tp, dPc), Sn = vfma(ninv, ts, S0);
   if (anyneed) {
+    float dpn[N], dsn[N], Pkn[N];
 #pragma unroll
     for (int n = 0; n < N; n++) {
-      const float S0 = in[n].S0;
+      // from the state the first step reached: its increments as applied
+      const float s0 = in[n].S0, pk0 = __fmul_rn(C.P_d[md], L::get(eS, n));
+      const float p = __fsub_rn(L::get(dPn, n), in[n].dPc), s = __fsub_rn(L::get(Sn, n), s0);
+      // a0, b0 of this lane again (the same operations), not kept across the branch
+      const float Ppn = __fmaf_rn((float)j, C.H, in[n].dPc);
+      const float a = __fmaf_rn(C.beta1, Ppn, 1.f);
+      const float b = __fmaf_rn(C.beta2, __fmaf_rn(C.P_d[md], L::get(eS, n), Ppn), 1.f);
       float dPk1;
-      const float Pk1 = split_Pk(C, md, S0 + ds[n], dPk1);
-      const float S1 = S0 + ds[n];
-      const float G1 = r1[n] + C.ro01 * (C.beta1 * dp[n] * (1.f - S1) - a0[n] * ds[n]);
-      const float G2 = r2[n] + C.ro02 * (b0[n] * ds[n] + C.beta2 * (dp[n] + (Pk1 - Pk0[n])) * S1);
-      const float J11 = C.ro01b1 * (1.f - S1);
-      const float J12 = -C.ro01 * (a0[n] + C.beta1 * dp[n]);
-      const float J21 = C.ro02b2 * S1;
-      const float J22 = C.ro02 * (b0[n] + C.beta2 * (dp[n] + (Pk1 - Pk0[n])) + C.beta2 * dPk1 * S1);
-      const float inv = __fdividef(1.f, J11 * J22 - J12 * J21);
-      const float ep = inv * (J22 * G1 - J12 * G2);
-      const float es = inv * (J11 * G2 - J21 * G1);
-      if (need[n]) {
-        dp[n] -= ep;
-        ds[n] -= es;
-        Pk[n] = fmaf(-dPk1, es, Pk1);  // P_k at the final S, to first order in the last correction
-      }
+      const float S1 = __fadd_rn(s0, s);
+      const float Pk1 = split_Pk(C, md, S1, dPk1);
+      const float dpk = __fadd_rn(p, __fsub_rn(Pk1, pk0));
+      const float G1 =
+          __fmaf_rn(C.ro01, __fmaf_rn(-a, s, __fmul_rn(__fmul_rn(C.beta1, p), __fsub_rn(1.f, S1))), L::get(r1, n));
+      const float G2 = __fmaf_rn(C.ro02, __fmaf_rn(b, s, __fmul_rn(__fmul_rn(C.beta2, dpk), S1)), L::get(r2, n));
+      const float K11 = __fmul_rn(C.ro01b1, __fsub_rn(1.f, S1));
+      const float mK12 = __fmul_rn(C.ro01, __fmaf_rn(C.beta1, p, a));
+      const float K21 = __fmul_rn(C.ro02b2, S1);
+      const float K22 = __fmul_rn(C.ro02, __fmaf_rn(__fmul_rn(C.beta2, dPk1), S1, __fmaf_rn(C.beta2, dpk, b)));
+      const float inv = split_rcp(__fmaf_rn(K11, K22, __fmul_rn(mK12, K21)));
+      const float ep = __fmul_rn(inv, __fmaf_rn(K22, G1, __fmul_rn(mK12, G2)));
+      const float es = __fmul_rn(inv, __fmaf_rn(K11, G2, -__fmul_rn(K21, G1)));
+      dpn[n] = need[n] ? __fadd_rn(in[n].dPc, __fsub_rn(p, ep)) : L::get(dPn, n);
+      dsn[n] = need[n] ? __fadd_rn(s0, __fsub_rn(s, es)) : L::get(Sn, n);
+      // P_k at the final S, to first order in the last correction
+      Pkn[n] = need[n] ? __fmaf_rn(-dPk1, es, Pk1) : L::get(Pk, n);
     }
+    dPn = L::make([&](int n) { return dpn[n]; });
+    Sn = L::make([&](int n) { return dsn[n]; });
+    Pk = L::make([&](int n) { return Pkn[n]; });
   }
+  const F fin = vadd(dPn, Sn);  // NaN and infinities carry through the sum
 #pragma unroll
   for (int n = 0; n < N; n++) {
-    o[n].dPn = in[n].dPc + dp[n];
-    o[n].Sn = in[n].S0 + ds[n];
-    if constexpr (DEF) {
-      // new defects: D1 + dm1 + c1 dS and D2 + dm2 + src - c2 dS - rho02 beta2 P_k S,
-      // with dS the stored change of S and c dS against the increment it
-      // balances inside one FMA (exact product, one rounding of a small sum)
-      const float dse = o[n].Sn - in[n].S0;
-      const float q = C.ro02b2 * Pk[n] * o[n].Sn;  // next step's ro2 S2 is taken without P_k (cpu.cpp:63 vs :306)
-      o[n].M1n = defect_add(M1[n], fmaf(rw.c1, dse, dm1[n]));
-      float u = fmaf(-rw.c2, dse, dm2[n]);
-      if (anysrc && insrc[n]) u = fmaf(-rw.c2, dse, srcf[n]) + (dm2[n] + srcl[n]);
-      o[n].M2n = defect_add(M2[n], u - q);
-      if (count[n]) {
-        if (mass) {  // phi T with T1 = c1 (1 - S) + D1, T2 = c2 S + D2 + q
-          const float ph = phi_field ? in[n].phi : C.m_df[md].x;
-          const float pl = phi_field ? 0.f : C.m_df[md].y;
-          acc.add(ph, pl, o[n].Sn, o[n].M1n, defect_add(o[n].M2n, q));
-        }
-        if (!isfinite(o[n].dPn + o[n].Sn)) acc.bad = 1;  // NaN and infinities carry through the sum
+    o[n].dPn = L::get(dPn, n);
+    o[n].Sn = L::get(Sn, n);
+    if (count[n] && !isfinite(L::get(fin, n))) acc.bad = 1;
+  }
+  if constexpr (DEF) {
+    // new defects: D1 + dm1 + c1 dS and D2 + dm2 + src - c2 dS - rho02 beta2 P_k S,
+    // with dS the stored change of S and c dS against the increment it
+    // balances inside one FMA (exact product, one rounding of a small sum)
+    const F dse = vsub(Sn, S0);
+    // q = rho02 beta2 P_k S: next step's ro2 S2 is taken without P_k
+    // (cpu.cpp:63 vs :306); qa S inside the FMAs that subtract or add it
+    const F qa = vmul(sp(C.ro02b2), Pk);
+    const F i1 = vfma(sp(rw.c1), dse, dm1);
+    F u = vfma(sp(-rw.c2), dse, dm2);
+    if (anysrc)
+      u = L::make([&](int n) {
+        return insrc[n] ? __fadd_rn(__fmaf_rn(-rw.c2, L::get(dse, n), srcf[n]),
+                                    __fadd_rn(__fmul_rn(L::get(gs, n), L::get(nrphi, n)), srcl[n]))
+                        : L::get(u, n);
+      });
+    const F i2 = vfma(vneg(qa), Sn, u);  // u - q
+    if constexpr (MR == kMassDefect) {
+      const F D1n = vadd(L::make([&](int n) { return M1[n]; }), i1);
+      const F D2n = vadd(L::make([&](int n) { return M2[n]; }), i2);
+#pragma unroll
+      for (int n = 0; n < N; n++) {
+        o[n].M1n = L::get(D1n, n);
+        o[n].M2n = L::get(D2n, n);
+      }
+      if (mass) {  // phi T with T1 = c1 (1 - S) + D1, T2 = c2 S + D2 + q
+        const F ph = phi_field ? L::make([&](int n) { return in[n].phi; }) : sp(C.m_df[md].x);
+        const F pl = sp(phi_field ? 0.f : C.m_df[md].y);
+        bool all = true;
+#pragma unroll
+        for (int n = 0; n < N; n++) all = all && count[n];
+        if (all)
+          acc.add(ph, pl, Sn, D1n, vfma(qa, Sn, D2n), !phi_field);
+        else
+#pragma unroll
+          for (int n = 0; n < N; n++)
+            if (count[n])
+              acc.add_lane(n, L::get(ph, n), L::get(pl, n), L::get(Sn, n), L::get(D1n, n),
+                           __fmaf_rn(L::get(qa, n), L::get(Sn, n), L::get(D2n, n)), !phi_field);
       }
     } else {
+#pragma unroll
+      for (int n = 0; n < N; n++) {
+        o[n].M1n = defect_add(M1[n], L::get(i1, n));
+        o[n].M2n = defect_add(M2[n], L::get(i2, n));
+        if (count[n] && mass) {
+          const float ph = phi_field ? in[n].phi : C.m_df[md].x;
+          const float pl = phi_field ? 0.f : C.m_df[md].y;
+          acc.add(ph, pl, o[n].Sn, o[n].M1n, defect_add(o[n].M2n, __fmul_rn(L::get(qa, n), o[n].Sn)));
+        }
+      }
+    }
+  } else {
+#pragma unroll
+    for (int n = 0; n < N; n++) {
       o[n].M1n = T1[n];
       // next step's ro2 S2 is taken at P2 = P1, without P_k (cpu.cpp:63 vs :306)
-      o[n].M2n = W::add_f(T2[n], -C.ro02b2 * Pk[n] * o[n].Sn);
-      if (count[n]) {
-        if (mass) {  // phi T in the wide type (phi exact: an FP32 input or a wide table value)
-          if (phi_field) {
-            acc.m1 = W::acc_phi(acc.m1, in[n].phi, T1[n]);
-            acc.m2 = W::acc_phi(acc.m2, in[n].phi, T2[n]);
-          } else {
-            const WT phw = W::c(C.m_d[md], C.m_df[md]);
-            acc.m1 = W::add(acc.m1, W::mul(phw, T1[n]));
-            acc.m2 = W::add(acc.m2, W::mul(phw, T2[n]));
-          }
+      o[n].M2n = W::add_f(T2[n], __fmul_rn(__fmul_rn(-C.ro02b2, L::get(Pk, n)), o[n].Sn));
+      if (count[n] && mass) {  // phi T in the wide type (phi exact: an FP32 input or a wide table value)
+        if (phi_field) {
+          acc.m1 = W::acc_phi(acc.m1, in[n].phi, T1[n]);
+          acc.m2 = W::acc_phi(acc.m2, in[n].phi, T2[n]);
+        } else {
+          const WT phw = W::c(C.m_d[md], C.m_df[md]);
+          acc.m1 = W::add(acc.m1, W::mul(phw, T1[n]));
+          acc.m2 = W::add(acc.m2, W::mul(phw, T2[n]));
         }
-        if (!isfinite(o[n].dPn + o[n].Sn)) acc.bad = 1;  // NaN and infinities carry through the sum
       }
     }
   }
