@@ -170,9 +170,10 @@ int gbf_newton_f64(const gbf_model* m, gbf_arrays d_arrays, gbf_cells d_cells, v
 int gbf_boundary_f64(const gbf_model* m, gbf_arrays d_arrays, double* d_scratch, void* stream);
 size_t gbf_boundary_scratch_doubles(const gbf_model* m);
 /* a5 for callers that cannot allocate device memory where they apply the
-   boundary conditions: code being captured into a CUDA graph (cudaMalloc is
-   not allowed during capture), callers whose memory belongs to another
-   allocator or is budgeted up front, drivers that bring their own arrays.
+   boundary conditions: a host loop that must not stall on cudaMalloc (it
+   synchronises the device), a process whose device memory belongs to another
+   framework's caching allocator or is budgeted up front, a driver that hands
+   over only its own state arrays and no workspace.
    No counterpart in the reference. Same results as gbf_boundary_f64; its
    scratch is a fixed 8 MiB array of the library in device memory that every
    GPU loading the library keeps until exit, so it serves grids with at most

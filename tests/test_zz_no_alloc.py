@@ -1,8 +1,9 @@
 """gbf_boundary_f64_noalloc: the boundary pass for callers that cannot
-allocate device memory where they apply the boundary conditions (code being
-captured into a CUDA graph, callers whose memory belongs to another allocator
-or is budgeted up front, drivers that bring their own arrays). Its scratch is
-a fixed device array of the library instead of a caller buffer.
+allocate device memory where they apply the boundary conditions (a host loop
+that must not stall on cudaMalloc's device synchronisation, a process whose
+device memory belongs to another framework's allocator or is budgeted up
+front, a driver that hands over only its state arrays). Its scratch is a fixed
+device array of the library instead of a caller buffer.
 
 Checked through the C ABI against the allocating entry point
 gbf_boundary_f64 on the same inputs, on two calls in a row (the second call
