@@ -1264,11 +1264,14 @@ __device__ __forceinline__ void split_block_mass(const GbfSplitAcc<MR>& acc, dou
 // thread's pair sits at an even offset: its x-stencil is three 64-bit
 // shared loads, its y neighbours and the plane above two more per field.
 // The interior rows of M1, M2 and phi arrive as {TXC, TY} boxes at x0 (no
-// halo). Shared memory exceeds the static 48 KB, so the kernel takes it as
-// dynamic shared memory (GbfPairSmem).
+// halo), two planes ahead of the plane being updated (a 3-stage ring). The
+// built planes hold dP, L1 and L2 of every box cell; S is needed only at the
+// thread's own pair, which the thread builds itself and keeps in registers.
+// Shared memory exceeds the static 48 KB, so the kernel takes it as dynamic
+// shared memory (GbfPairSmem).
 // Resident 256-thread x-pair CTAs per SM: three for the defect form (80
-// registers a thread, a 2-stage rows ring: 74 KB of shared memory), two for
-// the wide forms (116-120 registers, 3 stages).
+// registers a thread, 71 KB of shared memory), two for the wide forms
+// (116-120 registers).
 __host__ __device__ constexpr int gbf_pair_ctas(int MR) { return MR == kMassDefect ? 3 : 2; }
 
 template <int TXC, int TY, int MR = kMassF64>
@@ -1276,7 +1279,7 @@ struct GbfPairRing {
   static_assert(TXC % 16 == 0 && TXC <= 248, "x-pair tile width");
   static constexpr int BX = TXC + 8, HY = TY + 2, N = BX * HY, NP = (N + 31) / 32 * 32;
   static constexpr int NR = TXC * TY;  // interior-row elements per field
-  static constexpr int RS = gbf_pair_ctas(MR) == 3 ? 2 : 3;
+  static constexpr int RS = 3;
   static constexpr unsigned MB = (unsigned)sizeof(MassElem<MR>);
   static constexpr unsigned kHaloBytes = 3u * N * 4u;
   static constexpr unsigned kRowsBytes = (unsigned)NR * (MB + MB + 4u);
@@ -1288,7 +1291,7 @@ template <int TXC, int TY, int MR = kMassF64>
 struct GbfPairSmem {
   using Ring = GbfPairRing<TXC, TY, MR>;
   Ring ring;
-  float dP[kTmaStages][Ring::NP], S[kTmaStages][Ring::NP];
+  float dP[kTmaStages][Ring::NP];
   float L1[kTmaStages][Ring::NP], L2[kTmaStages][Ring::NP];
 };
 // The mbarriers of the two rings (halo planes, interior rows), apart from the
@@ -1296,7 +1299,7 @@ struct GbfPairSmem {
 // and their parities, for both.
 template <int MR>
 struct alignas(128) GbfPairBars {
-  static constexpr int RS = gbf_pair_ctas(MR) == 3 ? 2 : 3;
+  static constexpr int RS = 3;
   unsigned long long bar[kTmaStages], mbar[RS];
 };
 // Dynamic shared memory of an x-pair CTA: barriers, then one shape's rings and
@@ -1397,23 +1400,26 @@ __device__ bool split_tile_x2(const GbfSplitConsts& C, const GbfSplitGrid& G, in
   const int mi = ty * TXC + 2 * tx;           // own pair in the rows boxes (even)
 
   // halo pairs of this thread: even plane index, global row (rows or columns
-  // outside the grid hold zeros and give finite, unused properties). The
-  // interior pairs of a row go to consecutive threads (a row's THX pairs are
-  // contiguous in shared memory: no bank conflicts), then the left and right
-  // halo pair of every row.
+  // outside the grid hold zeros and give finite, unused properties). Slot 0
+  // is the thread's own pair (box row ty + 1); then the interior pairs of the
+  // halo rows 0 and HY - 1, then the left and right halo pair of every row.
+  // The pairs of a row go to consecutive threads (a row's THX pairs are
+  // contiguous in shared memory: no bank conflicts).
+  // (slot 0 is hc in row j: only the other slots keep their positions)
   int hq[SLOTS], hj[SLOTS];
 #pragma unroll
-  for (int s = 0; s < SLOTS; s++) {
+  for (int s = 1; s < SLOTS; s++) {
     const int q = threadIdx.x + s * NT;
     hq[s] = -1;
     hj[s] = 0;
     if (in_tile && q < NPAIR) {
       int r, c2;
-      if (q < HY * THX) {
-        r = q / THX;
-        c2 = 2 + q % THX;
+      if (q < NT + 2 * THX) {
+        const int h = q - NT;
+        r = h < THX ? 0 : HY - 1;
+        c2 = 2 + h % THX;
       } else {
-        const int h = q - HY * THX;
+        const int h = q - NT - 2 * THX;
         r = h >> 1;
         c2 = (h & 1) ? PCOLS : 1;
       }
@@ -1422,11 +1428,11 @@ __device__ bool split_tile_x2(const GbfSplitConsts& C, const GbfSplitGrid& G, in
     }
   }
 
+  // Both rings have three stages: plane p uses stage (p - k0) % 3 of each, so
+  // one rotating index u = (k - k0) % 3 names every stage the loop touches.
+  static_assert(RS == kTmaStages && kTmaStages == 3, "x-pair rings");
   unsigned pend = 0;
-  int h_issue = 0, r_issue = 0;
-  auto issue = [&](int p) {
-    const int s = h_issue;
-    h_issue = s == kTmaStages - 1 ? 0 : s + 1;
+  auto issue = [&](int p, int s) {  // halo planes of plane p into stage s
     if (threadIdx.x == 0) {
       gbf_mbar_expect_tx(&bars.bar[s], Ring::kHaloBytes);
       gbf_tma_plane(raw.v[s][0], &maps->dP[buf], x0 - 4, j0 - 1, p, &bars.bar[s]);
@@ -1435,9 +1441,7 @@ __device__ bool split_tile_x2(const GbfSplitConsts& C, const GbfSplitGrid& G, in
     }
     pend |= 1u << s;
   };
-  auto issue_rows = [&](int p) {
-    const int s = r_issue;
-    r_issue = s == RS - 1 ? 0 : s + 1;
+  auto issue_rows = [&](int p, int s) {  // M1, M2, phi rows of plane p into stage s
     if (threadIdx.x == 0) {
       gbf_mbar_expect_tx(&bars.mbar[s], Ring::kRowsBytes);
       gbf_tma_plane(raw.m1[s], &maps->M1, x0, j0, p, &bars.mbar[s]);
@@ -1463,26 +1467,29 @@ __device__ bool split_tile_x2(const GbfSplitConsts& C, const GbfSplitGrid& G, in
     pend = 0;
     if (threadIdx.x == 0) atomicOr(G.status, GBF_DEV_TIMEOUT);
   };
+  float2 s_own = make_float2(0.f, 0.f);  // S of the own pair in the plane built last
   auto build = [&](int s) {  // plane buffer s from halo stage s
 #pragma unroll
     for (int q = 0; q < SLOTS; q++) {
-      if ((NT == NTB && (q + 1) * NT <= NPAIR) || hq[q] >= 0) {  // the first slots hold a pair for every thread
-        const int e = hq[q];
+      // slot 0: the own pair of every thread in the tile; the first later
+      // slots hold a pair for every thread too where the halo is large enough
+      if (q == 0 ? in_tile : ((NT == NTB && (q + 1) * NT <= NPAIR) || hq[q] >= 0)) {
+        const int e = q == 0 ? hc : hq[q], jr = q == 0 ? j : hj[q];
         const float2 p = gbf_ld2(&raw.v[s][0][e]), sv = gbf_ld2(&raw.v[s][1][e]), kv = gbf_ld2(&raw.v[s][2][e]);
         float l1a, l2a, l1b, l2b;
-        split_props(C, 0, kv.x, p.x, sv.x, hj[q], l1a, l2a);
-        split_props(C, 0, kv.y, p.y, sv.y, hj[q], l1b, l2b);
+        split_props(C, 0, kv.x, p.x, sv.x, jr, l1a, l2a);
+        split_props(C, 0, kv.y, p.y, sv.y, jr, l1b, l2b);
         gbf_st2(&sm.dP[s][e], p.x, p.y);
-        gbf_st2(&sm.S[s][e], sv.x, sv.y);
         gbf_st2(&sm.L1[s][e], l1a, l1b);
         gbf_st2(&sm.L2[s][e], l2a, l2b);
+        if (q == 0) s_own = sv;
       }
     }
   };
 
   // prologue: own pair at k0 - 1 (registers), plane k0 (shared)
-  for (int q = 0; q < kTmaStages && k0 + q <= k1; q++) issue(k0 + q);
-  for (int q = 0; q < RS && k0 + q < k1; q++) issue_rows(k0 + q);
+  for (int q = 0; q < kTmaStages && k0 + q <= k1; q++) issue(k0 + q, q);
+  for (int q = 0; q < RS && k0 + q < k1; q++) issue_rows(k0 + q, q);
   float dPma = 0.f, L1ma = 0.f, L2ma = 0.f, dPmb = 0.f, L1mb = 0.f, L2mb = 0.f;
   if (any) {
     const unsigned c = (unsigned)(ia + j * nx) + (unsigned)(k0 - 1) * pln;
@@ -1499,7 +1506,7 @@ __device__ bool split_tile_x2(const GbfSplitConsts& C, const GbfSplitGrid& G, in
       give_up();
       return false;
     }
-    if (k0 + kTmaStages <= k1) issue(k0 + kTmaStages);
+    if (k0 + kTmaStages <= k1) issue(k0 + kTmaStages, 0);
   }
   // flux carry of both cells: the faces between planes k0 - 1 and k0
   float fza1 = 0.f, fza2 = 0.f, fzb1 = 0.f, fzb2 = 0.f;
@@ -1517,8 +1524,10 @@ __device__ bool split_tile_x2(const GbfSplitConsts& C, const GbfSplitGrid& G, in
     acc.c1 = rw.c1;
     acc.c2 = rw.c2;
   }
-  int t_cur = 0, t_next = 1, t_rows = 0;
+  int u = 0;  // (k - k0) % 3: plane buffer, halo stage and rows stage of plane k
   for (int k = k0; k < k1; k++) {
+    const float2 s0 = s_own;  // plane k's, before the build of plane k + 1 replaces it
+    const int t_cur = u, t_next = u == 2 ? 0 : u + 1, t_rows = u;
     {
       const int sn = t_next;
       bool ok = wait_bit(sn);
@@ -1528,8 +1537,10 @@ __device__ bool split_tile_x2(const GbfSplitConsts& C, const GbfSplitGrid& G, in
         give_up();
         return false;
       }
-      if (k + 1 + kTmaStages <= k1) issue(k + 1 + kTmaStages);
-      if (k > k0 && k - 1 + RS < k1) issue_rows(k - 1 + RS);
+      // halo stage sn was consumed by the build above; rows stage (u + 2) % 3
+      // (plane k - 1) by the previous plane's update
+      if (k + 1 + kTmaStages <= k1) issue(k + 1 + kTmaStages, sn);
+      if (k > k0 && k + 2 < k1) issue_rows(k + 2, sn == 2 ? 0 : sn + 1);
     }
     if (any) {
       const float* Pd = sm.dP[t_cur];
@@ -1541,7 +1552,6 @@ __device__ bool split_tile_x2(const GbfSplitConsts& C, const GbfSplitGrid& G, in
       const float2 au = gbf_ld2(P1 + hc - BX), ad = gbf_ld2(P1 + hc + BX);
       const float2 b0 = gbf_ld2(P2 + hc), bl = gbf_ld2(P2 + hc - 2), br = gbf_ld2(P2 + hc + 2);
       const float2 bu = gbf_ld2(P2 + hc - BX), bd = gbf_ld2(P2 + hc + BX);
-      const float2 s0 = gbf_ld2(sm.S[t_cur] + hc);
       const float2 dp = gbf_ld2(sm.dP[t_next] + hc), ap = gbf_ld2(sm.L1[t_next] + hc),
                    bp = gbf_ld2(sm.L2[t_next] + hc);
       const float2 ph = gbf_ld2(&raw.phi[t_rows][mi]);
@@ -1585,9 +1595,7 @@ __device__ bool split_tile_x2(const GbfSplitConsts& C, const GbfSplitGrid& G, in
       fza1 = o[0].fz1; fza2 = o[0].fz2;
       fzb1 = o[1].fz1; fzb2 = o[1].fz2;
     }
-    t_cur = t_next;
-    t_next = t_next == kTmaStages - 1 ? 0 : t_next + 1;
-    t_rows = t_rows == RS - 1 ? 0 : t_rows + 1;
+    u = t_next;
   }
   return true;
 }
