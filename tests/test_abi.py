@@ -3,6 +3,7 @@ declare, its struct layouts match the bindings, and its host-side logic
 (reference constants, stability bound, validation, field generator) is right.
 No GPU compute is called."""
 import ctypes
+import os
 import pathlib
 import re
 import shutil
@@ -12,7 +13,9 @@ import numpy as np
 import pytest
 
 ROOT = pathlib.Path(__file__).resolve().parents[1]
-REF = pathlib.Path("/root/reference")
+# the reference sources (main.cpp, no_communication.cpp, defines.h); the link
+# test skips where they are absent
+REF = pathlib.Path(os.environ.get("GBF_REFERENCE_DIR", "/root/reference"))
 
 
 @pytest.fixture(scope="module")
