@@ -33,8 +33,9 @@ def test_halo_builds_cover_every_read_once(TXC, TY):
         hc = (ty + 1) * BX + 2 * tx + 4
         if in_tile:  # slot 0: the own pair
             built += [hc, hc + 1]
-            # cell a: x-1 (odd half of the left pair), itself, x+1; cell b: x+2
-            reads |= {hc - 1, hc, hc + 1, hc + 2}
+            # 64-bit loads of the left, own and right pairs (cell a uses x-1,
+            # cell b x+2 of the outer ones) and of the pairs above and below
+            reads |= {hc - 2, hc - 1, hc, hc + 1, hc + 2, hc + 3}
             reads |= {hc - BX, hc - BX + 1, hc + BX, hc + BX + 1}
         q = t + NT  # slot 1
         if in_tile and q < PCOLS * HY:
