@@ -325,9 +325,13 @@ def run_ours(args, rank, world):
             "kernel_times_ms": {k: {"total_ms": v[0], "launches": v[1]} for k, v in ktimes.items()},
             "binding_resource": ("FP64 pipe (ncu: 85% of FP64-pipe cycles active in the flux/Newton pass; "
                                  "GB300 DFMA 1.2 TFLOP/s)") if "f64" in kname else
-                                ("instruction issue (ncu: 66-80% issue active; DRAM traffic 1.14x the "
-                                 "algorithmic bytes on config 4, halo rows re-read)"),
+                                ("instruction issue and the per-plane block barrier (ncu: 66-80% issue "
+                                 "active; DRAM traffic 1.12-1.16x the algorithmic bytes on config 4, halo "
+                                 "rows re-read)"),
             "ms_per_step_with_kernel_events": ms_k / args.steps}
+    if "f64" in kname:  # the FP64 kernels' own roof: the FP64 pipe, from the ncu capture of this pass
+        roof["fp64_pipe"] = {"frac": 0.853, "metric": "sm__pipe_fp64_cycles_active",
+                             "source": "profiles/f64_flux_newton_config1.md (flux/Newton pass, 192^3)"}
 
     # e2e through the C ABI with pinned host buffers: H2D state, one step, D2H P and S
     e2e_steps = max(2, min(args.steps, 10 if ensemble else 20))
