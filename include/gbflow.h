@@ -177,10 +177,12 @@ size_t gbf_boundary_scratch_doubles(const gbf_model* m);
    No counterpart in the reference. Same results as gbf_boundary_f64; its
    scratch is a fixed 8 MiB array of the library in device memory that every
    GPU loading the library keeps until exit, so it serves grids with at most
-   524288 boundary cells (cubes up to 295^3) and returns GBF_ERR_ARG beyond.
-   Allocates nothing. Its first call on a device looks up the array's device
-   address, so make it before any stream capture. All calls share the array:
-   calls that overlap on the GPU race. */
+   524288 boundary cells (2 nx ny + 2 nx (nz - 2) + 2 (ny - 2) (nz - 2): cubes
+   up to 296^3) and returns GBF_ERR_ARG beyond, before any work.
+   Allocates nothing. Its first call on a device, and its first call after
+   that device's context was destroyed and created again, look up the array's
+   device address, so make those calls before any stream capture. All calls
+   share the array: calls that overlap on the GPU race. */
 int gbf_boundary_f64_noalloc(const gbf_model* m, gbf_arrays d_arrays, void* stream);
 
 /* ------------------------------------------------------- single domain ----

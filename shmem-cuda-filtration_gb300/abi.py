@@ -130,6 +130,7 @@ def _declare(lib) -> None:
         "gbf_newton_f64": (c_int, [PM, GbfArrays, GbfCells, c_void_p]),
         "gbf_boundary_f64": (c_int, [PM, GbfArrays, c_void_p, c_void_p]),
         "gbf_boundary_scratch_doubles": (c_size_t, [PM]),
+        "gbf_boundary_f64_noalloc": (c_int, [PM, GbfArrays, c_void_p]),
         "gbf_abi_sizeof": (c_size_t, [c_int]),
         "gbf_domain_create": (c_int, [PM, PC, c_int, ctypes.POINTER(c_void_p)]),
         "gbf_domain_destroy": (c_int, [c_void_p]),

@@ -20,6 +20,9 @@
 
 #include <mutex>
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include "gbf_internal.h"
 
 namespace {
@@ -231,22 +234,58 @@ static __device__ __align__(256) double g_noalloc_scratch[kNoAllocScratchDoubles
 
 constexpr int kNoAllocMaxDevices = 64;
 std::mutex g_noalloc_mu;
+// Per device: the array's address and the id of the CUDA context it was looked
+// up in. A context that is destroyed (cudaDeviceReset, a reset of the primary
+// context) and created again may load the library's module elsewhere, so the
+// address is valid only while the context it came from is current.
 double* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+unsigned long long g_noalloc_ctx[kNoAllocMaxDevices] = {};
+PFN_cuCtxGetCurrent_v4000 g_ctx_current = nullptr;
+PFN_cuCtxGetId_v12000 g_ctx_id = nullptr;
+bool g_ctx_queries_resolved = false;
 
-// Device address of g_noalloc_scratch on the current device, looked up once
-// per device (with that device current) and cached.
+// Id of the calling thread's current CUDA context (cuCtxGetId: unique for the
+// life of the process), or 0 when no context is current or the driver cannot
+// tell. The driver functions are reached through the runtime's entry-point
+// query, so libgbflow does not link libcuda. Called with g_noalloc_mu held.
+unsigned long long current_context_id() {
+  if (!g_ctx_queries_resolved) {
+    g_ctx_queries_resolved = true;
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 4000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      g_ctx_current = (PFN_cuCtxGetCurrent_v4000)f;
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      g_ctx_id = (PFN_cuCtxGetId_v12000)f;
+  }
+  if (!g_ctx_current || !g_ctx_id) return 0;
+  CUcontext c = nullptr;
+  if (g_ctx_current(&c) != CUDA_SUCCESS || !c) return 0;
+  unsigned long long id = 0;
+  return g_ctx_id(c, &id) == CUDA_SUCCESS ? id : 0;
+}
+
+// Device address of g_noalloc_scratch on the current device, looked up with
+// that device current (cudaGetSymbolAddress) on the first call, and again
+// whenever the current context is not the one the address came from (or
+// cannot be identified); otherwise the cached address.
 int noalloc_scratch(double** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return gbf_cuda_check(e, "gbf_boundary_f64_noalloc: cudaGetDevice");
   if (dev < 0 || dev >= kNoAllocMaxDevices) return gbf_fail(GBF_ERR_ARG, "gbf_boundary_f64_noalloc: device index");
   std::lock_guard<std::mutex> lk(g_noalloc_mu);
-  if (!g_noalloc_ptr[dev]) {
+  const unsigned long long ctx = current_context_id();
+  if (!g_noalloc_ptr[dev] || ctx == 0 || ctx != g_noalloc_ctx[dev]) {
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || !p) return gbf_cuda_check(e != cudaSuccess ? e : cudaErrorInvalidSymbol,
                                                       "gbf_boundary_f64_noalloc: cudaGetSymbolAddress");
     g_noalloc_ptr[dev] = (double*)p;
+    g_noalloc_ctx[dev] = current_context_id();  // the lookup made a context current if none was
   }
   *out = g_noalloc_ptr[dev];
   return GBF_OK;
@@ -343,8 +382,9 @@ int gbf_boundary_f64(const gbf_model* m, gbf_arrays a, double* scratch, void* st
 // gbf_boundary_f64; the gather scratch is the library's fixed device array
 // g_noalloc_scratch instead of a caller buffer. Allocates nothing: no
 // cudaMalloc, cudaFree or allocating library routine. The first call on a
-// device looks up the array's address there (cudaGetSymbolAddress), so make
-// that first call before any stream capture. Every call on a device uses the
+// device looks up the array's address there (cudaGetSymbolAddress), and so
+// does the first call after that device's context was destroyed and created
+// again, so make those calls before any stream capture. Every call on a device uses the
 // same array, which keeps the last call's contents: the gather fills every
 // slot the scatter reads, so nothing needs clearing, and calls that overlap
 // on the same GPU (from several streams or host threads) race on it.

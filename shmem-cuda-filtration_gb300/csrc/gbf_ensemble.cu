@@ -10,9 +10,9 @@
 // boundary cells and one per-member phase-mass reduction. A step is a CUDA
 // graph (counter reset, step, faces, masses), captured once per buffer parity.
 //
-// Tuning: the tile shape (one of three compiled shapes) and the k-range per
-// CTA ("fusion depth": planes marched per tile pass) per member edge are
-// picked by gbf_ensemble_autotune from timed trial steps.
+// Tuning: the tile shape (one of the six compiled shapes of the enum below)
+// and the k-range per CTA ("fusion depth": planes marched per tile pass) per
+// member edge are picked by gbf_ensemble_autotune from timed trial steps.
 #include <string.h>
 
 #include <algorithm>

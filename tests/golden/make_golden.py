@@ -7,8 +7,9 @@ this script drives them through their own functions (initial_data,
 time_step_function, the five hot-path calls, the checkpoint writer save and
 the Tecplot writer save_data_plots).
 
-Run from the repository root where the reference sources are present:
-    python tests/golden/make_golden.py
+Run from the repository root, with GBF_REFERENCE_DIR naming the reference
+checkout (oracle/Makefile compiles it from there):
+    GBF_REFERENCE_DIR=<reference checkout> python tests/golden/make_golden.py
 Outputs tests/golden/*.npz (small, committed).
 """
 from __future__ import annotations

@@ -13,9 +13,9 @@ import numpy as np
 import pytest
 
 ROOT = pathlib.Path(__file__).resolve().parents[1]
-# the reference sources (main.cpp, no_communication.cpp, defines.h); the link
-# test skips where they are absent
-REF = pathlib.Path(os.environ.get("GBF_REFERENCE_DIR", "/root/reference"))
+# the reference sources (main.cpp, no_communication.cpp, defines.h), named by
+# GBF_REFERENCE_DIR; the link test skips where it is unset or they are absent
+REF = pathlib.Path(os.environ["GBF_REFERENCE_DIR"]) if os.environ.get("GBF_REFERENCE_DIR") else None
 
 
 @pytest.fixture(scope="module")
@@ -117,6 +117,24 @@ def test_validate_rejects_bad_models(abi, lib):
     lib.gbf_clear_status()
 
 
+def test_noalloc_boundary_refuses_grids_beyond_its_array(lib, abi):
+    """The allocation-free boundary pass holds 2 doubles per boundary cell in
+    its fixed 2^20-double array: at most 524288 boundary cells. The size check
+    comes before any device work, so grids just beyond the limit are refused
+    here without a GPU (the grids at the limit, 296^3 and a 4 x 43690 x 4
+    column with exactly 524288 boundary cells, run in the GPU test)."""
+    def nb(m):
+        return 2 * m.nx * m.ny + 2 * m.nx * (m.nz - 2) + 2 * (m.ny - 2) * (m.nz - 2)
+    assert nb(abi.reference_model(296, 296, 296, 0.02)) == 522152
+    assert nb(abi.reference_model(4, 43690, 4, 0.02)) == 524288
+    for dims in ((297, 297, 297), (3, 65536, 3), (5, 32767, 5)):  # 525698, 524290, 524290 cells
+        m = abi.reference_model(*dims, 0.02)
+        assert nb(m) > 524288
+        assert lib.gbf_boundary_f64_noalloc(ctypes.byref(m), abi.GbfArrays(), None) == abi.GBF_ERR_ARG
+    assert lib.gbf_last_status() == abi.GBF_ERR_ARG
+    lib.gbf_clear_status()
+
+
 def test_lognormal_field_statistics_and_determinism(lib):
     shape = (48, 40, 32)
     K = np.empty(shape, np.float32)
@@ -137,8 +155,8 @@ def test_lognormal_field_statistics_and_determinism(lib):
     assert phi.min() >= 0.3 and phi.max() <= 0.4 and abs(phi.mean() - 0.35) < 1e-3
 
 
-@pytest.mark.skipif(not (REF / "main.cpp").exists() or shutil.which("g++") is None,
-                    reason="reference sources not present on this machine")
+@pytest.mark.skipif(REF is None or not (REF / "main.cpp").exists() or shutil.which("g++") is None,
+                    reason="GBF_REFERENCE_DIR unset or the reference sources absent")
 def test_dropin_links_with_unmodified_reference_driver(tmp_path):
     """main.cpp and no_communication.cpp, compiled from the reference's own
     sources, link against libgbflow.so in place of gpu.cu (sh/cuda.sh:23-24)."""
