@@ -3,13 +3,16 @@
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                     [--workload NAME] [--cube N] [--no-compare] [--no-cpu-baseline]
 
-Workloads are <config>_<precision>: config0..config4 (the benchmark
-configurations as seeded synthetic inputs, see workloads.py) and f64, split
-(masses at FP64 precision: FP32-pair defects), splitdf (FP32-pair masses), splitdefect
-(FP32 mass defects).
-The default, config4_splitdefect, is the combined
-precision + batching form on the 256-member ensemble; the same line also
-reports plain FP64 and the other split forms on the same members.
+Workloads are <config>_<form>: config0..config4 (the benchmark configurations
+as seeded synthetic inputs, see workloads.py) and the forms f64 (plain FP64),
+split (FP32 state and fluxes, phase masses at FP64 precision as FP32-pair
+defects, one residual-correction Newton step per cell), splitdf (FP32-pair
+masses), splitdefect (FP32 mass defects, no correction step); and
+config1_dropin, config 1's grid through the reference's own host function set
+(defines.h: the five calls of time_step_function, fused mode).
+The default, config4_split, is the combined precision + batching form on the
+256-member ensemble; the same line also reports plain FP64 and the other split
+forms on the same members.
 
 One JSON line on rank 0. `value` is device-resident throughput (inputs in
 HBM, CUDA events on the stream the kernels run on, CUDA graphs for
@@ -17,7 +20,12 @@ ensembles); `e2e` is the same metric through the public C ABI with host
 buffers (pinned host -> device state, the step, device -> host P and S,
 every step). `--impl reference` times the reference CPU algorithm (the
 oracle: a bit-exact restatement of the reference's cpu.cpp) on the host
-cores instead.
+cores instead, on inputs made by libgbf_inputs.so (libgbflow is not loaded).
+
+Under torchrun (N ranks) an ensemble workload is N times the configuration's
+members (the same parameter and field streams, continued) and rank r advances
+members r, r + N, ...: per-GPU work stays that of the configuration ("weak");
+single grids run one replica per rank.
 """
 from __future__ import annotations
 
@@ -114,14 +122,24 @@ def dist_setup():
     return rank, world
 
 
-def dist_max(x: float, world: int) -> float:
+def _dist_reduce(x: float, world: int, op):
     if world == 1:
         return x
     import torch
     import torch.distributed as dist
     t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(t, op=op)
     return float(t.item())
+
+
+def dist_max(x: float, world: int) -> float:
+    import torch.distributed as dist
+    return x if world == 1 else _dist_reduce(x, world, dist.ReduceOp.MAX)
+
+
+def dist_sum(x: float, world: int) -> float:
+    import torch.distributed as dist
+    return x if world == 1 else _dist_reduce(x, world, dist.ReduceOp.SUM)
 
 
 def barrier(world):
@@ -134,28 +152,79 @@ def barrier(world):
 
 PRECISIONS = {"f64": ("GBF_PREC_F64", "plain FP64", "f64"),
               "split": ("GBF_PREC_SPLIT", "FP32 state and fluxes, phase masses at FP64 precision (FP32-pair "
-                        "defects over the state's mass at the row's hydrostatic density)", "f32+f32x2"),
+                        "defects over the state's mass at the row's hydrostatic density), one residual-"
+                        "correction Newton step per cell with the residual in FP32 pairs", "f32+f32x2"),
               "splitdf": ("GBF_PREC_SPLIT_DF", "FP32 state and fluxes, FP32-pair masses and residual",
                           "f32+f32x2"),
               "splitdefect": ("GBF_PREC_SPLIT_DEFECT", "FP32 state and fluxes, phase masses as FP32 defects over "
-                              "the state's mass at the row's hydrostatic density", "f32")}
+                              "the state's mass at the row's hydrostatic density, no correction step", "f32"),
+              "dropin": ("GBF_PREC_F64", "plain FP64 through the reference's host function set (defines.h), "
+                         "fused mode", "f64")}
+ENSEMBLE_BASE = {"config3": 96, "config4": 256}
+DESC = {"config0": "config 0: 40^3 homogeneous single grid",
+        "config1": "config 1: {n}^3 heterogeneous single grid",
+        "config1_dropin": "config 1's {n}^3 grid in the reference's media-table physics (Dirichlet patch, 7 "
+                          "Newton iterations: all that the defines.h calls express)",
+        "config2": "config 2: 512x512x256 heterogeneous single grid (sigma_lnK 1.5)",
+        "config3": "config 3: {m} realizations, edges in {{64,96,128,160}}",
+        "config4": "config 4: {m} realizations, edges 48..128 step 16, anisotropic"}
 
 
-def make_members(pkg, lib, cfg, cube):
-    from importlib import import_module
-    wl = import_module(pkg.__name__ + ".workloads")
-    if cfg == "config0":
-        return [wl.config0(lib)], "config 0: 40^3 homogeneous single grid", False
-    if cfg == "config1":
-        mem = wl.config1(lib, n=cube or 256)
-        return [mem], f"config 1: {mem.model.nx}^3 heterogeneous single grid", False
-    if cfg == "config2":
-        return [wl.config2(lib)], "config 2: 512x512x256 heterogeneous single grid (sigma_lnK 1.5)", False
-    if cfg == "config3":
-        return wl.config3(lib), "config 3: 96 realizations, edges in {64,96,128,160}", True
-    if cfg == "config4":
-        return wl.config4(lib), "config 4: 256 realizations, edges 48..128 step 16, anisotropic", True
-    raise SystemExit(f"unknown configuration {cfg}")
+class Workload:
+    """The workload of a --workload name: this rank's members, and the shape
+    of the whole job (all ranks) from the members' parameters alone."""
+
+    def __init__(self, pkg, lib, name, cube, rank, world, limit=0):
+        from importlib import import_module
+        self.wl = wl = import_module(pkg.__name__ + ".workloads")
+        cfg, _, form = name.partition("_")
+        if form not in PRECISIONS:
+            raise SystemExit(f"unknown form in {name}")
+        self.name, self.cfg, self.form = name, cfg, form
+        self.ensemble = cfg in ENSEMBLE_BASE
+        if form == "dropin" and cfg != "config1":
+            raise SystemExit("the drop-in form runs config 1's grid only (config1_dropin)")
+        n = cube or 256
+        if self.ensemble:
+            specs = (wl.config3_specs if cfg == "config3" else wl.config4_specs)(ENSEMBLE_BASE[cfg] * world)
+            if limit:
+                specs = [s for s in specs if s["index"] % ENSEMBLE_BASE[cfg] < limit]
+            self.members_all = len(specs)
+            self.cells_all = sum(wl.spec_cells(s) for s in specs)
+            self.members = [wl.build_member(lib, s) for s in wl.shard(specs, rank, world)]
+            self.desc = DESC[cfg].format(m=self.members_all)
+            self.partition = (f"members r::{world} of {self.members_all} on rank r (weak scaling: "
+                              f"{ENSEMBLE_BASE[cfg] if not limit else limit} members' worth per GPU)")
+        else:
+            if cfg == "config0":
+                mem = wl.config0(lib)
+            elif cfg == "config1":
+                mem = wl.config1_dropin(lib, n=n) if form == "dropin" else wl.config1(lib, n=n)
+            elif cfg == "config2":
+                mem = wl.config2(lib)
+            else:
+                raise SystemExit(f"unknown configuration {cfg}")
+            self.members = [mem]
+            self.members_all = world
+            self.cells_all = world * mem.ncells
+            self.desc = DESC["config1_dropin" if form == "dropin" else cfg].format(n=n)
+            self.partition = "replicas: one grid per rank" if world > 1 else "one grid"
+
+    @property
+    def cells(self):
+        return sum(m.ncells for m in self.members)
+
+    @property
+    def interior_cells(self):
+        return sum((m.model.nx - 2) * (m.model.ny - 2) * (m.model.nz - 2) for m in self.members)
+
+    def config(self):
+        """The `config` of the JSON line: the workload, identical in both arms."""
+        gb = self.cells_all * 32 / 1e9
+        return {"workload": self.name, "desc": self.desc, "cells": self.cells_all, "members": self.members_all,
+                "form": PRECISIONS[self.form][1], "partition": self.partition,
+                "l2": (f"inputs larger than L2 (state and fields >= {gb:.1f} GB > 129 MB)" if gb > 0.129 else
+                       f"inputs smaller than L2 ({gb:.3f} GB): a profiling or test case")}
 
 
 class Runner:
@@ -194,17 +263,86 @@ class Runner:
         return getattr(self.obj, name)
 
     @property
-    def cells(self):
-        return sum(m.ncells for m in self.members)
-
-    @property
     def uses_tma(self):
         lib = self.obj.lib
         return bool(lib.gbf_ensemble_uses_tma(self.obj.h) if self.ensemble else lib.gbf_domain_uses_tma(self.obj.h))
 
+
+class DropinRunner:
+    """Config 1's grid through the reference's host function set, called like
+    main.cpp: device_memory_alloc, load_data_to_device(_int), then per step
+    time_step_function's five calls (main.cpp:83-94) in fused mode."""
+
+    def __init__(self, pkg, member):
+        import ctypes
+        from importlib import import_module
+        self.abi = pkg.abi
+        self.dp = dp = import_module(pkg.__name__ + ".dropin")
+        self.mem = member
+        self.di = dp.DropIn()
+        self.di.set_mode(1)
+        m = member.model
+        self.c = dp.consts_from_model(m)
+        self.H = dp.PtrArrays()
+        self.D = dp.PtrArrays()
+        self.buf = ctypes.c_void_p()
+        self.di.f["device_memory_alloc"](ctypes.byref(self.D), ctypes.byref(self.buf), m.nx, self.c)
+        self.t = 0.0
+        self.lib = self.di.lib
+        status = self.lib.gbf_last_status()
+        if status:
+            raise RuntimeError(f"device_memory_alloc: {self.lib.gbf_status_string(status).decode()}")
+
+    def upload(self, P, S):
+        f, c = self.di.f, self.c
+        f["load_data_to_device"](P.ctypes.data, self.D.P1, c.NX, c)
+        f["load_data_to_device"](S.ctypes.data, self.D.S2, c.NX, c)
+
+    def upload_initial(self):
+        P, S = self.mem.initial_state()
+        self.upload(P, S)
+        media = np.zeros(self.mem.model.shape, np.int32) if self.mem.media is None else self.mem.media
+        self.di.f["load_data_to_device_int"](np.ascontiguousarray(media, np.int32).ctypes.data, self.D.media,
+                                             self.c.NX, self.c)
+        self.t = 0.0
+
+    def step(self, n=1):
+        for _ in range(n):
+            self.t += self.c.dt
+            self.di.time_step(self.H, self.D, self.c, self.t)
+
+    def download(self, field, out):
+        self.di.f["load_data_to_host"](out.ctypes.data, getattr(self.D, field), self.c.NX, self.c)
+        return out
+
     @property
-    def interior_cells(self):
-        return sum((m.model.nx - 2) * (m.model.ny - 2) * (m.model.nz - 2) for m in self.members)
+    def handle(self):
+        return self.di.domain(self.D.P1)
+
+    def set_timing(self, on):
+        h = self.handle
+        if h:
+            self.lib.gbf_domain_set_timing(h, int(on))
+
+    def kernel_times(self):
+        n = self.lib.gbf_kernel_kinds()
+        ms = np.zeros(n, np.float64)
+        cnt = np.zeros(n, np.int32)
+        self.lib.gbf_domain_kernel_times(self.handle, ms.ctypes.data, cnt.ctypes.data, n)
+        return {self.lib.gbf_kernel_name(k).decode(): (float(ms[k]), int(cnt[k])) for k in range(n) if cnt[k]}
+
+    def status(self):
+        h = self.handle
+        return self.lib.gbf_domain_status(h) if h else self.lib.gbf_last_status()
+
+    def sync(self):
+        import torch
+        torch.cuda.synchronize()
+
+    def close(self):
+        if self.D.P1:
+            self.di.f["device_memory_free"](self.D, self.buf)
+            self.D.P1 = None
 
 
 # Algorithmic bytes per interior (or every) cell of each kernel: the
@@ -219,9 +357,12 @@ ALGO_BYTES = {
 }
 # The defect form holds M1, M2 in 4 bytes: read 16 + 8, write 8 + 8.
 ALGO_BYTES_DEFECT = {"split_step": (40.0, "interior"), "ensemble_step": (40.0, "interior")}
+# The drop-in's media-table grid reads an int media index instead of K, phi (props: P, S, media;
+# flux/Newton: no phi read).
+ALGO_BYTES_DROPIN = {"f64_props": (60.0, "all"), "f64_flux_newton": (72.0, "interior")}
 
 
-def timed(runner, steps, stream, world, clocks=None):
+def timed(runner, steps, stream, world):
     """Device time of `steps` steps on the runner's stream (CUDA events)."""
     import torch
     barrier(world)
@@ -236,34 +377,88 @@ def timed(runner, steps, stream, world, clocks=None):
     return dist_max(e0.elapsed_time(e1), world)
 
 
-def cpu_baseline(O, abi, members, budget_s=12.0, threads=None):
-    """The oracle on the host cores over a bounded sample of the workload:
-    whole members (largest first), one time step at a time, until ~budget_s."""
-    orc = O.Oracle(abi)
-    threads = threads or os.cpu_count()
+# --------------------------------------------------- reference CPU algorithm
+
+def reference_cpu_run(O, abi, members, steps, warmup, step_budget_s):
+    """The reference CPU algorithm (the oracle: a bit-exact restatement of
+    cpu.cpp, 7 Newton iterations, OpenMP over i) on all host cores. Each step
+    advances whole members, largest first, until the step's time budget is
+    spent (every member at least once per step counted); `steps` timed steps
+    after `warmup` untimed ones. The same measurement serves the reference arm
+    and the repo arm's cpu_baseline."""
+    threads = os.cpu_count() or 1
     os.environ["OMP_NUM_THREADS"] = str(threads)
-    done_cells = 0
-    t0 = time.perf_counter()
-    sample = []
-    for mem in sorted(members, key=lambda x: -x.ncells):
+    orc = O.Oracle(abi)
+    order = sorted(members, key=lambda x: -x.ncells)
+    states = []
+
+    def state(mem):
         st = O.State(mem.model, mem.media, mem.K, mem.phi)
         P, S = mem.initial_state()
         st["P1"][...] = P
         st["S2"][...] = S
-        n = 0
-        while time.perf_counter() - t0 < budget_s or n == 0:
-            orc.step(st, 1)
-            done_cells += mem.ncells
-            n += 1
-            if n >= 1000:
+        return st
+
+    def one_step():
+        t0 = time.perf_counter()
+        c = 0
+        for q, mem in enumerate(order):
+            if q >= len(states):
+                states.append(state(mem))
+            orc.step(states[q], 1)
+            c += mem.ncells
+            if time.perf_counter() - t0 > step_budget_s:
                 break
-        sample.append(f"{mem.model.nx}x{mem.model.ny}x{mem.model.nz} x {n} steps")
-        if time.perf_counter() - t0 >= budget_s:
-            break
-    dt = time.perf_counter() - t0
-    return {"value": done_cells / dt, "unit": "cell-steps/s", "cores": threads, "kind": "port",
-            "sample": "; ".join(sample) + f" ({dt:.1f} s; oracle = bit-exact restatement of the reference "
-                                          f"cpu.cpp, OpenMP over i, 7 Newton iterations)"}
+        return c, time.perf_counter() - t0
+
+    for _ in range(warmup):
+        one_step()
+    tot_c, tot_t = 0, 0.0
+    for _ in range(steps):
+        c, t = one_step()
+        tot_c += c
+        tot_t += t
+    v = tot_c / tot_t
+    sample = (f"{len(states)} of {len(members)} member(s) per step (largest first), each step bounded to "
+              f"~{step_budget_s:.1f} s, {steps} timed step(s) after {warmup}; oracle = bit-exact restatement of "
+              f"the reference cpu.cpp (OpenMP over i), 7 Newton iterations")
+    return {"value": v, "unit": "cell-steps/s", "cores": threads, "kind": "port", "sample": sample,
+            "seconds": tot_t}
+
+
+def step_budget(args):
+    return max(1.0, 120.0 / max(1, args.steps + args.warmup))
+
+
+# ------------------------------------------------------------------- our arm
+
+def link_bandwidth(torch, nbytes=1 << 30):
+    """Pinned host <-> device copy rates (GB/s), each direction alone and both at once."""
+    h = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    h2 = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    d = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    d2 = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+    for _ in range(2):
+        d.copy_(h, non_blocking=True)
+        h.copy_(d, non_blocking=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    d.copy_(h, non_blocking=True)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    h.copy_(d, non_blocking=True)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    with torch.cuda.stream(s1):
+        d.copy_(h, non_blocking=True)
+    with torch.cuda.stream(s2):
+        h2.copy_(d2, non_blocking=True)
+    torch.cuda.synchronize()
+    t3 = time.perf_counter()
+    del h, h2, d, d2
+    return {"h2d_gbs": nbytes / (t1 - t0) / 1e9, "d2h_gbs": nbytes / (t2 - t1) / 1e9,
+            "both_gbs": 2 * nbytes / (t3 - t2) / 1e9}
 
 
 def run_ours(args, rank, world):
@@ -274,29 +469,30 @@ def run_ours(args, rank, world):
     torch.cuda.init()
     if args.no_tma:
         lib.gbf_set_tma(0)
-    cfg, _, p = args.workload.partition("_")
-    if p not in PRECISIONS:
-        raise SystemExit(f"unknown precision in {args.workload}")
-    members, desc, ensemble = make_members(pkg, lib, cfg, args.cube)
-    if args.members:
-        members = members[: args.members]
-        desc += f" (first {len(members)} members)"
+    W = Workload(pkg, lib, args.workload, args.cube, rank, world, args.members)
+    members, ensemble, p = W.members, W.ensemble, W.form
     prec = getattr(abi, PRECISIONS[p][0])
-    stream = torch.cuda.Stream()
     cap = args.warmup + 2 * args.steps + 8
-    run = Runner(pkg, members, prec, ensemble, cap)
-    run.set_stream(stream.cuda_stream)
     tuning = None
-    if ensemble and prec != abi.GBF_PREC_F64 and args.tile >= 0:
-        run.set_tuning(args.tile, 0, 0)
-        tuning = run.tuning()
-    elif ensemble and prec != abi.GBF_PREC_F64 and not args.no_autotune:
+    if p == "dropin":
+        stream = torch.cuda.default_stream()  # the drop-in runs on the legacy default stream, like gpu.cu
+        run = DropinRunner(pkg, members[0])
         run.upload_initial()
-        tuning = run.autotune(2)
-    run.upload_initial()
+        run.step(1)  # the first fused step creates the domain behind the arrays
+    else:
+        stream = torch.cuda.Stream()
+        run = Runner(pkg, members, prec, ensemble, cap)
+        run.set_stream(stream.cuda_stream)
+        if ensemble and prec != abi.GBF_PREC_F64 and args.tile >= 0:
+            run.set_tuning(args.tile, 0, 0)
+            tuning = run.tuning()
+        elif ensemble and prec != abi.GBF_PREC_F64 and not args.no_autotune:
+            run.upload_initial()
+            tuning = run.autotune(2)
+        run.upload_initial()
     run.step(args.warmup)
     run.sync()
-    cells = run.cells
+    cells, icells = W.cells, W.interior_cells
     with ClockSampler(torch.cuda.current_device()) as clk:
         ms = timed(run, args.steps, stream, world)            # value: graphs, no per-kernel events
         run.set_timing(True)                                   # roofline: the same steps with kernel events
@@ -304,36 +500,39 @@ def run_ours(args, rank, world):
     ktimes = run.kernel_times()
     run.set_timing(False)
     status = run.status()
-    value = world * cells * args.steps / (ms / 1e3)
+    cells_job = dist_sum(float(cells), world)
+    value = cells_job * args.steps / (ms / 1e3)
 
     # roofline of the dominant kernel
     hbm, peak_kind = peaks()
     kname, (kms, klaunch) = max(ktimes.items(), key=lambda kv: kv[1][0])
     per_launch_s = kms / 1e3 / max(klaunch, 1)
-    bpc, which = (ALGO_BYTES_DEFECT if p == "splitdefect" else ALGO_BYTES).get(kname, ALGO_BYTES.get(kname, (0.0, "all")))
-    algo = bpc * (run.interior_cells if which == "interior" else cells)
+    table = ALGO_BYTES_DROPIN if p == "dropin" else ALGO_BYTES_DEFECT if p == "splitdefect" else ALGO_BYTES
+    bpc, which = table.get(kname, ALGO_BYTES.get(kname, (0.0, "all")))
+    algo = bpc * (icells if which == "interior" else cells)
     achieved = algo / per_launch_s / 1e9 if per_launch_s > 0 else 0.0
     traffic = None
     tfile = ROOT / "profiles" / "traffic.json"
     if tfile.exists():  # ncu DRAM bytes per cell of a smaller capture, scaled to this launch's cells
         ent = json.loads(tfile.read_text()).get(args.workload, {}).get(kname)
         if ent:
-            traffic = ent["bytes_per_cell"] * (run.interior_cells if ent["cells"] == "interior" else cells)
+            traffic = ent["bytes_per_cell"] * (icells if ent["cells"] == "interior" else cells)
+    f64 = "f64" in kname
     roof = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": hbm, "unit": "GB/s",
             "frac": achieved / hbm, "peak_source": peak_kind, "traffic": traffic,
             "algorithmic_bytes_per_launch": algo, "bytes_per_cell": bpc, "ms_per_launch": per_launch_s * 1e3,
             "kernel_times_ms": {k: {"total_ms": v[0], "launches": v[1]} for k, v in ktimes.items()},
             "binding_resource": ("FP64 pipe (ncu: 85% of FP64-pipe cycles active in the flux/Newton pass; "
-                                 "GB300 DFMA 1.2 TFLOP/s)") if "f64" in kname else
+                                 "GB300 DFMA 1.2 TFLOP/s)") if f64 else
                                 ("instruction issue and the per-plane block barrier (ncu: 66-80% issue "
                                  "active; DRAM traffic 1.12-1.16x the algorithmic bytes on config 4, halo "
                                  "rows re-read)"),
             "ms_per_step_with_kernel_events": ms_k / args.steps}
-    if "f64" in kname:  # the FP64 kernels' own roof: the FP64 pipe, from the ncu capture of this pass
+    if f64:  # the FP64 kernels' own roof: the FP64 pipe, from the ncu capture of this pass
         roof["fp64_pipe"] = {"frac": 0.853, "metric": "sm__pipe_fp64_cycles_active",
                              "source": "profiles/f64_flux_newton_config1.md (flux/Newton pass, 192^3)"}
 
-    # e2e through the C ABI with pinned host buffers: H2D state, one step, D2H P and S
+    # e2e through the public API with pinned host buffers: H2D state, one step, D2H P and S
     e2e_steps = max(2, min(args.steps, 10 if ensemble else 20))
     if ensemble:
         Pall = torch.empty(cells, dtype=torch.float64, pin_memory=True).numpy()
@@ -348,39 +547,57 @@ def run_ours(args, rank, world):
         api = ("gbf_ensemble_advance_host(P, S, 1, P, S): every member's P1, S2 host->device, one step, "
                "device->host, pipelined over member groups")
     else:
-        hostP = torch.empty(members[0].model.shape, dtype=torch.float64, pin_memory=True).numpy()
-        hostS = torch.empty(members[0].model.shape, dtype=torch.float64, pin_memory=True).numpy()
-        run.download(0, "P1", hostP)
-        run.download(0, "S2", hostS)
-        for _ in range(max(1, args.warmup)):  # warm-up round trips
-            run.upload(0, hostP, hostS)
-            run.step(1)
+        shape = members[0].model.shape
+        hostP = torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+        hostS = torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+        if p == "dropin":
+            def rt():
+                run.upload(hostP, hostS)
+                run.step(1)
+                run.download("P1", hostP)
+                run.download("S2", hostS)
+            run.download("P1", hostP)
+            run.download("S2", hostS)
+            api = ("load_data_to_device(P1), load_data_to_device(S2), time_step_function's five calls, "
+                   "load_data_to_host(P1), load_data_to_host(S2) (defines.h)")
+        else:
+            def rt():
+                run.upload(0, hostP, hostS)
+                run.step(1)
+                run.download(0, "P1", hostP)
+                run.download(0, "S2", hostS)
             run.download(0, "P1", hostP)
             run.download(0, "S2", hostS)
+            api = "gbf_domain_upload + gbf_domain_step(1) + gbf_domain_download(P1, S2)"
+        for _ in range(max(1, args.warmup)):
+            rt()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
-            run.upload(0, hostP, hostS)
-            run.step(1)
-            run.download(0, "P1", hostP)
-            run.download(0, "S2", hostS)
-        api = "gbf_domain_upload + gbf_domain_step(1) + gbf_domain_download(P1, S2)"
+            rt()
     e2e_s = dist_max(time.perf_counter() - t0, world)
-    e2e = {"value": world * cells * e2e_steps / e2e_s, "unit": "cell-steps/s",
-           "h2d_bytes_per_step": 2 * cells * 8, "d2h_bytes_per_step": 2 * cells * 8, "api": api}
+    link = link_bandwidth(torch)
+    moved = 2 * cells * 8 * 2 * e2e_steps  # P, S each way
+    e2e = {"value": cells_job * e2e_steps / e2e_s, "unit": "cell-steps/s",
+           "h2d_bytes_per_step": 2 * cells * 8, "d2h_bytes_per_step": 2 * cells * 8, "api": api,
+           "host_link": {"bytes_per_s": moved / e2e_s, "measured_pinned_copy_gbs": link,
+                         "frac_of_concurrent_copy": moved / e2e_s / 1e9 / link["both_gbs"]}}
 
     out = {"metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": PRECISIONS[p][2],
            "data": "synthetic (seeded fields with the configuration's shapes and statistics)",
-           "config": {"workload": args.workload, "desc": f"{desc}, {PRECISIONS[p][1]}", "cells": cells,
-                      "members": len(members), "dt_used_range": [min(m.model.dt for m in members),
-                                                                 max(m.model.dt for m in members)],
-                      "l2": f"inputs larger than L2 (state and fields {cells * 40 / 1e9:.1f} GB > 129 MB)",
-                      "newton": "FP64: converge-and-exit (tol 1e-11, max 7); split: 2 increment iterations",
-                      "tuning": tuning, "graphs": ensemble,
-                      "plane_staging": "TMA" if run.uses_tma else "plain loads"},
-           "clocks": clk.summary(), "e2e": e2e, "gpu_launches": run.launches_per_step * args.steps,
+           "config": W.config(),
+           "details": {"dt_used_range": [min(m.model.dt for m in members), max(m.model.dt for m in members)],
+                       "newton": ("reference: 7 iterations" if p == "dropin" else
+                                  "FP64: converge-and-exit (tol 1e-11, max 7); split: increment Newton, a second "
+                                  "iteration where nonlinear, and (split) one residual-correction step"),
+                       "tuning": tuning, "graphs": ensemble, "rank_cells": cells,
+                       "plane_staging": ("none (FP64)" if p in ("f64", "dropin") else
+                                         "TMA" if run.uses_tma else "plain loads")},
+           "clocks": clk.summary(), "e2e": e2e,
+           "gpu_launches": (run.launches_per_step if p != "dropin" else run.lib.gbf_domain_launches_per_step(
+               run.handle)) * args.steps,
            "roofline": roof, "status": lib.gbf_status_string(status).decode()}
     run.close()
     del run
@@ -406,39 +623,40 @@ def run_ours(args, rank, world):
             del r2
         out["same_members"] = comp
         if "f64" in comp:
-            out["split_batched_over_fp64_batched"] = value / comp["f64"]["value"]
+            out["split_batched_over_fp64_batched"] = (cells * args.steps / (ms / 1e3)) / comp["f64"]["value"]
     if rank == 0 and not args.no_compare and prec != abi.GBF_PREC_F64:
-        out["accuracy"] = accuracy_block(pkg, ge.load_oracle_module(), members, prec, ensemble)
+        O = ge.load_oracle_module()
+        out["accuracy"] = accuracy_block(pkg, O, members, prec, ensemble)
+        out["accuracy_stiff"] = accuracy_stiff(pkg, lib, W.wl, members, prec, ensemble)
     if rank == 0 and not args.no_cpu_baseline:
         O = ge.load_oracle_module()
-        out["cpu_baseline"] = cpu_baseline(O, abi, members, budget_s=args.cpu_budget)
+        cb = reference_cpu_run(O, abi, members, steps=min(args.steps, 3), warmup=1, step_budget_s=step_budget(args))
+        cb.pop("seconds", None)
+        out["cpu_baseline"] = cb
     return out
 
 
-def accuracy_block(pkg, O, members, prec, ensemble, steps=20):
-    """The measured form against plain FP64 on the same members and steps
-    (the GPU FP64 path, itself pinned to the oracle at 1e-12), and against
-    the oracle on the smallest member: max|dS|, relative L2 of P, relative
-    phase-mass difference per step, and how far S moved (max|S - S0|)."""
-    import numpy as np
+def compare(pkg, members, prec, ensemble, steps, flags=0):
+    """The same members advanced `steps` steps in form `prec` and in plain FP64
+    on the GPU: both states and both phase-mass histories."""
     abi = pkg.abi
 
     def run(p):
         r = Runner(pkg, members, p, ensemble, steps + 2)
-        split = p != abi.GBF_PREC_F64
-        if split:
-            r.set_outputs(abi.GBF_OUT_MASS | abi.GBF_OUT_CFL, steps + 2)
+        if p != abi.GBF_PREC_F64:
+            r.set_outputs(abi.GBF_OUT_MASS | flags, steps + 2)
         r.upload_initial()
         r.step(steps)
         out = [(r.download(i, "P1"), r.download(i, "S2")) for i in range(len(members))] if ensemble else \
             [(r.download(0, "P1"), r.download(0, "S2"))]
         mass = r.mass_history(steps)
-        cfl = r.cfl_history(steps) if split else None
+        cfl = r.cfl_history(steps) if (flags & abi.GBF_OUT_CFL) and p != abi.GBF_PREC_F64 else None
+        st = r.status()
         r.close()
-        return out, mass, cfl
+        return out, mass, cfl, st
 
-    got, mg, cfl = run(prec)
-    ref, mr, _ = run(abi.GBF_PREC_F64)
+    got, mg, cfl, s1 = run(prec)
+    ref, mr, _, s2 = run(abi.GBF_PREC_F64)
     ds = max(float(np.abs(a[1] - b[1]).max()) for a, b in zip(got, ref))
     num = sum(float(np.sum((a[0] - b[0]) ** 2)) for a, b in zip(got, ref))
     den = sum(float(np.sum(b[0] ** 2)) for b in ref)
@@ -447,8 +665,19 @@ def accuracy_block(pkg, O, members, prec, ensemble, steps=20):
     drift = float(np.max(np.abs(mg - mr) / scale * (np.abs(mr) > 0)))
     block = {"vs": "plain FP64 GPU path of the same members (pinned to the oracle at 1e-12)", "steps": steps,
              "max_dS": ds, "rel_l2_P": (num / den) ** 0.5, "phase_mass_rel_diff_max": drift, "S_moved_max": moved,
-             "cfl_max": [float(cfl[..., 0].max()), float(cfl[..., 1].max())]}
-    # the oracle itself on the smallest member
+             "status": [int(s1), int(s2)]}
+    if cfl is not None:
+        block["cfl_max"] = [float(cfl[..., 0].max()), float(cfl[..., 1].max())]
+    return block, got
+
+
+def accuracy_block(pkg, O, members, prec, ensemble, steps=20):
+    """The measured form against plain FP64 on the same members and steps
+    (the GPU FP64 path, itself pinned to the oracle at 1e-12), and against
+    the oracle on the smallest member: max|dS|, relative L2 of P, relative
+    phase-mass difference per step, and how far S moved (max|S - S0|)."""
+    abi = pkg.abi
+    block, got = compare(pkg, members, prec, ensemble, steps, abi.GBF_OUT_CFL)
     i = min(range(len(members)), key=lambda q: members[q].ncells)
     mem = members[i]
     st = O.State(mem.model, mem.media, mem.K, mem.phi)
@@ -462,62 +691,50 @@ def accuracy_block(pkg, O, members, prec, ensemble, steps=20):
     return block
 
 
+def accuracy_stiff(pkg, lib, wl, members, prec, ensemble, steps=30, count=5):
+    """The same comparison where the saturation moves: up to `count` members
+    spanning the sizes, at the reference parameter file's compressibilities
+    (1e-4 water, 1e-8 DNAPL) with 2 kg/s injected at half their stable dt."""
+    import copy
+    order = sorted(range(len(members)), key=lambda q: members[q].ncells)
+    pick = sorted({order[round(k * (len(order) - 1) / max(1, count - 1))] for k in range(min(count, len(order)))})
+    sel = []
+    for q in pick:
+        m = copy.copy(members[q])
+        m.model = members[q].model.copy()
+        m.model.beta1, m.model.beta2 = 1e-4, 1e-8
+        if m.model.source_mode == pkg.abi.GBF_SOURCE_RATE:
+            m.model.rate = 2.0
+        m.model.newton_tol = 1e-11
+        sel.append(wl.set_stable_dt(lib, m, 0.5))
+    block, _ = compare(pkg, sel, prec, ensemble, steps)
+    block["members"] = pick
+    block["params"] = "beta1 1e-4, beta2 1e-8, 2 kg/s, dt = 0.5 x stable"
+    return block
+
+
+# ------------------------------------------------------------- reference arm
+
 def run_reference(args, rank, world):
-    """The reference CPU algorithm (oracle) on all host cores, same workload and metric."""
+    """The reference CPU algorithm (oracle) on all host cores, same workload,
+    metric and config; inputs from libgbf_inputs.so (libgbflow not loaded)."""
     if rank != 0:
         return None
     pkg = ge.load_package()
-    lib = pkg.load_library()
     O = ge.load_oracle_module()
-    cfg, _, p = args.workload.partition("_")
-    members, desc, _ = make_members(pkg, lib, cfg, args.cube)
-    threads = os.cpu_count()
-    os.environ["OMP_NUM_THREADS"] = str(threads)
-    orc = O.Oracle(pkg.abi)
-    # bounded sample per step: whole members, largest first, until ~budget
-    budget = max(1.0, 120.0 / max(1, args.steps + args.warmup))
-    states = []
-
-    def state(mem):
-        st = O.State(mem.model, mem.media, mem.K, mem.phi)
-        P, S = mem.initial_state()
-        st["P1"][...] = P
-        st["S2"][...] = S
-        return st
-
-    order = sorted(members, key=lambda x: -x.ncells)
-
-    def one_step():
-        t0 = time.perf_counter()
-        c = 0
-        for q, mem in enumerate(order):
-            if q >= len(states):
-                states.append(state(mem))
-            orc.step(states[q], 1)
-            c += mem.ncells
-            if time.perf_counter() - t0 > budget:
-                break
-        return c, time.perf_counter() - t0
-
-    for _ in range(args.warmup):
-        one_step()
-    tot_c, tot_t = 0, 0.0
-    for _ in range(args.steps):
-        c, t = one_step()
-        tot_c += c
-        tot_t += t
-    v = tot_c / tot_t
-    sample = f"{len(states)} of {len(members)} member(s) per step, each step bounded to ~{budget:.1f} s"
+    lib = O.inputs_library(pkg.abi)
+    W = Workload(pkg, lib, args.workload, args.cube, 0, world, args.members)
+    cb = reference_cpu_run(O, pkg.abi, W.members, args.steps, args.warmup, step_budget(args))
+    v = cb["value"]
     return {"metric": METRIC, "impl": "reference", "value": v, "unit": "cell-steps/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / args.steps,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * cb.pop("seconds") / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded fields with the configuration's shapes and statistics)",
-            "config": {"workload": args.workload, "desc": desc + " (reference CPU algorithm, FP64)",
-                       "cells": sum(m.ncells for m in members)},
+            "config": W.config(),
+            "details": {"arm": "reference CPU algorithm in FP64 (the bit-exact port of cpu.cpp) on rank 0's "
+                               "members; inputs from libgbf_inputs.so"},
             "e2e": {"value": v, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "cpu_baseline": {"value": v, "unit": "cell-steps/s", "cores": threads, "kind": "port",
-                             "sample": sample + "; oracle = bit-exact restatement of the reference cpu.cpp "
-                                                "(OpenMP over i), 7 Newton iterations"}}
+            "cpu_baseline": cb}
 
 
 def main():
@@ -526,10 +743,9 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="config4_splitdefect")
+    ap.add_argument("--workload", default="config4_split")
     ap.add_argument("--cube", type=int, default=0, help="override the grid edge of config1 (profiling runs)")
     ap.add_argument("--members", type=int, default=0, help="first N members of an ensemble (profiling runs)")
-    ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-compare", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")

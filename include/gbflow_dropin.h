@@ -67,6 +67,13 @@ extern "C" {
    intermediate arrays are materialised on demand by load_data_to_host). */
 int gbf_dropin_set_mode(int mode);
 int gbf_dropin_get_mode(void);
+/* The gbflow domain behind arrays from device_memory_alloc (keyed by their
+   device P1 pointer) in fused mode, once the first step created it; NULL
+   otherwise. It accepts the gbf_domain_* timing and status calls of
+   gbflow.h (gbf_domain_set_timing, gbf_domain_kernel_times,
+   gbf_domain_status); the drop-in owns it and frees it in
+   device_memory_free. No counterpart in the reference. */
+struct gbf_domain* gbf_dropin_domain(const double* dev_P1);
 #ifdef __cplusplus
 }
 #endif

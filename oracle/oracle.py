@@ -3,8 +3,11 @@
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
 this module; it is the checker and never the thing measured or shipped.
 
-Two libraries are wrapped:
+Three libraries are wrapped:
   * _build/libgbf_oracle.so — the C restatement (gbf_oracle.c), always built;
+  * _build/libgbf_inputs.so — the product's seeded field generator and
+    stability bound (gbf_fields.cpp) built alone, so that the timed reference
+    CPU run makes the same inputs without loading libgbflow;
   * _ref/libgbf_refcpu.so   — the reference's own cpu.cpp/main.cpp/
     no_communication.cpp compiled from their sources (only where the
     reference sources exist at build time).
@@ -20,6 +23,7 @@ import numpy as np
 HERE = pathlib.Path(__file__).resolve().parent
 ORACLE_SO = HERE / "_build" / "libgbf_oracle.so"
 REF_SO = HERE / "_ref" / "libgbf_refcpu.so"
+INPUTS_SO = HERE / "_build" / "libgbf_inputs.so"
 
 # Field order of the reference's ptr_Arrays after x, y, z (defines.h:44).
 ARRAY_ORDER = ["P1", "P2", "S2", "ro1", "ro2", "u1x", "u1y", "u1z", "u2x", "u2y", "u2z",
@@ -29,6 +33,30 @@ ARRAY_ORDER = ["P1", "P2", "S2", "ro1", "ro2", "u1x", "u1y", "u1z", "u2x", "u2y"
 def build() -> None:
     """Compile the oracle (and the reference library when its sources exist)."""
     subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
+
+
+_inputs = None
+
+
+def inputs_library(abi):
+    """libgbf_inputs.so with the signatures of gbf_fill_lognormal_K,
+    gbf_fill_porosity and gbf_stable_dt (the same C symbols and results as
+    libgbflow's)."""
+    global _inputs
+    if _inputs is None:
+        if not INPUTS_SO.exists():
+            build()
+        lib = ctypes.CDLL(str(INPUTS_SO))
+        c_int, c_double, c_void_p = ctypes.c_int, ctypes.c_double, ctypes.c_void_p
+        lib.gbf_fill_lognormal_K.restype = c_int
+        lib.gbf_fill_lognormal_K.argtypes = [c_int, c_int, c_int, ctypes.c_uint64, c_double, c_double, c_double,
+                                             c_void_p]
+        lib.gbf_fill_porosity.restype = c_int
+        lib.gbf_fill_porosity.argtypes = [c_int, c_int, c_int, ctypes.c_uint64, c_double, c_double, c_void_p]
+        lib.gbf_stable_dt.restype = c_double
+        lib.gbf_stable_dt.argtypes = [ctypes.POINTER(abi.GbfModel), ctypes.POINTER(abi.GbfCells), c_double]
+        _inputs = lib
+    return _inputs
 
 
 class Consts(ctypes.Structure):

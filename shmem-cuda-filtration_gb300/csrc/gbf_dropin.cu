@@ -313,4 +313,8 @@ int gbf_dropin_set_mode(int mode) {
   return GBF_OK;
 }
 int gbf_dropin_get_mode(void) { return g_mode; }
+gbf_domain* gbf_dropin_domain(const double* dev_P1) {
+  DropinDomain* dd = find_domain(dev_P1);
+  return dd ? dd->fused : nullptr;
+}
 }

@@ -11,6 +11,14 @@
 //     truncated at 3 sigma, mirrored at the faces), then renormalisation of
 //     the smoothed field to zero mean and unit variance;
 //   * ln K = ln(K_geo) + sigma_lnK * z, K = exp(ln K) rounded to FP32.
+// It also holds the stability bound gbf_stable_dt, which the workloads derive
+// their time step from.
+//
+// The file needs the host compiler only. Built with GBF_INPUTS_STANDALONE it
+// makes a small library of its own (libgbf_inputs.so, oracle/Makefile), so
+// that a CPU-only caller — the timed reference CPU run — generates the same
+// inputs without loading libgbflow; both builds use -ffp-contract=off and give
+// the same bits (tested).
 #include <math.h>
 #include <stdint.h>
 
@@ -18,7 +26,13 @@
 #include <thread>
 #include <vector>
 
+#ifdef GBF_INPUTS_STANDALONE
+#include "gbflow.h"
+// Alone, errors are returned without libgbflow's sticky status.
+static int gbf_fail(int s, const char*) { return s; }
+#else
 #include "gbf_internal.h"
+#endif
 
 namespace {
 
@@ -125,6 +139,53 @@ int gbf_fill_porosity(int nx, int ny, int nz, uint64_t seed, double base, double
   const uint64_t s = splitmix64(seed ^ 0x5bd1e995ull);
   parallel_for(n, [&](size_t c) { phi_out[c] = (float)(base + amp * (2.0 * u01(s, c) - 1.0)); });
   return GBF_OK;
+}
+
+// Explicit-scheme bound of the pressure equation. Its diffusivity is
+// D = K lambda_t(S) / (phi c_t(S)) with the total mobility
+// lambda_t = kr1/mu1 + kr2/mu2 (Brooks-Corey, as in cpu.cpp:60-62) and the
+// total compressibility c_t = (1 - S) beta1 + S beta2, maximised over the
+// saturations the source can produce (S in [0, S2_gr] for the reference's
+// Dirichlet patch, [0, 1 - S_wr) for a mass rate); then
+// dt <= 1 / (2 D (1/h1^2 + kv/h2^2 + 1/h3^2)). It bounds the pressure
+// diffusion only (advection limits are far looser in the configurations used
+// here).
+double gbf_stable_dt(const gbf_model* m, const gbf_cells* cells, double safety) {
+  if (!m) return 0;
+  const size_t n = (size_t)m->nx * m->ny * m->nz;
+  double ratio[2] = {0, 0};  // max over S of lambda_t / c_t, per media
+  for (int md = 0; md < 2; md++) {
+    const double swr = m->S_wr[md], lam = m->lambda[md];
+    const double scap = (m->source_mode == GBF_SOURCE_DIRICHLET_PATCH) ? fmin(m->S2_gr, 1 - swr) : 1 - swr;
+    for (int q = 0; q <= 256; q++) {
+      const double s = scap * q / 256.0;
+      const double se = fmax(0.0, (1 - s - swr) / (1 - swr));
+      const double kr1 = pow(se, (2 + 3 * lam) / lam);
+      const double kr2 = (1 - se) * (1 - se) * (1 - pow(se, (2 + lam) / lam));
+      const double ct = (1 - s) * m->beta1 + s * m->beta2;
+      if (ct > 0) ratio[md] = fmax(ratio[md], (kr1 / m->mu1 + kr2 / m->mu2) / ct);
+    }
+  }
+  double dmax = 0;
+  const bool per_cell = cells && (cells->K || cells->phi);
+  if (!per_cell) {
+    for (int md = 0; md < 2; md++) {
+      bool used = !(cells && cells->media) ? (md == 0) : false;
+      if (cells && cells->media)
+        for (size_t c = 0; c < n && !used; c++) used = cells->media[c] == md;
+      if (used) dmax = fmax(dmax, m->K[md] * ratio[md] / m->m[md]);
+    }
+  } else {
+    for (size_t c = 0; c < n; c++) {
+      int md = (cells->media) ? cells->media[c] : 0;
+      double K = cells->K ? (double)cells->K[c] : m->K[md];
+      double phi = cells->phi ? (double)cells->phi[c] : m->m[md];
+      dmax = fmax(dmax, K * ratio[md] / phi);
+    }
+  }
+  double inv = 1.0 / (m->h1 * m->h1) + m->kv / (m->h2 * m->h2) + 1.0 / (m->h3 * m->h3);
+  if (dmax <= 0 || inv <= 0) return 0;
+  return safety / (2.0 * dmax * inv);
 }
 
 }  // extern "C"

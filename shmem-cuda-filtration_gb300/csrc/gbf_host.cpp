@@ -174,53 +174,6 @@ void gbf_model_reference(gbf_model* m, int nx, int ny, int nz, double dt) {
   *m = r;
 }
 
-// Explicit-scheme bound of the pressure equation. Its diffusivity is
-// D = K lambda_t(S) / (phi c_t(S)) with the total mobility
-// lambda_t = kr1/mu1 + kr2/mu2 (Brooks-Corey, as in cpu.cpp:60-62) and the
-// total compressibility c_t = (1 - S) beta1 + S beta2, maximised over the
-// saturations the source can produce (S in [0, S2_gr] for the reference's
-// Dirichlet patch, [0, 1 - S_wr) for a mass rate); then
-// dt <= 1 / (2 D (1/h1^2 + kv/h2^2 + 1/h3^2)). It bounds the pressure
-// diffusion only (advection limits are far looser in the configurations used
-// here).
-double gbf_stable_dt(const gbf_model* m, const gbf_cells* cells, double safety) {
-  if (!m) return 0;
-  const size_t n = (size_t)m->nx * m->ny * m->nz;
-  double ratio[2] = {0, 0};  // max over S of lambda_t / c_t, per media
-  for (int md = 0; md < 2; md++) {
-    const double swr = m->S_wr[md], lam = m->lambda[md];
-    const double scap = (m->source_mode == GBF_SOURCE_DIRICHLET_PATCH) ? fmin(m->S2_gr, 1 - swr) : 1 - swr;
-    for (int q = 0; q <= 256; q++) {
-      const double s = scap * q / 256.0;
-      const double se = fmax(0.0, (1 - s - swr) / (1 - swr));
-      const double kr1 = pow(se, (2 + 3 * lam) / lam);
-      const double kr2 = (1 - se) * (1 - se) * (1 - pow(se, (2 + lam) / lam));
-      const double ct = (1 - s) * m->beta1 + s * m->beta2;
-      if (ct > 0) ratio[md] = fmax(ratio[md], (kr1 / m->mu1 + kr2 / m->mu2) / ct);
-    }
-  }
-  double dmax = 0;
-  const bool per_cell = cells && (cells->K || cells->phi);
-  if (!per_cell) {
-    for (int md = 0; md < 2; md++) {
-      bool used = !(cells && cells->media) ? (md == 0) : false;
-      if (cells && cells->media)
-        for (size_t c = 0; c < n && !used; c++) used = cells->media[c] == md;
-      if (used) dmax = fmax(dmax, m->K[md] * ratio[md] / m->m[md]);
-    }
-  } else {
-    for (size_t c = 0; c < n; c++) {
-      int md = (cells->media) ? cells->media[c] : 0;
-      double K = cells->K ? (double)cells->K[c] : m->K[md];
-      double phi = cells->phi ? (double)cells->phi[c] : m->m[md];
-      dmax = fmax(dmax, K * ratio[md] / phi);
-    }
-  }
-  double inv = 1.0 / (m->h1 * m->h1) + m->kv / (m->h2 * m->h2) + 1.0 / (m->h3 * m->h3);
-  if (dmax <= 0 || inv <= 0) return 0;
-  return safety / (2.0 * dmax * inv);
-}
-
 int gbf_model_validate(const gbf_model* m, const gbf_cells* cells, int check_dt) {
   if (!m) return gbf_fail(GBF_ERR_ARG, "model is NULL");
   if (m->nx < 3 || m->ny < 3 || m->nz < 3) return gbf_fail(GBF_ERR_ARG, "grid dimensions must be >= 3");

@@ -58,6 +58,8 @@ GbfSplitConsts gbf_split_consts(const gbf_model& m) {
   C.V = V;
   C.ro01b1_d = m.ro01 * m.beta1;
   C.ro02b2_d = m.ro02 * m.beta2;
+  C.ro01b1_lo = (float)(C.ro01b1_d - (double)C.ro01b1);
+  C.ro02b2_lo = (float)(C.ro02b2_d - (double)C.ro02b2);
   C.gh1 = (float)(m.g * m.ro01 * m.beta1 * m.h2);
   C.gh2 = (float)(m.g * m.ro02 * m.beta2 * m.h2);
   C.ghd = (float)(m.g * (m.ro02 - m.ro01) * m.h2);

@@ -21,6 +21,7 @@ struct GbfSplitConsts {
   float ro01, ro02, beta1, beta2, bmax;  // bmax = max(beta1, beta2)
   float nmr1, nmr2;      // -rho01 / mu1, -rho02 / mu2
   float ro01b1, ro02b2;  // rho01 beta1, rho02 beta2
+  float ro01b1_lo, ro02b2_lo;  // their FP64 values' remainders (pairs; the residual-correction step)
   float K[2], m[2], e1[2], e2[2], m_inv_lam[2], inv_lam_1mswr[2], P_d[2];
   float se_b[2];  // S_e = 1 + se_b S = (1 - S_wr - S) / (1 - S_wr)
   double H_d, beta1_d, beta2_d, ro01_d, ro02_d, dtsrc_d, V;

@@ -769,6 +769,68 @@ __device__ __forceinline__ void split_cells(const GbfSplitConsts& C, const GbfCe
     Sn = L::make([&](int n) { return dsn[n]; });
     Pk = L::make([&](int n) { return Pkn[n]; });
   }
+  if constexpr (MR == kMassDefectDF) {
+    // One residual-correction Newton step per cell (iterative refinement):
+    // the nonlinear residual of both mass equations at the state (p1, S1) the
+    // FP32 Newton reached, against the step's targets held at FP64 precision
+    // (the pair defect plus this step's increment: T1 - c1 (1 - S1) =
+    // D1 + dm1 + c1 (S1 - S0), T2 - c2 S1 = D2 + dm2 + src - c2 (S1 - S0)),
+    // evaluated with error-free transformations (TwoSum, TwoProduct) so that
+    // it is exact to about 2^-48 of the defects, where the FP32 Newton's own
+    // residual rounds at 2^-24 of them (of the masses themselves at
+    // compressibility 1e-4). The capillary pressure, its derivative (stiff
+    // near residual saturation, S_e -> 0) and the Jacobian are taken afresh
+    // at (p1, S1); the step's increments are applied in FP32.
+    //   r1 = (rho01 beta1 p1 + e1) (1 - S1) - T1',  r2 = (rho02 beta2 (p1 + P_k(S1)) + e2) S1 - T2'
+    float dpn[N], dsn[N], Pkn[N];
+#pragma unroll
+    for (int n = 0; n < N; n++) {
+      const float s0 = in[n].S0, S1 = L::get(Sn, n), p1 = L::get(dPn, n);
+      float dPk1;
+      const float Pk1 = split_Pk(C, md, S1, dPk1);
+      const float ds1 = __fsub_rn(S1, s0);
+      const float t1 = __fmaf_rn(rw.c1, ds1, L::get(dm1, n));
+      const float t2 = insrc[n] ? __fadd_rn(__fmaf_rn(-rw.c2, ds1, srcf[n]),
+                                            __fadd_rn(__fmul_rn(L::get(gs, n), L::get(nrphi, n)), srcl[n]))
+                                : __fmaf_rn(-rw.c2, ds1, L::get(dm2, n));
+      const GbfDF T1 = Wide<true>::add_f(M1[n], t1), T2 = Wide<true>::add_f(M2[n], t2);
+      // water: A1 = rho01 beta1 p1 + e1 (pair), times 1 - S1 (exact as a pair)
+      const float a1 = __fmul_rn(C.ro01b1, p1);
+      const float a1e = __fmaf_rn(C.ro01b1_lo, p1, __fmaf_rn(C.ro01b1, p1, -a1));
+      const GbfDF A1s = df_two_sum(a1, rw.e1);
+      const float A1lo = __fadd_rn(A1s.lo, a1e);
+      const GbfDF B1 = df_two_sum(1.f, -S1);
+      const float f1 = __fmul_rn(A1s.hi, B1.hi);
+      const float f1e = __fmaf_rn(A1s.hi, B1.lo, __fmaf_rn(A1lo, B1.hi, __fmaf_rn(A1s.hi, B1.hi, -f1)));
+      const float r1c = __fadd_rn(__fsub_rn(f1, T1.hi), __fsub_rn(f1e, T1.lo));
+      // DNAPL: A2 = rho02 beta2 (p1 + P_k) + e2 (pair), times S1
+      const GbfDF q = df_two_sum(p1, Pk1);
+      const float a2 = __fmul_rn(C.ro02b2, q.hi);
+      const float a2e = __fmaf_rn(C.ro02b2, q.lo, __fmaf_rn(C.ro02b2_lo, q.hi, __fmaf_rn(C.ro02b2, q.hi, -a2)));
+      const GbfDF A2s = df_two_sum(a2, rw.e2);
+      const float A2lo = __fadd_rn(A2s.lo, a2e);
+      const float f2 = __fmul_rn(A2s.hi, S1);
+      const float f2e = __fmaf_rn(A2lo, S1, __fmaf_rn(A2s.hi, S1, -f2));
+      const float r2c = __fadd_rn(__fsub_rn(f2, T2.hi), __fsub_rn(f2e, T2.lo));
+      // the Jacobian at (p1, S1) and one Newton step
+      const float Pp = __fmaf_rn((float)j, C.H, p1);
+      const float a = __fmaf_rn(C.beta1, Pp, 1.f);
+      const float b = __fmaf_rn(C.beta2, __fadd_rn(Pp, Pk1), 1.f);
+      const float K11 = __fmul_rn(C.ro01b1, __fsub_rn(1.f, S1));
+      const float mK12 = __fmul_rn(C.ro01, a);
+      const float K21 = __fmul_rn(C.ro02b2, S1);
+      const float K22 = __fmul_rn(C.ro02, __fmaf_rn(__fmul_rn(C.beta2, dPk1), S1, b));
+      const float inv = split_rcp(-__fmaf_rn(K11, K22, __fmul_rn(mK12, K21)));
+      const float ep = __fmul_rn(inv, __fmaf_rn(K22, r1c, __fmul_rn(mK12, r2c)));
+      const float es = __fmul_rn(inv, __fmaf_rn(K11, r2c, -__fmul_rn(K21, r1c)));
+      dpn[n] = __fadd_rn(p1, ep);
+      dsn[n] = __fadd_rn(S1, es);
+      Pkn[n] = __fmaf_rn(dPk1, es, Pk1);  // P_k at the final S, to first order in the correction
+    }
+    dPn = L::make([&](int n) { return dpn[n]; });
+    Sn = L::make([&](int n) { return dsn[n]; });
+    Pk = L::make([&](int n) { return Pkn[n]; });
+  }
   const F fin = vadd(dPn, Sn);  // NaN and infinities carry through the sum
 #pragma unroll
   for (int n = 0; n < N; n++) {

@@ -87,6 +87,12 @@ class DropIn:
         f["Device_Initialize"].argtypes = [i, ctypes.POINTER(i), ctypes.POINTER(i), ctypes.POINTER(i), i, C]
         self.f = f
         lib.gbf_dropin_set_mode.argtypes = [ctypes.c_int]
+        lib.gbf_dropin_domain.restype = ctypes.c_void_p
+        lib.gbf_dropin_domain.argtypes = [ctypes.c_void_p]
+
+    def domain(self, dev_P1) -> int | None:
+        """Handle of the gbflow domain behind fused-mode arrays (gbf_dropin_domain)."""
+        return self.lib.gbf_dropin_domain(dev_P1)
 
     def set_mode(self, mode: int):
         abi.check(self.lib.gbf_dropin_set_mode(mode), "gbf_dropin_set_mode")

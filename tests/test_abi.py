@@ -135,6 +135,25 @@ def test_noalloc_boundary_refuses_grids_beyond_its_array(lib, abi):
     lib.gbf_clear_status()
 
 
+def test_standalone_inputs_library_gives_the_same_inputs(lib, abi, O, pkg):
+    """libgbf_inputs.so (gbf_fields.cpp built alone, which the timed reference
+    CPU run uses so that it does not load libgbflow) makes the same K, phi and
+    stable dt as libgbflow, bit for bit, for workloads of every configuration."""
+    from importlib import import_module
+    wl = import_module(pkg.__name__ + ".workloads")
+    inp = O.inputs_library(abi)
+    assert inp is not lib
+    pairs = [(wl.config0(lib), wl.config0(inp)), (wl.config1(lib, n=40), wl.config1(inp, n=40))]
+    pairs += list(zip(wl.config4(lib, members=3), wl.config4(inp, members=3)))
+    pairs += list(zip(wl.config3(lib, members=2), wl.config3(inp, members=2)))
+    for a, b in pairs:
+        assert a.model.dt == b.model.dt and a.model.dt > 0
+        for x, y in ((a.K, b.K), (a.phi, b.phi)):
+            assert (x is None) == (y is None)
+            if x is not None:
+                assert np.array_equal(x.view(np.uint32), y.view(np.uint32))
+
+
 def test_lognormal_field_statistics_and_determinism(lib):
     shape = (48, 40, 32)
     K = np.empty(shape, np.float32)

@@ -43,3 +43,26 @@ def test_reference_arm_under_torchrun_prints_once():
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [ln for ln in r.stdout.splitlines() if ln.strip().startswith("{")]
     assert len(lines) == 1 and json.loads(lines[0])["impl"] == "reference"
+
+
+def test_reference_arm_loads_no_gpu_library_and_prints_the_same_config():
+    """The reference arm makes its inputs with libgbf_inputs.so and never maps
+    libgbflow; its `config` equals the one the GPU arm builds for the same
+    workload from libgbflow's generator."""
+    code = (
+        "import json, sys, types; sys.path.insert(0, %r); import bench, __graft_entry__ as ge\n"
+        "a = types.SimpleNamespace(workload='config4_split', cube=0, members=3, steps=1, warmup=0)\n"
+        "out = bench.run_reference(a, 0, 1)\n"
+        "maps = open('/proc/self/maps').read()\n"
+        "print(json.dumps({'config': out['config'], 'gbflow': 'libgbflow' in maps,\n"
+        "                  'inputs': 'libgbf_inputs' in maps, 'oracle': 'libgbf_oracle' in maps}))\n" % str(ROOT))
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    d = json.loads(r.stdout.strip().splitlines()[-1])
+    assert not d["gbflow"] and d["inputs"] and d["oracle"]
+    import __graft_entry__ as ge
+    sys.path.insert(0, str(ROOT))
+    import bench
+    pkg = ge.load_package()
+    W = bench.Workload(pkg, pkg.load_library(), "config4_split", 0, 0, 1, 3)
+    assert W.config() == d["config"]
