@@ -163,8 +163,8 @@ PRECISIONS = {"f64": ("GBF_PREC_F64", "plain FP64", "f64"),
 ENSEMBLE_BASE = {"config3": 96, "config4": 256}
 DESC = {"config0": "config 0: 40^3 homogeneous single grid",
         "config1": "config 1: {n}^3 heterogeneous single grid",
-        "config1_dropin": "config 1's {n}^3 grid in the reference's media-table physics (Dirichlet patch, 7 "
-                          "Newton iterations: all that the defines.h calls express)",
+        "config1_dropin": "config 1's {n}^3 grid in the reference's media-table physics (Dirichlet patch, "
+                          "reference boundary rules: all that the defines.h calls express)",
         "config2": "config 2: 512x512x256 heterogeneous single grid (sigma_lnK 1.5)",
         "config3": "config 3: {m} realizations, edges in {{64,96,128,160}}",
         "config4": "config 4: {m} realizations, edges 48..128 step 16, anisotropic"}
@@ -589,7 +589,7 @@ def run_ours(args, rank, world):
            "data": "synthetic (seeded fields with the configuration's shapes and statistics)",
            "config": W.config(),
            "details": {"dt_used_range": [min(m.model.dt for m in members), max(m.model.dt for m in members)],
-                       "newton": ("reference: 7 iterations" if p == "dropin" else
+                       "newton": ("converge-and-exit (tol 1e-11, at most the reference's 7)" if p == "dropin" else
                                   "FP64: converge-and-exit (tol 1e-11, max 7); split: increment Newton, a second "
                                   "iteration where nonlinear, and (split) one residual-correction step"),
                        "tuning": tuning, "graphs": ensemble, "rank_cells": cells,

@@ -151,7 +151,22 @@ void orc_velocity(const gbf_model* m, gbf_arrays a) {
    (Xm, rm), (Xp, rp) the mobility Xi and density ro at the centre, minus and
    plus neighbours, multiplied in the reference's left-to-right order. */
 static double upwind_div(double x1, double x2, double Xc, double rc, double Xm, double rm,
+                         double Xp, double rp, double h);
+
+/* Experiment switch (off by default; the tests only): with it on, the flux
+   stage rounds every upwinded mobility Xi*ro to FP32 before it multiplies the
+   face potential, and nothing else: the oracle then shows what FP32
+   mobilities alone, in an otherwise FP64 scheme, do to the phase masses. */
+static int g_fp32_mobilities = 0;
+void orc_set_fp32_mobilities(int on) { g_fp32_mobilities = on; }
+
+static double upwind_div(double x1, double x2, double Xc, double rc, double Xm, double rm,
                          double Xp, double rp, double h) {
+  if (g_fp32_mobilities) {
+    const double Lc = (float)(Xc * rc), Lm = (float)(Xm * rm), Lp = (float)(Xp * rp);
+    return (((x2 + fabs(x2)) / 2.0 - (x1 - fabs(x1)) / 2.0) * (-1) * Lc - (x1 + fabs(x1)) / 2.0 * (-1) * Lm +
+            (x2 - fabs(x2)) / 2.0 * (-1) * Lp) / h;
+  }
   return (((x2 + fabs(x2)) / 2.0 - (x1 - fabs(x1)) / 2.0) * (-1) * Xc * rc -
           (x1 + fabs(x1)) / 2.0 * (-1) * Xm * rm +
           (x2 - fabs(x2)) / 2.0 * (-1) * Xp * rp) / h;

@@ -151,7 +151,13 @@ class Oracle:
         lib.orc_step.argtypes = [PM, PC, abi.GbfArrays, ctypes.c_int, ctypes.c_void_p]
         lib.orc_mass_totals.argtypes = [PM, PC, abi.GbfArrays, ctypes.c_void_p]
         lib.orc_in_rate_patch.argtypes = [PM, ctypes.c_int, ctypes.c_int]
+        lib.orc_set_fp32_mobilities.argtypes = [ctypes.c_int]
         self.lib = lib
+
+    def fp32_mobilities(self, on: bool):
+        """Experiment switch: round the flux stage's upwinded mobilities to
+        FP32, everything else FP64 (off: the bit-exact reference)."""
+        self.lib.orc_set_fp32_mobilities(int(on))
 
     def _call(self, name, st: State, with_cells=True):
         m = ctypes.byref(st.model)

@@ -775,61 +775,70 @@ __device__ __forceinline__ void split_cells(const GbfSplitConsts& C, const GbfCe
     // FP32 Newton reached, against the step's targets held at FP64 precision
     // (the pair defect plus this step's increment: T1 - c1 (1 - S1) =
     // D1 + dm1 + c1 (S1 - S0), T2 - c2 S1 = D2 + dm2 + src - c2 (S1 - S0)),
-    // evaluated with error-free transformations (TwoSum, TwoProduct) so that
-    // it is exact to about 2^-48 of the defects, where the FP32 Newton's own
-    // residual rounds at 2^-24 of them (of the masses themselves at
-    // compressibility 1e-4). The capillary pressure, its derivative (stiff
-    // near residual saturation, S_e -> 0) and the Jacobian are taken afresh
-    // at (p1, S1); the step's increments are applied in FP32.
+    // evaluated with error-free transformations (TwoSum, FastTwoSum,
+    // TwoProduct through FMA: Knuth, Dekker) so that only the final, small
+    // residual rounds, where the FP32 Newton's own residual rounds at 2^-24
+    // of the defects (of the masses themselves at compressibility 1e-4). The
+    // capillary pressure, its derivative (stiff near residual saturation,
+    // S_e -> 0) and the Jacobian are taken afresh at (p1, S1); the step's
+    // increments are applied in FP32.
     //   r1 = (rho01 beta1 p1 + e1) (1 - S1) - T1',  r2 = (rho02 beta2 (p1 + P_k(S1)) + e2) S1 - T2'
-    float dpn[N], dsn[N], Pkn[N];
-#pragma unroll
-    for (int n = 0; n < N; n++) {
-      const float s0 = in[n].S0, S1 = L::get(Sn, n), p1 = L::get(dPn, n);
-      float dPk1;
-      const float Pk1 = split_Pk(C, md, S1, dPk1);
-      const float ds1 = __fsub_rn(S1, s0);
-      const float t1 = __fmaf_rn(rw.c1, ds1, L::get(dm1, n));
-      const float t2 = insrc[n] ? __fadd_rn(__fmaf_rn(-rw.c2, ds1, srcf[n]),
-                                            __fadd_rn(__fmul_rn(L::get(gs, n), L::get(nrphi, n)), srcl[n]))
-                                : __fmaf_rn(-rw.c2, ds1, L::get(dm2, n));
-      const GbfDF T1 = Wide<true>::add_f(M1[n], t1), T2 = Wide<true>::add_f(M2[n], t2);
-      // water: A1 = rho01 beta1 p1 + e1 (pair), times 1 - S1 (exact as a pair)
-      const float a1 = __fmul_rn(C.ro01b1, p1);
-      const float a1e = __fmaf_rn(C.ro01b1_lo, p1, __fmaf_rn(C.ro01b1, p1, -a1));
-      const GbfDF A1s = df_two_sum(a1, rw.e1);
-      const float A1lo = __fadd_rn(A1s.lo, a1e);
-      const GbfDF B1 = df_two_sum(1.f, -S1);
-      const float f1 = __fmul_rn(A1s.hi, B1.hi);
-      const float f1e = __fmaf_rn(A1s.hi, B1.lo, __fmaf_rn(A1lo, B1.hi, __fmaf_rn(A1s.hi, B1.hi, -f1)));
-      const float r1c = __fadd_rn(__fsub_rn(f1, T1.hi), __fsub_rn(f1e, T1.lo));
-      // DNAPL: A2 = rho02 beta2 (p1 + P_k) + e2 (pair), times S1
-      const GbfDF q = df_two_sum(p1, Pk1);
-      const float a2 = __fmul_rn(C.ro02b2, q.hi);
-      const float a2e = __fmaf_rn(C.ro02b2, q.lo, __fmaf_rn(C.ro02b2_lo, q.hi, __fmaf_rn(C.ro02b2, q.hi, -a2)));
-      const GbfDF A2s = df_two_sum(a2, rw.e2);
-      const float A2lo = __fadd_rn(A2s.lo, a2e);
-      const float f2 = __fmul_rn(A2s.hi, S1);
-      const float f2e = __fmaf_rn(A2lo, S1, __fmaf_rn(A2s.hi, S1, -f2));
-      const float r2c = __fadd_rn(__fsub_rn(f2, T2.hi), __fsub_rn(f2e, T2.lo));
-      // the Jacobian at (p1, S1) and one Newton step
-      const float Pp = __fmaf_rn((float)j, C.H, p1);
-      const float a = __fmaf_rn(C.beta1, Pp, 1.f);
-      const float b = __fmaf_rn(C.beta2, __fadd_rn(Pp, Pk1), 1.f);
-      const float K11 = __fmul_rn(C.ro01b1, __fsub_rn(1.f, S1));
-      const float mK12 = __fmul_rn(C.ro01, a);
-      const float K21 = __fmul_rn(C.ro02b2, S1);
-      const float K22 = __fmul_rn(C.ro02, __fmaf_rn(__fmul_rn(C.beta2, dPk1), S1, b));
-      const float inv = split_rcp(-__fmaf_rn(K11, K22, __fmul_rn(mK12, K21)));
-      const float ep = __fmul_rn(inv, __fmaf_rn(K22, r1c, __fmul_rn(mK12, r2c)));
-      const float es = __fmul_rn(inv, __fmaf_rn(K11, r2c, -__fmul_rn(K21, r1c)));
-      dpn[n] = __fadd_rn(p1, ep);
-      dsn[n] = __fadd_rn(S1, es);
-      Pkn[n] = __fmaf_rn(dPk1, es, Pk1);  // P_k at the final S, to first order in the correction
-    }
-    dPn = L::make([&](int n) { return dpn[n]; });
-    Sn = L::make([&](int n) { return dsn[n]; });
-    Pk = L::make([&](int n) { return Pkn[n]; });
+    // On lane vectors like the rest; products that feed a TwoSum or an add
+    // are taken lane by lane (vmul_exact), never fused.
+    auto two_sum = [](F a, F b, F& s, F& e) {
+      s = vadd(a, b);
+      const F bb = vsub(s, a);
+      e = vadd(vsub(a, vsub(s, bb)), vsub(b, bb));
+    };
+    const F S1 = Sn, p1 = dPn;
+    const F Se1 = vfma(S1, sp(C.se_b[md]), sp(1.f));
+    const F lS1 = L::make([&](int n) { return split_lg2(L::get(Se1, n)); });
+    const F ex1 = vmul(sp(C.m_inv_lam[md]), lS1);
+    const F Pk1 = vmul_exact(sp(C.P_d[md]), L::make([&](int n) { return split_ex2(L::get(ex1, n)); }));
+    const F rSe1 = L::make([&](int n) { return split_rcp(L::get(Se1, n)); });
+    // targets: T' = D + t as (hi, err) beside D's low part
+    const F ds1 = vsub(S1, S0);
+    const F t1 = vfma(sp(rw.c1), ds1, dm1);
+    F t2 = vfma(sp(-rw.c2), ds1, dm2);
+    if (anysrc)
+      t2 = L::make([&](int n) {
+        return insrc[n] ? __fadd_rn(__fmaf_rn(-rw.c2, L::get(ds1, n), srcf[n]),
+                                    __fadd_rn(__fmul_rn(L::get(gs, n), L::get(nrphi, n)), srcl[n]))
+                        : L::get(t2, n);
+      });
+    F T1h, T1e, T2h, T2e;
+    two_sum(L::make([&](int n) { return M1[n].hi; }), t1, T1h, T1e);
+    two_sum(L::make([&](int n) { return M2[n].hi; }), t2, T2h, T2e);
+    const F T1l = vadd(T1e, L::make([&](int n) { return M1[n].lo; }));
+    const F T2l = vadd(T2e, L::make([&](int n) { return M2[n].lo; }));
+    // water: A1 = rho01 beta1 p1 + e1 as a pair, B = 1 - S1 exactly (FastTwoSum, S1 <= 1)
+    const F a1 = vmul_exact(sp(C.ro01b1), p1);
+    const F a1e = vfma(sp(C.ro01b1_lo), p1, vfma(sp(C.ro01b1), p1, vneg(a1)));
+    F A1h, A1e;
+    two_sum(a1, sp(rw.e1), A1h, A1e);
+    const F Bh = vsub(sp(1.f), S1);
+    const F Be = vsub(vsub(sp(1.f), Bh), S1);
+    // A1 B - T1' with the large product inside one FMA (its result is small)
+    const F r1 = vadd(vfma(A1h, Bh, vneg(T1h)), vfma(A1h, Be, vfma(vadd(A1e, a1e), Bh, vneg(T1l))));
+    // DNAPL: A2 = rho02 beta2 (p1 + P_k) + e2 as a pair
+    F qh, qe;
+    two_sum(p1, Pk1, qh, qe);
+    const F a2 = vmul_exact(sp(C.ro02b2), qh);
+    const F a2e = vfma(sp(C.ro02b2), qe, vfma(sp(C.ro02b2_lo), qh, vfma(sp(C.ro02b2), qh, vneg(a2))));
+    F A2h, A2e;
+    two_sum(a2, sp(rw.e2), A2h, A2e);
+    const F r2 = vadd(vfma(A2h, S1, vneg(T2h)), vfma(vadd(A2e, a2e), S1, vneg(T2l)));
+    // the Jacobian at (p1, S1) and one Newton step
+    const F Pp1 = vfma(sp((float)j), sp(C.H), p1);
+    const F dPk1 = vmul(vmul(Pk1, sp(C.inv_lam_1mswr[md])), rSe1);
+    const F K11 = vmul(sp(C.ro01b1), Bh), mK12 = vmul(sp(C.ro01), vfma(sp(C.beta1), Pp1, sp(1.f)));
+    const F K21 = vmul(sp(C.ro02b2), S1);
+    const F K22 = vmul(sp(C.ro02), vfma(vmul(sp(C.beta2), dPk1), S1, vfma(sp(C.beta2), vadd(Pp1, Pk1), sp(1.f))));
+    const F kinv = L::make([&](int n) { return split_rcp(-L::get(vfma(K11, K22, vmul(mK12, K21)), n)); });
+    const F es = vmul(kinv, vfma(K11, r2, vneg(vmul(K21, r1))));
+    dPn = vfma(kinv, vfma(K22, r1, vmul(mK12, r2)), p1);
+    Sn = vadd(S1, es);
+    Pk = vfma(dPk1, es, Pk1);  // P_k at the final S, to first order in the correction
   }
   const F fin = vadd(dPn, Sn);  // NaN and infinities carry through the sum
 #pragma unroll

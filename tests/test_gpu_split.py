@@ -3,10 +3,13 @@ cannot finish quickly, against the FP64 GPU path that the oracle pins).
 
 Bars (the precision form's targets): max |dS| <= 1e-5 against the FP64
 oracle; relative L2 of P reported and bounded; relative phase-mass drift
-<= 1e-9 per step where DNAPL enters through the mass-rate source (the wide
-source term is exact to ~1e-15). Where it enters through the reference's
-Dirichlet patch instead, every kilogram of it crosses an FP32 face flux, so
-its total carries FP32 rounding (bound 1e-6 there).
+<= 1e-9 per step for water, and for DNAPL where it enters through the
+mass-rate source (the wide source term is exact to ~1e-15). Where DNAPL enters
+through the reference's Dirichlet patch instead, every kilogram of it crosses
+the patch faces' FP32 fluxes, and FP32 mobilities alone, in an otherwise FP64
+oracle, already move its total by 2.7e-8 (test_oracle's FP32-mobility
+experiment): 1e-9 is out of reach of any FP32-flux form there, and the bar is
+a fixed multiple of that experiment's drift, computed per case.
 """
 import numpy as np
 import pytest
@@ -18,6 +21,19 @@ pytestmark = pytest.mark.gpu
 
 SPLITS = ["split", "split_df", "split_defect"]
 DS_TOL = 1e-5
+# Dirichlet-patch DNAPL: the bar is this multiple of what FP32 mobilities alone
+# do to the oracle's DNAPL total (test_oracle.fp32_mobility_drift): the split
+# forms' mobilities come from the FP32 hardware log2/exp2 (about 2^-22 relative,
+# four times a correctly rounded FP32 value's 2^-24) on FP32 pressure
+# differences, and the patch cells' inflow carries their rounding into every
+# kilogram of DNAPL.
+PATCH_FACTOR = 16.0
+
+
+def patch_bound(abi, O, lib, case):
+    from test_oracle import fp32_mobility_drift
+    drift, _ = fp32_mobility_drift(abi, O, O.Oracle(abi), lib, case)
+    return float(drift[1])
 
 
 def prec(abi, name):
@@ -61,8 +77,9 @@ def test_split_matches_fp64_oracle(gpu_lib, abi, O, oracle, pkg, case, form):
         if not mask.any():
             continue
         drift = np.abs(mass[mask, ph] - ref[mask]) / np.abs(ref[mask])
-        bar = 1e-9 if (rate_mode or ph == 0) else 1e-6
-        assert drift.max() <= bar, f"phase {ph + 1} drift {drift.max():.3e} > {bar:.0e}"
+        bar = 1e-9 if (rate_mode or ph == 0) else max(1e-9, PATCH_FACTOR * patch_bound(abi, O, gpu_lib, case))
+        print(f"\n{case} {form} phase {ph + 1}: mass drift {drift.max():.3e} (bar {bar:.1e})")
+        assert drift.max() <= bar, f"phase {ph + 1} drift {drift.max():.3e} > {bar:.1e}"
     dom.close()
 
 

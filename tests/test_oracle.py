@@ -159,3 +159,43 @@ def test_rate_injection_adds_mass(O, oracle, abi):
     mass = oracle.step(st, 3, want_mass=True)
     assert mass[0, 1] == pytest.approx(1e-4 * 1e-3, rel=1e-9)
     assert st["S2"].max() > 0
+
+
+def fp32_mobility_drift(abi, O, oracle, lib, case):
+    """Largest relative phase-mass difference per phase over a case's steps
+    between the oracle and the oracle with only its upwinded face mobilities
+    rounded to FP32 (everything else FP64)."""
+    from test_gpu_f64 import make_case
+    out = []
+    for on in (False, True):
+        m, st, steps = make_case(abi, O, lib, case)
+        m.newton_tol = 0.0
+        st.model = m
+        oracle.initial(st)
+        oracle.fp32_mobilities(on)
+        try:
+            out.append(oracle.step(st, steps, want_mass=True))
+        finally:
+            oracle.fp32_mobilities(False)
+    ref, exp = out
+    scale = np.where(np.abs(ref) > 0, np.abs(ref), 1.0)
+    return (np.abs(exp - ref) / scale).max(axis=0), m
+
+
+@pytest.mark.parametrize("case", ["reference_ini_16", "reference_odd_5x7x6", "c0_rate_hydrostatic_40",
+                                  "heterogeneous_aniso_24x20x18"])
+def test_fp32_mobilities_alone_bound_patch_dnapl_mass(abi, O, oracle, pkg, case):
+    """Why the DNAPL mass of a Dirichlet-patch run cannot stay within 1e-9 of
+    FP64 when face fluxes are FP32: there every kilogram of DNAPL enters
+    through the patch faces, so the total inherits the relative rounding of
+    the patch cells' mobilities (2^-24 for a correctly rounded FP32 value).
+    The oracle with those mobilities alone rounded to FP32 moves the DNAPL
+    total by more than 1e-8 in the Dirichlet cases, while water, and both
+    phases of the mass-rate cases (whose source is exact), stay at round-off."""
+    lib = pkg.load_library()
+    drift, m = fp32_mobility_drift(abi, O, oracle, lib, case)
+    assert drift[0] <= 1e-10, drift
+    if m.source_mode == abi.GBF_SOURCE_DIRICHLET_PATCH:
+        assert drift[1] >= 1e-8, drift
+    else:
+        assert drift[1] <= 1e-12, drift
