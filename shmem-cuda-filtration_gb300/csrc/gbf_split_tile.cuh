@@ -692,7 +692,8 @@ __device__ __forceinline__ void split_cells(const GbfSplitConsts& C, const GbfCe
   const F exS = vmul(sp(C.m_inv_lam[md]), lSe);
   const F eS = L::make([&](int n) { return split_ex2(L::get(exS, n)); });
   const F Pk0 = vmul(sp(C.P_d[md]), eS);  // FMA operands only; its sums below are FMAs
-  const F dPk0 = vmul(vmul(Pk0, sp(C.inv_lam_1mswr[md])), L::make([&](int n) { return split_rcp(L::get(Se, n)); }));
+  const F rSe0 = L::make([&](int n) { return split_rcp(L::get(Se, n)); });
+  const F dPk0 = vmul(vmul(Pk0, sp(C.inv_lam_1mswr[md])), rSe0);
   const F PpPk = vfma(sp(C.P_d[md]), eS, Pp);  // P' + P_k
   const F omS = vsub(sp(1.f), S0);
   F r1, r2;
@@ -735,7 +736,8 @@ __device__ __forceinline__ void split_cells(const GbfSplitConsts& C, const GbfCe
   }
   // the new state: the first step inside one FMA each
   F dPn = vfma(ninv, tp, dPc), Sn = vfma(ninv, ts, S0);
-  if (anyneed) {
+  // (the corrected form below takes its second step from the exact residual instead)
+  if (MR != kMassDefectDF && anyneed) {
     float dpn[N], dsn[N], Pkn[N];
 #pragma unroll
     for (int n = 0; n < N; n++) {
@@ -770,19 +772,22 @@ __device__ __forceinline__ void split_cells(const GbfSplitConsts& C, const GbfCe
     Pk = L::make([&](int n) { return Pkn[n]; });
   }
   if constexpr (MR == kMassDefectDF) {
-    // One residual-correction Newton step per cell (iterative refinement):
-    // the nonlinear residual of both mass equations at the state (p1, S1) the
-    // FP32 Newton reached, against the step's targets held at FP64 precision
-    // (the pair defect plus this step's increment: T1 - c1 (1 - S1) =
-    // D1 + dm1 + c1 (S1 - S0), T2 - c2 S1 = D2 + dm2 + src - c2 (S1 - S0)),
-    // evaluated with error-free transformations (TwoSum, FastTwoSum,
-    // TwoProduct through FMA: Knuth, Dekker) so that only the final, small
-    // residual rounds, where the FP32 Newton's own residual rounds at 2^-24
-    // of the defects (of the masses themselves at compressibility 1e-4). The
-    // capillary pressure, its derivative (stiff near residual saturation,
-    // S_e -> 0) and the Jacobian are taken afresh at (p1, S1); the step's
-    // increments are applied in FP32.
-    //   r1 = (rho01 beta1 p1 + e1) (1 - S1) - T1',  r2 = (rho02 beta2 (p1 + P_k(S1)) + e2) S1 - T2'
+    // One residual-correction Newton step per cell (iterative refinement),
+    // the second step of this form's Newton: the nonlinear residual of both
+    // mass equations at the state (p1, S1) the FP32 step reached, against the
+    // step's targets held at FP64 precision (the pair defect plus this step's
+    // increment: T1 - c1 (1 - S1) = D1 + dm1 + c1 (S1 - S0), T2 - c2 S1 =
+    // D2 + dm2 + src - c2 (S1 - S0)), with the capillary pressure P_k(S1)
+    // evaluated afresh (it is stiff near residual saturation, S_e -> 0):
+    //   r1 = (rho01 beta1 p1 + e1) (1 - S1) - T1',  r2 = (rho02 beta2 (p1 + P_k(S1)) + e2) S1 - T2'.
+    // Error-free transformations (TwoSum, FastTwoSum, TwoProduct through FMA:
+    // Knuth, Dekker) keep every large term exact, so the residual rounds at
+    // about 2^-24 of the small hydrostatic remainder e (6e-13 of a density,
+    // near an FP64 mass's own rounding), where the FP32 step's residual rounds
+    // at 2^-24 of the defects (of the masses themselves at compressibility
+    // 1e-4). The Jacobian is taken at (p1, S1) too; its two reciprocals (of
+    // S_e and of the determinant) by one Newton refinement of those of the
+    // first step (relative error the square of their change over the step).
     // On lane vectors like the rest; products that feed a TwoSum or an add
     // are taken lane by lane (vmul_exact), never fused.
     auto two_sum = [](F a, F b, F& s, F& e) {
@@ -795,7 +800,6 @@ __device__ __forceinline__ void split_cells(const GbfSplitConsts& C, const GbfCe
     const F lS1 = L::make([&](int n) { return split_lg2(L::get(Se1, n)); });
     const F ex1 = vmul(sp(C.m_inv_lam[md]), lS1);
     const F Pk1 = vmul_exact(sp(C.P_d[md]), L::make([&](int n) { return split_ex2(L::get(ex1, n)); }));
-    const F rSe1 = L::make([&](int n) { return split_rcp(L::get(Se1, n)); });
     // targets: T' = D + t as (hi, err) beside D's low part
     const F ds1 = vsub(S1, S0);
     const F t1 = vfma(sp(rw.c1), ds1, dm1);
@@ -811,30 +815,29 @@ __device__ __forceinline__ void split_cells(const GbfSplitConsts& C, const GbfCe
     two_sum(L::make([&](int n) { return M2[n].hi; }), t2, T2h, T2e);
     const F T1l = vadd(T1e, L::make([&](int n) { return M1[n].lo; }));
     const F T2l = vadd(T2e, L::make([&](int n) { return M2[n].lo; }));
-    // water: A1 = rho01 beta1 p1 + e1 as a pair, B = 1 - S1 exactly (FastTwoSum, S1 <= 1)
+    // water: a1 = rho01 beta1 p1 exactly as a1 + a1e, B = 1 - S1 exactly as
+    // Bh + Be (FastTwoSum, S1 <= 1); a1 Bh - T1' inside one FMA (a small
+    // result), the small terms beside it
     const F a1 = vmul_exact(sp(C.ro01b1), p1);
     const F a1e = vfma(sp(C.ro01b1_lo), p1, vfma(sp(C.ro01b1), p1, vneg(a1)));
-    F A1h, A1e;
-    two_sum(a1, sp(rw.e1), A1h, A1e);
     const F Bh = vsub(sp(1.f), S1);
     const F Be = vsub(vsub(sp(1.f), Bh), S1);
-    // A1 B - T1' with the large product inside one FMA (its result is small)
-    const F r1 = vadd(vfma(A1h, Bh, vneg(T1h)), vfma(A1h, Be, vfma(vadd(A1e, a1e), Bh, vneg(T1l))));
-    // DNAPL: A2 = rho02 beta2 (p1 + P_k) + e2 as a pair
+    const F r1 = vadd(vfma(a1, Bh, vneg(T1h)), vfma(vadd(sp(rw.e1), a1e), Bh, vfma(a1, Be, vneg(T1l))));
+    // DNAPL: q = p1 + P_k exactly as qh + qe, a2 = rho02 beta2 q exactly as a2 + a2e
     F qh, qe;
     two_sum(p1, Pk1, qh, qe);
     const F a2 = vmul_exact(sp(C.ro02b2), qh);
     const F a2e = vfma(sp(C.ro02b2), qe, vfma(sp(C.ro02b2_lo), qh, vfma(sp(C.ro02b2), qh, vneg(a2))));
-    F A2h, A2e;
-    two_sum(a2, sp(rw.e2), A2h, A2e);
-    const F r2 = vadd(vfma(A2h, S1, vneg(T2h)), vfma(vadd(A2e, a2e), S1, vneg(T2l)));
+    const F r2 = vadd(vfma(a2, S1, vneg(T2h)), vfma(vadd(sp(rw.e2), a2e), S1, vneg(T2l)));
     // the Jacobian at (p1, S1) and one Newton step
+    const F rSe1 = vmul(rSe0, vfma(vneg(Se1), rSe0, sp(2.f)));  // 1 / S_e(S1)
     const F Pp1 = vfma(sp((float)j), sp(C.H), p1);
     const F dPk1 = vmul(vmul(Pk1, sp(C.inv_lam_1mswr[md])), rSe1);
     const F K11 = vmul(sp(C.ro01b1), Bh), mK12 = vmul(sp(C.ro01), vfma(sp(C.beta1), Pp1, sp(1.f)));
     const F K21 = vmul(sp(C.ro02b2), S1);
     const F K22 = vmul(sp(C.ro02), vfma(vmul(sp(C.beta2), dPk1), S1, vfma(sp(C.beta2), vadd(Pp1, Pk1), sp(1.f))));
-    const F kinv = L::make([&](int n) { return split_rcp(-L::get(vfma(K11, K22, vmul(mK12, K21)), n)); });
+    // -1 / det: ninv = -1 / det0 refined, -1/d1 = ninv (2 + d1 ninv)
+    const F kinv = vmul(ninv, vfma(vfma(K11, K22, vmul(mK12, K21)), ninv, sp(2.f)));
     const F es = vmul(kinv, vfma(K11, r2, vneg(vmul(K21, r1))));
     dPn = vfma(kinv, vfma(K22, r1, vmul(mK12, r2)), p1);
     Sn = vadd(S1, es);
