@@ -64,7 +64,10 @@ extern "C" {
 /* 0 = eager (one kernel per reference function, reference intermediate
    arrays written by every call; the default), 1 = fused (the five calls of a
    step are deferred and run as one fused FP64 step at boundary_conditions;
-   intermediate arrays are materialised on demand by load_data_to_host). */
+   intermediate arrays are materialised on demand by load_data_to_host). A
+   process starts in mode 1 when its environment holds GBF_DROPIN_MODE=1, so
+   that a driver which cannot call this function (the reference's main.cpp)
+   can select it. */
 int gbf_dropin_set_mode(int mode);
 int gbf_dropin_get_mode(void);
 /* The gbflow domain behind arrays from device_memory_alloc (keyed by their

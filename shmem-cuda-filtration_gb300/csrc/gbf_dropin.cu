@@ -22,6 +22,7 @@
 //     (the tests hold both modes to the oracle at 1e-12) in about a third of
 //     the time, since every FP64 iteration costs a log and an exp per cell.
 #include <stdio.h>
+#include <stdlib.h>
 
 #include <mutex>
 #include <unordered_map>
@@ -41,7 +42,14 @@ struct DropinDomain {
 
 std::mutex g_mu;
 std::unordered_map<const double*, DropinDomain> g_domains;
-int g_mode = 0;
+// The mode a process starts in: GBF_DROPIN_MODE=1 in the environment selects
+// the fused mode for drivers that cannot call gbf_dropin_set_mode (the
+// reference's own main.cpp); anything else, or nothing, the eager mode.
+int initial_mode() {
+  const char* e = getenv("GBF_DROPIN_MODE");
+  return (e && e[0] == '1' && e[1] == '\0') ? 1 : 0;
+}
+int g_mode = initial_mode();
 constexpr double kFusedNewtonTol = 1e-11;  // converge-and-exit Newton of the fused mode
 
 gbf_model model_from(const consts& def, int localNx) {
