@@ -24,9 +24,11 @@ fused mode (GBF_DROPIN_MODE=1):
            oracle's state after 12500 steps: restore (main.cpp:541-572), then
            steps 12501..25000.
 Every file the CPU build writes (plot_*/*.dat, media.dat) must exist in the
-GB300 runs and be equal byte for byte; where bytes differ the values are
-compared (a last printed digit may flip only where a value sits on a rounding
-boundary). Prints one JSON summary line; exit code 0 when all match.
+GB300 runs. The eager mode, which runs the reference's arithmetic, must write
+them byte for byte; the fused mode (log/exp instead of pow, FMA, a
+converge-and-exit Newton) values within FUSED_TOL of each column's largest
+magnitude, beyond last printed digits that flip where a value sits on a
+rounding boundary. Prints one JSON summary line; exit code 0 when all match.
 """
 from __future__ import annotations
 
@@ -42,6 +44,12 @@ ROOT = pathlib.Path(__file__).resolve().parents[2]
 LIBDIR = ROOT / "shmem-cuda-filtration_gb300" / "_build"
 INI_DIR = pathlib.Path("C:", "Users", "dmitry", "Documents", "Visual Studio 2010", "Projects", "Buckley-Leverett")
 STEPS, DT, SAVE_EVERY = 25000, 0.02, 5000
+# Fused mode against the CPU build: P and S agree with the oracle to 1e-12
+# and the velocities, first differences of P over h, to 1e-10 of their
+# largest magnitude after a few steps (the drop-in tests); here after 25000
+# steps, where near-hydrostatic columns carry velocities many orders below
+# the largest, the bar is on each column's largest magnitude.
+FUSED_TOL = 1e-8
 NX = NY = NZ = 15
 
 # The reference parameter file's keys (main.cpp:601-684) with its values,
@@ -115,32 +123,54 @@ def outputs(wd: pathlib.Path) -> list[str]:
     return sorted(files + (["media.dat"] if (wd / "media.dat").exists() else []))
 
 
+def _unit(tok: str) -> float:
+    """One unit of the last printed digit of a number printed as %.Ne or %d."""
+    s = tok.lower()
+    mant, _, exp = s.partition("e")
+    digits = len(mant.split(".")[1]) if "." in mant else 0
+    return 10.0 ** ((int(exp) if exp else 0) - digits)
+
+
 def compare(a: pathlib.Path, b: pathlib.Path) -> dict:
-    """Byte equality, else the largest difference of the printed values in
-    units of each value's last printed digit."""
+    """Byte equality; else, value by value, the differences beyond one unit of
+    the last printed digit (a value on a rounding boundary may print either
+    way) relative to the largest magnitude of the value's column."""
     ba, bb = a.read_bytes(), b.read_bytes()
     if ba == bb:
         return {"equal": True}
     la, lb = ba.decode().splitlines(), bb.decode().splitlines()
     if len(la) != len(lb):
-        return {"equal": False, "lines": [len(la), len(lb)]}
-    worst, nlines = 0.0, 0
-    for x, y in zip(la, lb):
+        return {"equal": False, "lines": [len(la), len(lb)], "max_rel": float("inf")}
+    rows = [(x.split(), y.split()) for x, y in zip(la, lb)]
+    colmax = {}
+    for x, _ in rows:
+        for c, u in enumerate(x):
+            try:
+                colmax[c] = max(colmax.get(c, 0.0), abs(float(u)))
+            except ValueError:
+                pass
+    flips, beyond, worst = 0, 0, {}
+    for x, y in rows:
         if x == y:
             continue
-        nlines += 1
-        for u, v in zip(x.split(), y.split()):
+        if len(x) != len(y):
+            return {"equal": False, "text": [" ".join(x), " ".join(y)], "max_rel": float("inf")}
+        for c, (u, v) in enumerate(zip(x, y)):
             if u == v:
                 continue
             try:
                 fu, fv = float(u), float(v)
             except ValueError:
-                return {"equal": False, "text": [x, y]}
-            mant = u.lower().split("e")[0]
-            digits = len(mant.split(".")[1]) if "." in mant else 0
-            exp = int(u.lower().split("e")[1]) if "e" in u.lower() else 0
-            worst = max(worst, abs(fu - fv) / 10.0 ** (exp - digits))
-    return {"equal": False, "lines_differing": nlines, "max_last_digit_units": worst}
+                return {"equal": False, "text": [" ".join(x), " ".join(y)], "max_rel": float("inf")}
+            d = abs(fu - fv)
+            if d <= max(_unit(u), _unit(v)) * (1 + 1e-9):
+                flips += 1
+                continue
+            beyond += 1
+            worst[c] = max(worst.get(c, 0.0), d / colmax[c] if colmax.get(c) else float("inf"))
+    return {"equal": False, "last_digit_flips": flips, "beyond_one_digit": beyond,
+            "max_rel_by_column": {str(c): w for c, w in sorted(worst.items())},
+            "max_rel": max(worst.values(), default=0.0)}
 
 
 def main():
@@ -166,7 +196,12 @@ def main():
             per = {f: compare(out / scen / "cpu" / f, out / scen / mode / f) for f in files if f in got}
             c["byte_equal"] = sum(1 for v in per.values() if v["equal"])
             c["differing"] = {f: v for f, v in per.items() if not v["equal"]}
-            ok &= not c["missing"] and all(v.get("max_last_digit_units", 99) <= 1.0 for v in c["differing"].values())
+            # eager mode runs the reference's own arithmetic: byte equality;
+            # fused mode (log/exp, FMA, converge-and-exit Newton): values
+            # within FUSED_TOL of their column's scale beyond digit flips
+            tol = 0.0 if mode == "gb300_eager" else FUSED_TOL
+            c["max_rel"] = max((v["max_rel"] for v in c["differing"].values()), default=0.0)
+            ok &= not c["missing"] and c["max_rel"] <= tol and (mode != "gb300_eager" or not c["differing"])
             res["compare"][mode] = c
         summary["scenarios"][scen] = res
     summary["ok"] = bool(ok)
