@@ -44,7 +44,10 @@ enum { GBF_BC_REFERENCE = 0,           /* reference Border_S2/Border_P1 rules   
 enum { GBF_PREC_F64 = 0,               /* plain FP64 state and arithmetic               */
        GBF_PREC_SPLIT = 1,             /* FP32 P,S,K,fluxes; phase masses at least as precise
                                           as FP64: FP32-pair defects over the state's exact
-                                          FP32-product mass (FP32 pipes only)            */
+                                          FP32-product mass; after the FP32 Newton step one
+                                          residual-correction step per cell, its residual
+                                          exact to FP64 precision by error-free FP32
+                                          transformations (FP32 pipes only)              */
        GBF_PREC_SPLIT_DF = 2,          /* as SPLIT, masses and residual as FP32 pairs
                                           (about 48 significant bits, FP32 pipes only)  */
        GBF_PREC_SPLIT_DEFECT = 3 };    /* as SPLIT, each phase mass held as its FP32
