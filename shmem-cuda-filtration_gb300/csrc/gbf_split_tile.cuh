@@ -454,8 +454,11 @@ struct GbfSplitAcc<kMassDefect> {
     b = __dadd_rn(__dmul_rn((double)c2, S), (double)b2);
   }
 };
-// Pair defects: sum phi D1 and sum phi (D2 + ...) as FP32 pairs (each
-// product's rounding error kept, TwoSum into the high part).
+// Pair defects: sum phi S, sum phi D1 and sum phi (D2 + q) as FP32 pairs
+// (each product's rounding error kept, TwoSum into the high part; q = rho02
+// beta2 P_k S, the DNAPL mass's small capillary term, joins D2 by one TwoSum,
+// its error into the low part). pl: the low part of a media-table porosity
+// (has_pl; zero with a porosity field, whose FP32 values are exact).
 template <>
 struct GbfSplitAcc<kMassDefectDF> {
   float sS, lS;
@@ -465,16 +468,22 @@ struct GbfSplitAcc<kMassDefectDF> {
   unsigned bad;
   __device__ GbfSplitAcc()
       : sS(0.f), lS(0.f), b1{0.f, 0.f}, b2{0.f, 0.f}, c1(0.f), c2(0.f), cfl1(0.f), cfl2(0.f), bad(0) {}
-  __device__ __forceinline__ void add(float ph, float pl, float S, GbfDF D1, GbfDF D2q) {
-    const float p = ph * S, pe = fmaf(pl, S, fmaf(ph, S, -p));
-    const float s = sS + p;
-    const float bb = s - sS;
-    lS += ((sS - (s - bb)) + (p - bb)) + pe;
+  __device__ __forceinline__ void add(float ph, float pl, float S, GbfDF D1, GbfDF D2, float q, bool has_pl) {
+    const float p = __fmul_rn(ph, S);
+    float pe = __fmaf_rn(ph, S, -p);
+    if (has_pl) pe = __fmaf_rn(pl, S, pe);
+    const float s = __fadd_rn(sS, p);
+    const float bb = __fsub_rn(s, sS);
+    lS = __fadd_rn(lS, __fadd_rn(__fadd_rn(__fsub_rn(sS, __fsub_rn(s, bb)), __fsub_rn(p, bb)), pe));
     sS = s;
+    const GbfDF d2 = df_two_sum(D2.hi, q);  // D2 + q, not renormalised: acc_phi takes both parts
+    const GbfDF D2q = {d2.hi, __fadd_rn(d2.lo, D2.lo)};
     b1 = Wide<true>::acc_phi(b1, ph, D1);
     b2 = Wide<true>::acc_phi(b2, ph, D2q);
-    b1.lo = fmaf(pl, D1.hi, b1.lo);
-    b2.lo = fmaf(pl, D2q.hi, b2.lo);
+    if (has_pl) {
+      b1.lo = __fmaf_rn(pl, D1.hi, b1.lo);
+      b2.lo = __fmaf_rn(pl, D2q.hi, b2.lo);
+    }
   }
   __device__ __forceinline__ void masses(double& a, double& b) const {
     const double S = __dadd_rn((double)sS, (double)lS);
@@ -898,7 +907,7 @@ __device__ __forceinline__ void split_cells(const GbfSplitConsts& C, const GbfCe
         if (count[n] && mass) {
           const float ph = phi_field ? in[n].phi : C.m_df[md].x;
           const float pl = phi_field ? 0.f : C.m_df[md].y;
-          acc.add(ph, pl, o[n].Sn, o[n].M1n, defect_add(o[n].M2n, __fmul_rn(L::get(qa, n), o[n].Sn)));
+          acc.add(ph, pl, o[n].Sn, o[n].M1n, o[n].M2n, __fmul_rn(L::get(qa, n), o[n].Sn), !phi_field);
         }
       }
     }
