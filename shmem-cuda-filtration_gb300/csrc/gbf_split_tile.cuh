@@ -794,9 +794,11 @@ __device__ __forceinline__ void split_cells(const GbfSplitConsts& C, const GbfCe
     // about 2^-24 of the small hydrostatic remainder e (6e-13 of a density,
     // near an FP64 mass's own rounding), where the FP32 step's residual rounds
     // at 2^-24 of the defects (of the masses themselves at compressibility
-    // 1e-4). The Jacobian is taken at (p1, S1) too; its two reciprocals (of
-    // S_e and of the determinant) by one Newton refinement of those of the
-    // first step (relative error the square of their change over the step).
+    // 1e-4). The Jacobian is taken at (p1, S1) too, with its own reciprocals
+    // of S_e and of the determinant (a refinement of the first step's would
+    // carry the square of their change over the step, 14% where 1 - S falls
+    // by a third in one step near residual saturation, and leave the
+    // correction that much short).
     // On lane vectors like the rest; products that feed a TwoSum or an add
     // are taken lane by lane (vmul_exact), never fused.
     auto two_sum = [](F a, F b, F& s, F& e) {
@@ -839,14 +841,13 @@ __device__ __forceinline__ void split_cells(const GbfSplitConsts& C, const GbfCe
     const F a2e = vfma(sp(C.ro02b2), qe, vfma(sp(C.ro02b2_lo), qh, vfma(sp(C.ro02b2), qh, vneg(a2))));
     const F r2 = vadd(vfma(a2, S1, vneg(T2h)), vfma(vadd(sp(rw.e2), a2e), S1, vneg(T2l)));
     // the Jacobian at (p1, S1) and one Newton step
-    const F rSe1 = vmul(rSe0, vfma(vneg(Se1), rSe0, sp(2.f)));  // 1 / S_e(S1)
+    const F rSe1 = L::make([&](int n) { return split_rcp(L::get(Se1, n)); });  // 1 / S_e(S1)
     const F Pp1 = vfma(sp((float)j), sp(C.H), p1);
     const F dPk1 = vmul(vmul(Pk1, sp(C.inv_lam_1mswr[md])), rSe1);
     const F K11 = vmul(sp(C.ro01b1), Bh), mK12 = vmul(sp(C.ro01), vfma(sp(C.beta1), Pp1, sp(1.f)));
     const F K21 = vmul(sp(C.ro02b2), S1);
     const F K22 = vmul(sp(C.ro02), vfma(vmul(sp(C.beta2), dPk1), S1, vfma(sp(C.beta2), vadd(Pp1, Pk1), sp(1.f))));
-    // -1 / det: ninv = -1 / det0 refined, -1/d1 = ninv (2 + d1 ninv)
-    const F kinv = vmul(ninv, vfma(vfma(K11, K22, vmul(mK12, K21)), ninv, sp(2.f)));
+    const F kinv = L::make([&](int n) { return split_rcp(-L::get(vfma(K11, K22, vmul(mK12, K21)), n)); });
     const F es = vmul(kinv, vfma(K11, r2, vneg(vmul(K21, r1))));
     dPn = vfma(kinv, vfma(K22, r1, vmul(mK12, r2)), p1);
     Sn = vadd(S1, es);
