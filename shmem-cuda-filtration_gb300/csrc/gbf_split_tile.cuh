@@ -840,14 +840,36 @@ __device__ __forceinline__ void split_cells(const GbfSplitConsts& C, const GbfCe
     const F a2 = vmul_exact(sp(C.ro02b2), qh);
     const F a2e = vfma(sp(C.ro02b2), qe, vfma(sp(C.ro02b2_lo), qh, vfma(sp(C.ro02b2), qh, vneg(a2))));
     const F r2 = vadd(vfma(a2, S1, vneg(T2h)), vfma(vadd(sp(rw.e2), a2e), S1, vneg(T2l)));
-    // the Jacobian at (p1, S1) and one Newton step
-    const F rSe1 = L::make([&](int n) { return split_rcp(L::get(Se1, n)); });  // 1 / S_e(S1)
-    const F Pp1 = vfma(sp((float)j), sp(C.H), p1);
-    const F dPk1 = vmul(vmul(Pk1, sp(C.inv_lam_1mswr[md])), rSe1);
-    const F K11 = vmul(sp(C.ro01b1), Bh), mK12 = vmul(sp(C.ro01), vfma(sp(C.beta1), Pp1, sp(1.f)));
-    const F K21 = vmul(sp(C.ro02b2), S1);
-    const F K22 = vmul(sp(C.ro02), vfma(vmul(sp(C.beta2), dPk1), S1, vfma(sp(C.beta2), vadd(Pp1, Pk1), sp(1.f))));
-    const F kinv = L::make([&](int n) { return split_rcp(-L::get(vfma(K11, K22, vmul(mK12, K21)), n)); });
+    // One Newton step with the Jacobian at (p1, S1) where the first step
+    // moved S by more than 1e-3 of S_e (which also bounds 1 - S), the
+    // first step's elsewhere: there every entry of the Jacobian changed by
+    // less than about 1e-3 over the step, so the step it gives is short by
+    // that much of a correction that is itself small. Lane by lane, so that
+    // each cell takes the same path in every tile shape.
+    F K11 = J11, mK12 = mJ12, K21 = J21, K22 = J22, kinv = ninv, dPk1 = dPk0;
+    bool fresh[N], anyfresh = false;
+#pragma unroll
+    for (int n = 0; n < N; n++) {
+      fresh[n] = __fmul_rn(fabsf(L::get(ds1, n)), L::get(rSe0, n)) > 1e-3f;
+      anyfresh |= fresh[n];
+    }
+    if (anyfresh) {
+      const F rSe1 = L::make([&](int n) { return split_rcp(L::get(Se1, n)); });  // 1 / S_e(S1)
+      const F Pp1 = vfma(sp((float)j), sp(C.H), p1);
+      const F dPkf = vmul(vmul(Pk1, sp(C.inv_lam_1mswr[md])), rSe1);
+      const F K11f = vmul(sp(C.ro01b1), Bh), mK12f = vmul(sp(C.ro01), vfma(sp(C.beta1), Pp1, sp(1.f)));
+      const F K21f = vmul(sp(C.ro02b2), S1);
+      const F K22f =
+          vmul(sp(C.ro02), vfma(vmul(sp(C.beta2), dPkf), S1, vfma(sp(C.beta2), vadd(Pp1, Pk1), sp(1.f))));
+      const F kinvf = L::make([&](int n) { return split_rcp(-L::get(vfma(K11f, K22f, vmul(mK12f, K21f)), n)); });
+      auto pick = [&](F a, F b) { return L::make([&](int n) { return fresh[n] ? L::get(a, n) : L::get(b, n); }); };
+      K11 = pick(K11f, K11);
+      mK12 = pick(mK12f, mK12);
+      K21 = pick(K21f, K21);
+      K22 = pick(K22f, K22);
+      kinv = pick(kinvf, kinv);
+      dPk1 = pick(dPkf, dPk1);
+    }
     const F es = vmul(kinv, vfma(K11, r2, vneg(vmul(K21, r1))));
     dPn = vfma(kinv, vfma(K22, r1, vmul(mK12, r2)), p1);
     Sn = vadd(S1, es);
