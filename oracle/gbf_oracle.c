@@ -153,16 +153,57 @@ void orc_velocity(const gbf_model* m, gbf_arrays a) {
 static double upwind_div(double x1, double x2, double Xc, double rc, double Xm, double rm,
                          double Xp, double rp, double h);
 
-/* Experiment switch (off by default; the tests only): with it on, the flux
-   stage rounds every upwinded mobility Xi*ro to FP32 before it multiplies the
-   face potential, and nothing else: the oracle then shows what FP32
-   mobilities alone, in an otherwise FP64 scheme, do to the phase masses. */
+/* Experiment switch (off by default; the tests only): what the split forms'
+   FP32 flux stage does to the phase masses in an otherwise FP64 scheme.
+   1: every upwinded mobility Xi*ro rounded to FP32 before it multiplies the
+      face potential, and nothing else.
+   2: the same except on the DNAPL face between a Dirichlet patch cell and the
+      j = 1 cell below it, which keeps its FP64 mobility (the split forms' FP64
+      patch inflow).
+   3: mobilities FP64 and the flux arithmetic FP32 as in the split forms: each
+      face's upwinded flux (potential times mobility) rounded to FP32, each
+      direction's in - out and its dt / h^2 weighting rounded, the cell's sum
+      of the three rounded, the increment over phi rounded and added to the
+      FP64 mass; the DNAPL flux through the Dirichlet patch faces stays FP64
+      and is added apart, like the rate source.
+   4: 3 with the split tile's remaining FP32 steps: mobilities rounded to FP32
+      (but the patch faces' DNAPL one), and in y the minus face's product
+      entering the difference unrounded (the tile's FMA) while the plus face's
+      is rounded, so that a y face's flux differs by one rounding between its
+      two cells. */
 static int g_fp32_mobilities = 0;
 void orc_set_fp32_mobilities(int on) { g_fp32_mobilities = on; }
 
+/* The y-direction DNAPL divergence of a j = 1 cell under the Dirichlet patch
+   at experiment level 2: FP32 mobilities on its plus face, FP64 on its minus
+   (patch) face. */
+static double upwind_div_patch(double x1, double x2, double Xc, double rc, double Xm, double rm,
+                               double Xp, double rp, double h) {
+  const double Lc = (float)(Xc * rc), Lp = (float)(Xp * rp);
+  return ((x2 + fabs(x2)) / 2.0 * (-1) * Lc - (x1 - fabs(x1)) / 2.0 * (-1) * (Xc * rc) -
+          (x1 + fabs(x1)) / 2.0 * (-1) * (Xm * rm) + (x2 - fabs(x2)) / 2.0 * (-1) * Lp) / h;
+}
+
+/* Experiment levels 3 and 4: the upwinded fluxes through the minus (F1) and
+   plus (F2) faces as the split tile signs them, -(potential times mobility):
+   h upwind_div = F2 - F1. */
+static double mob(double X, double r, int r32) { return r32 ? (double)(float)(X * r) : X * r; }
+static void face_fluxes(double x1, double x2, double Xc, double rc, double Xm, double rm, double Xp, double rp,
+                        double* F1, double* F2) {
+  const int r32 = g_fp32_mobilities == 4;
+  *F1 = x1 >= 0 ? x1 * (-mob(Xm, rm, r32)) : x1 * (-mob(Xc, rc, r32));
+  *F2 = x2 >= 0 ? x2 * (-mob(Xc, rc, r32)) : x2 * (-mob(Xp, rp, r32));
+}
+/* dt/h^2 (kv in y) times in - out, FP32 as the split tile forms it (fma_minus:
+   the minus face's product unrounded inside the difference, level 4 in y). */
+static float fp32_dir(double F1, double F2, double w, int fma_minus) {
+  const float d = fma_minus ? (float)(F1 - (double)(float)F2) : (float)F1 - (float)F2;
+  return d * (float)w;
+}
+
 static double upwind_div(double x1, double x2, double Xc, double rc, double Xm, double rm,
                          double Xp, double rp, double h) {
-  if (g_fp32_mobilities) {
+  if (g_fp32_mobilities == 1 || g_fp32_mobilities == 2) {
     const double Lc = (float)(Xc * rc), Lm = (float)(Xm * rm), Lp = (float)(Xp * rp);
     return (((x2 + fabs(x2)) / 2.0 - (x1 - fabs(x1)) / 2.0) * (-1) * Lc - (x1 + fabs(x1)) / 2.0 * (-1) * Lm +
             (x2 - fabs(x2)) / 2.0 * (-1) * Lp) / h;
@@ -216,7 +257,60 @@ void orc_mass(const gbf_model* m, const gbf_cells* cells, gbf_arrays a) {
         y1 = -(P2 - a.P2[c - nx]) / m->h2 + a.ro2[c] * m->g;
         if (noflow_bottom && j == ny - 2) y2 = 0;
         g1 = upwind_div(x1, x2, a.Xi2[c], a.ro2[c], a.Xi2[c - 1], a.ro2[c - 1], a.Xi2[c + 1], a.ro2[c + 1], m->h1);
-        g2 = m->kv * upwind_div(y1, y2, a.Xi2[c], a.ro2[c], a.Xi2[c - nx], a.ro2[c - nx], a.Xi2[c + nx], a.ro2[c + nx], m->h2);
+        if (g_fp32_mobilities == 2 && j == 1 && m->source_mode == GBF_SOURCE_DIRICHLET_PATCH && in_dirichlet_patch(m, i, k))
+          g2 = m->kv * upwind_div_patch(y1, y2, a.Xi2[c], a.ro2[c], a.Xi2[c - nx], a.ro2[c - nx], a.Xi2[c + nx],
+                                        a.ro2[c + nx], m->h2);
+        else
+          g2 = m->kv * upwind_div(y1, y2, a.Xi2[c], a.ro2[c], a.Xi2[c - nx], a.ro2[c - nx], a.Xi2[c + nx], a.ro2[c + nx], m->h2);
+        if (g_fp32_mobilities == 3 || g_fp32_mobilities == 4) {  /* FP32 flux arithmetic, FP64 patch inflow */
+          const int fy = g_fp32_mobilities == 4;
+          const int ptop = j == 1 && m->source_mode == GBF_SOURCE_DIRICHLET_PATCH && in_dirichlet_patch(m, i, k);
+          double F1, F2;
+          float s1 = 0.f, s2 = 0.f;
+          double pin = 0.0;
+          if (nz >= 2) {
+            z2 = -(a.P1[c + pl] - P1) / m->h3;
+            z1 = -(P1 - a.P1[c - pl]) / m->h3;
+            face_fluxes(z1, z2, a.Xi1[c], a.ro1[c], a.Xi1[c - pl], a.ro1[c - pl], a.Xi1[c + pl], a.ro1[c + pl], &F1, &F2);
+            s1 = fp32_dir(F1 * m->h3, F2 * m->h3, m->dt / (m->h3 * m->h3), 0);
+            z2 = -(a.P2[c + pl] - P2) / m->h3;
+            z1 = -(P2 - a.P2[c - pl]) / m->h3;
+            face_fluxes(z1, z2, a.Xi2[c], a.ro2[c], a.Xi2[c - pl], a.ro2[c - pl], a.Xi2[c + pl], a.ro2[c + pl], &F1, &F2);
+            s2 = fp32_dir(F1 * m->h3, F2 * m->h3, m->dt / (m->h3 * m->h3), 0);
+          }
+          x2 = -(a.P1[c + 1] - P1) / m->h1;
+          x1 = -(P1 - a.P1[c - 1]) / m->h1;
+          face_fluxes(x1, x2, a.Xi1[c], a.ro1[c], a.Xi1[c - 1], a.ro1[c - 1], a.Xi1[c + 1], a.ro1[c + 1], &F1, &F2);
+          s1 = s1 + fp32_dir(F1 * m->h1, F2 * m->h1, m->dt / (m->h1 * m->h1), 0);
+          y2 = -(a.P1[c + nx] - P1) / m->h2 + a.ro1[c] * m->g;
+          y1 = -(P1 - a.P1[c - nx]) / m->h2 + a.ro1[c] * m->g;
+          if (noflow_bottom && j == ny - 2) y2 = 0;
+          face_fluxes(y1, y2, a.Xi1[c], a.ro1[c], a.Xi1[c - nx], a.ro1[c - nx], a.Xi1[c + nx], a.ro1[c + nx], &F1, &F2);
+          s1 = s1 + fp32_dir(F1 * m->h2, F2 * m->h2, m->dt * m->kv / (m->h2 * m->h2), fy);
+          x2 = -(a.P2[c + 1] - P2) / m->h1;
+          x1 = -(P2 - a.P2[c - 1]) / m->h1;
+          face_fluxes(x1, x2, a.Xi2[c], a.ro2[c], a.Xi2[c - 1], a.ro2[c - 1], a.Xi2[c + 1], a.ro2[c + 1], &F1, &F2);
+          s2 = s2 + fp32_dir(F1 * m->h1, F2 * m->h1, m->dt / (m->h1 * m->h1), 0);
+          y2 = -(a.P2[c + nx] - P2) / m->h2 + a.ro2[c] * m->g;
+          y1 = -(P2 - a.P2[c - nx]) / m->h2 + a.ro2[c] * m->g;
+          if (noflow_bottom && j == ny - 2) y2 = 0;
+          face_fluxes(y1, y2, a.Xi2[c], a.ro2[c], a.Xi2[c - nx], a.ro2[c - nx], a.Xi2[c + nx], a.ro2[c + nx], &F1, &F2);
+          if (ptop) {
+            const double Fp = y1 >= 0 ? y1 * (-(a.Xi2[c - nx] * a.ro2[c - nx])) : y1 * (-(a.Xi2[c] * a.ro2[c]));
+            pin = Fp * m->h2 * (m->dt * m->kv / (m->h2 * m->h2));
+            F1 = 0.0;
+          }
+          s2 = s2 + fp32_dir(F1 * m->h2, F2 * m->h2, m->dt * m->kv / (m->h2 * m->h2), fy);
+          /* the FP32 increments over phi (rounded), the patch inflow and the rate source exact */
+          f1 = (double)(float)((double)s1 / phi);
+          g1 = (double)(float)((double)s2 / phi);
+          const double srcv = (src != 0.0 && j == 1 && orc_in_rate_patch(m, i, k)) ? (m->dt / phi) * src : 0.0;
+          a.roS1_old[c] = roS1;
+          a.roS2_old[c] = roS2;
+          a.roS1[c] = roS1 + f1;
+          a.roS2[c] = roS2 + g1 + pin / phi + srcv;
+          continue;
+        }
         double A1 = roS1 - (m->dt / phi) * (f1 + f2 + f3);
         double A2;
         if (src != 0.0 && j == 1 && orc_in_rate_patch(m, i, k))

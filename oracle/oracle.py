@@ -154,10 +154,12 @@ class Oracle:
         lib.orc_set_fp32_mobilities.argtypes = [ctypes.c_int]
         self.lib = lib
 
-    def fp32_mobilities(self, on: bool):
+    def fp32_mobilities(self, level):
         """Experiment switch: round the flux stage's upwinded mobilities to
-        FP32, everything else FP64 (off: the bit-exact reference)."""
-        self.lib.orc_set_fp32_mobilities(int(on))
+        FP32, everything else FP64 (False / 0: the bit-exact reference; True /
+        1: every face; 2: every face but the DNAPL faces between the
+        Dirichlet patch and the cells below it)."""
+        self.lib.orc_set_fp32_mobilities(int(level))
 
     def _call(self, name, st: State, with_cells=True):
         m = ctypes.byref(st.model)

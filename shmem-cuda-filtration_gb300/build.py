@@ -34,7 +34,7 @@ def nvcc() -> str:
 
 
 def _deps(src: pathlib.Path):
-    return [src] + sorted(CSRC.glob("*.h")) + sorted(INCLUDE.glob("*.h"))
+    return [src] + sorted(CSRC.glob("*.h")) + sorted(CSRC.glob("*.cuh")) + sorted(INCLUDE.glob("*.h"))
 
 
 def _compile(src: pathlib.Path) -> pathlib.Path:

@@ -38,6 +38,10 @@ struct EnsMember {
   int part_begin, part_end;  // this member's slots in the partial-sum array
   double k1v;                // defect form: water-mass part left out of the tiles' sums (gbf_defect_k1)
   unsigned long long off;    // first cell of this member in the packed all-members layout
+  // split forms under a Dirichlet patch: the pre-pass's constants and its FP64
+  // inflow array (pc.n = 0, patch NULL: no patch)
+  GbfPatchConsts pc;
+  float2* patch;
 };
 
 struct EnsChunk {
@@ -75,7 +79,7 @@ __device__ __forceinline__ float* ens_cfl_slot(const EnsCfl& cfl, int member) {
   return step < (unsigned)cfl.cap ? cfl.hist + 2 * ((size_t)step * cfl.n + member) : nullptr;
 }
 
-template <int MR, int TX, int TY, bool TMA, bool CFL>
+template <int MR, int TX, int TY, bool TMA, bool CFL, bool PATCH>
 __global__ void __launch_bounds__(TX * TY, 1024 / (TX * TY)) k_ens_split_step(const EnsMember* __restrict__ mem,
                                                                              const int4* __restrict__ tiles,
                                                                              const int* __restrict__ order,
@@ -127,10 +131,11 @@ __global__ void __launch_bounds__(TX * TY, 1024 / (TX * TY)) k_ens_split_step(co
       Gs.mass_partials = partials;
       Gs.status = status;
       Gs.cfl_out = CFL ? ens_cfl_slot(cfl, tl.x) : nullptr;
+      if constexpr (PATCH) Gs.patch_in = me->patch;
     }
     __syncthreads();
     GbfSplitAcc<MR> acc;
-    const bool ok = split_tile<MR, TX, TY, TMA, CFL>(Cs, Gs, tl.y, tl.z, tl.w & 0xffff, tl.w >> 16, pl, acc, raw,
+    const bool ok = split_tile<MR, TX, TY, TMA, CFL, PATCH>(Cs, Gs, tl.y, tl.z, tl.w & 0xffff, tl.w >> 16, pl, acc, raw,
                                                 TMA ? maps + tl.x : nullptr, cur, &phases);
     if (!ok) break;  // a plane wait gave up (status set); the whole CTA stops
     if (acc.bad) atomicOr(status, GBF_DEV_NONFINITE);
@@ -142,7 +147,7 @@ __global__ void __launch_bounds__(TX * TY, 1024 / (TX * TY)) k_ens_split_step(co
 }
 
 // Per tile: the member's constants to shared memory, its arrays to Gs.
-template <int NT, bool CFL>
+template <int NT, bool CFL, bool PATCH>
 __device__ __forceinline__ void ens_tile_setup(const EnsMember* me, int member, int cur, double* partials,
                                                unsigned* status, const EnsCfl& cfl, GbfSplitConsts& Cs,
                                                GbfSplitGrid& Gs) {
@@ -162,6 +167,7 @@ __device__ __forceinline__ void ens_tile_setup(const EnsMember* me, int member, 
     Gs.mass_partials = partials;
     Gs.status = status;
     Gs.cfl_out = CFL ? ens_cfl_slot(cfl, member) : nullptr;
+    if constexpr (PATCH) Gs.patch_in = me->patch;
   }
 }
 
@@ -171,7 +177,7 @@ constexpr int kTileKindShift = 30;
 __host__ __device__ constexpr int tile_x0(int y) { return y & ((1 << kTileKindShift) - 1); }
 __host__ __device__ constexpr int tile_kind(int y) { return y >> kTileKindShift; }
 
-template <int MR, int TXC, int TY, bool CFL>
+template <int MR, int TXC, int TY, bool CFL, bool PATCH>
 __global__ void __launch_bounds__(TXC / 2 * TY, gbf_pair_ctas(MR) * 256 / (TXC / 2 * TY)) k_ens_split_step_x2(
     const EnsMember* __restrict__ mem, const int4* __restrict__ tiles, const int* __restrict__ order, int ntiles,
     int cur, unsigned* counter, double* partials, unsigned* status, const GbfTmaSet* __restrict__ maps,
@@ -197,11 +203,12 @@ __global__ void __launch_bounds__(TXC / 2 * TY, gbf_pair_ctas(MR) * 256 / (TXC /
     if (t >= ntiles) break;
     const int ti = order ? order[t] : t;  // list index (mass-partial slot)
     const int4 tl = tiles[ti];
-    ens_tile_setup<NT, CFL>(mem + tl.x, tl.x, cur, partials, status, cfl, Cs, Gs);
+    ens_tile_setup<NT, CFL, PATCH>(mem + tl.x, tl.x, cur, partials, status, cfl, Cs, Gs);
     __syncthreads();
     GbfSplitAcc<MR> acc;
-    const bool ok = split_tile_x2<MR, TXC, TY, CFL>(Cs, Gs, tile_x0(tl.y), tl.z, tl.w & 0xffff, tl.w >> 16,
-                                                   cta.bars, cta.body, acc, maps + tl.x, cur, &phases);
+    const bool ok = split_tile_x2<MR, TXC, TY, CFL, NT, PATCH>(Cs, Gs, tile_x0(tl.y), tl.z, tl.w & 0xffff,
+                                                              tl.w >> 16, cta.bars, cta.body, acc, maps + tl.x, cur,
+                                                              &phases);
     if (!ok) break;
     if (acc.bad) atomicOr(status, GBF_DEV_NONFINITE);
     if (partials) split_block_mass<MR, NT>(acc, Cs.V, partials + 2 * ti);
@@ -216,7 +223,7 @@ __global__ void __launch_bounds__(TXC / 2 * TY, gbf_pair_ctas(MR) * 256 / (TXC /
 // lanes than a half-empty 32-wide tile). One set of barriers serves both
 // shapes' rings, which share the shared memory (a union); `maps` holds two
 // sets per member (32x16, 48x10 boxes).
-template <int MR, bool CFL>
+template <int MR, bool CFL, bool PATCH>
 __global__ void __launch_bounds__(256, gbf_pair_ctas(MR)) k_ens_split_step_x2m(
     const EnsMember* __restrict__ mem, const int4* __restrict__ tiles, const int* __restrict__ order, int ntiles,
     int cur, unsigned* counter, double* partials, unsigned* status, const GbfTmaSet* __restrict__ maps,
@@ -242,15 +249,15 @@ __global__ void __launch_bounds__(256, gbf_pair_ctas(MR)) k_ens_split_step_x2m(
     if (t >= ntiles) break;
     const int ti = order ? order[t] : t;
     const int4 tl = tiles[ti];
-    ens_tile_setup<NT, CFL>(mem + tl.x, tl.x, cur, partials, status, cfl, Cs, Gs);
+    ens_tile_setup<NT, CFL, PATCH>(mem + tl.x, tl.x, cur, partials, status, cfl, Cs, Gs);
     __syncthreads();
     GbfSplitAcc<MR> acc;
     const int x0 = tile_x0(tl.y), k0 = tl.w & 0xffff, k1 = tl.w >> 16;
     const bool ok = tile_kind(tl.y)
-                        ? split_tile_x2<MR, 48, 10, CFL, NT>(Cs, Gs, x0, tl.z, k0, k1, cta.bars, cta.b, acc,
-                                                             maps + 2 * tl.x + 1, cur, &phases)
-                        : split_tile_x2<MR, 32, 16, CFL, NT>(Cs, Gs, x0, tl.z, k0, k1, cta.bars, cta.a, acc,
-                                                             maps + 2 * tl.x, cur, &phases);
+                        ? split_tile_x2<MR, 48, 10, CFL, NT, PATCH>(Cs, Gs, x0, tl.z, k0, k1, cta.bars, cta.b, acc,
+                                                                    maps + 2 * tl.x + 1, cur, &phases)
+                        : split_tile_x2<MR, 32, 16, CFL, NT, PATCH>(Cs, Gs, x0, tl.z, k0, k1, cta.bars, cta.a, acc,
+                                                                    maps + 2 * tl.x, cur, &phases);
     if (!ok) break;
     if (acc.bad) atomicOr(status, GBF_DEV_NONFINITE);
     if (partials) split_block_mass<MR, NT>(acc, Cs.V, partials + 2 * ti);
@@ -387,6 +394,21 @@ __global__ void k_ens_mass_tail(const EnsMember* __restrict__ mem, const double*
 }
 __global__ void k_ens_count(unsigned* count) { atomicAdd(count, 1u); }
 
+// The step's pre-pass for split members under a Dirichlet patch
+// (gbf_split_patch_cell), one block per member of [r0, r0 + gridDim.x).
+__global__ void __launch_bounds__(64) k_ens_split_patch(const EnsMember* __restrict__ mem, int r0, int cur) {
+  const EnsMember& me = mem[r0 + blockIdx.x];
+  if (!me.patch) return;
+  GbfSplitGrid G = {};
+  G.dP = me.dPf[cur];
+  G.S = me.Sf[cur];
+  G.K = me.cells.K;
+  G.phi = me.cells.phi;
+  G.media = me.cells.media;
+  G.patch_in = me.patch;
+  for (int t = threadIdx.x; t < me.pc.n * me.pc.n; t += blockDim.x) gbf_split_patch_cell(me.C, me.pc, G, t);
+}
+
 // Packed all-members FP64 state (staging) -> every member's current buffer
 // (and the next buffer's faces, which the next step rewrites), one chunk
 // (member, cell range) per block.
@@ -470,6 +492,7 @@ struct gbf_ensemble {
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   int cur = 0;
+  bool any_patch = false;  // a split member under a Dirichlet patch: PATCH tiles and the step's pre-pass
   int shape = kShape32x8;
   std::map<int, int> kchunk_by_edge;  // fusion depth per member edge (0 = default rule)
   int persistent_blocks = 0;
@@ -685,11 +708,12 @@ EnsCfl ens_cfl(const gbf_ensemble* e) {
   return {e->d_mass_count, on ? e->d_cfl_hist : nullptr, e->n, e->mass_cap};
 }
 
-template <int MR, int TX, int TY>
+template <int MR, int TX, int TY, bool PATCH>
 int launch_split_step_t(gbf_ensemble* e, double* partials, cudaStream_t st, const TileRange& tr) {
   const bool tma = e->d_maps != nullptr, cfl = partials && ens_cfl(e).hist;
-  auto kern = tma ? (cfl ? k_ens_split_step<MR, TX, TY, true, true> : k_ens_split_step<MR, TX, TY, true, false>)
-                  : (cfl ? k_ens_split_step<MR, TX, TY, false, true> : k_ens_split_step<MR, TX, TY, false, false>);
+  auto kern = tma ? (cfl ? k_ens_split_step<MR, TX, TY, true, true, PATCH> : k_ens_split_step<MR, TX, TY, true, false, PATCH>)
+                  : (cfl ? k_ens_split_step<MR, TX, TY, false, true, PATCH>
+                         : k_ens_split_step<MR, TX, TY, false, false, PATCH>);
   int per_sm = 0;
   GBF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TX * TY, 0));
   const int blocks = std::max(1, std::min(tr.nt, per_sm * gbf_num_sms()));
@@ -700,10 +724,11 @@ int launch_split_step_t(gbf_ensemble* e, double* partials, cudaStream_t st, cons
   return GBF_OK;
 }
 
-template <int MR, int TXC, int TY>
+template <int MR, int TXC, int TY, bool PATCH>
 int launch_split_step_x2(gbf_ensemble* e, double* partials, cudaStream_t st, const TileRange& tr) {
   if (!e->d_maps) return gbf_fail(GBF_ERR_STATE, "x-pair tile without TMA maps");
-  auto kern = (partials && ens_cfl(e).hist) ? k_ens_split_step_x2<MR, TXC, TY, true> : k_ens_split_step_x2<MR, TXC, TY, false>;
+  auto kern = (partials && ens_cfl(e).hist) ? k_ens_split_step_x2<MR, TXC, TY, true, PATCH>
+                                            : k_ens_split_step_x2<MR, TXC, TY, false, PATCH>;
   const int bytes = (int)sizeof(GbfPairCta<TXC, TY, MR>);
   GBF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
   int per_sm = 0;
@@ -716,10 +741,10 @@ int launch_split_step_x2(gbf_ensemble* e, double* partials, cudaStream_t st, con
   return GBF_OK;
 }
 
-template <int MR>
+template <int MR, bool PATCH>
 int launch_split_step_x2m(gbf_ensemble* e, double* partials, cudaStream_t st, const TileRange& tr) {
   if (!e->d_maps) return gbf_fail(GBF_ERR_STATE, "x-pair tile without TMA maps");
-  auto kern = (partials && ens_cfl(e).hist) ? k_ens_split_step_x2m<MR, true> : k_ens_split_step_x2m<MR, false>;
+  auto kern = (partials && ens_cfl(e).hist) ? k_ens_split_step_x2m<MR, true, PATCH> : k_ens_split_step_x2m<MR, false, PATCH>;
   const int bytes = (int)sizeof(GbfPairCtaMixed<MR>);
   GBF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
   int per_sm = 0;
@@ -732,16 +757,23 @@ int launch_split_step_x2m(gbf_ensemble* e, double* partials, cudaStream_t st, co
   return GBF_OK;
 }
 
+template <int MR, bool PATCH>
+int launch_split_shape(gbf_ensemble* e, double* partials, cudaStream_t st, const TileRange& tr) {
+  switch (e->shape) {
+    case kShapeMixedx2: return launch_split_step_x2m<MR, PATCH>(e, partials, st, tr);
+    case kShape64x8x2: return launch_split_step_x2<MR, 64, 8, PATCH>(e, partials, st, tr);
+    case kShape32x16x2: return launch_split_step_x2<MR, 32, 16, PATCH>(e, partials, st, tr);
+    case kShape64x4: return launch_split_step_t<MR, 64, 4, PATCH>(e, partials, st, tr);
+    case kShape32x4: return launch_split_step_t<MR, 32, 4, PATCH>(e, partials, st, tr);
+    default: return launch_split_step_t<MR, 32, 8, PATCH>(e, partials, st, tr);
+  }
+}
+
+// Ensembles with a member under a Dirichlet patch run the PATCH tiles.
 template <int MR>
 int launch_split_form(gbf_ensemble* e, double* partials, cudaStream_t st, const TileRange& tr) {
-  switch (e->shape) {
-    case kShapeMixedx2: return launch_split_step_x2m<MR>(e, partials, st, tr);
-    case kShape64x8x2: return launch_split_step_x2<MR, 64, 8>(e, partials, st, tr);
-    case kShape32x16x2: return launch_split_step_x2<MR, 32, 16>(e, partials, st, tr);
-    case kShape64x4: return launch_split_step_t<MR, 64, 4>(e, partials, st, tr);
-    case kShape32x4: return launch_split_step_t<MR, 32, 4>(e, partials, st, tr);
-    default: return launch_split_step_t<MR, 32, 8>(e, partials, st, tr);
-  }
+  return e->any_patch ? launch_split_shape<MR, true>(e, partials, st, tr)
+                      : launch_split_shape<MR, false>(e, partials, st, tr);
 }
 
 int launch_split_step(gbf_ensemble* e, double* partials, cudaStream_t st, const TileRange& tr) {
@@ -761,6 +793,7 @@ int enqueue_step(gbf_ensemble* e, cudaStream_t st) {
   if (e->precision != GBF_PREC_F64) {
     GBF_CUDA(cudaMemsetAsync(e->d_counter, 0, sizeof(unsigned), st));
     ev = gbf_timer_begin(tm, st);
+    if (e->any_patch) k_ens_split_patch<<<e->n, 64, 0, st>>>(e->d_mem, 0, e->cur);  // timed with the step
     if (int s = launch_split_step(e, partials, st, {0, (int)e->tiles.size(), e->cur, e->d_counter, e->d_order}))
       return s;
     gbf_timer_end(tm, GBF_K_ENS_STEP, ev, st);
@@ -828,6 +861,7 @@ int enqueue_group_step(gbf_ensemble* e, int r0, int r1, int cur, unsigned* count
   const auto &a = e->starts[r0], &b = e->starts[r1];
   if (e->precision != GBF_PREC_F64) {
     GBF_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned), st));
+    if (e->any_patch) k_ens_split_patch<<<r1 - r0, 64, 0, st>>>(e->d_mem, r0, cur);
     if (int s = launch_split_step(e, nullptr, st, {a.tiles, b.tiles - a.tiles, cur, counter, nullptr})) return s;
     if (kShapePairs[e->shape])
       k_ens_split_faces<<<(unsigned)(b.bnd - a.bnd), kThreads, 0, st>>>(e->d_mem, e->d_bnd + a.bnd, cur);
@@ -935,6 +969,13 @@ int gbf_ensemble_create(int n, const gbf_model* models, const gbf_cells* host_ce
       }
       s |= ens_alloc(e, (void**)&me.M1, nc * gbf_mass_bytes(gbf_mass_rep(precision)));
       s |= ens_alloc(e, (void**)&me.M2, nc * gbf_mass_bytes(gbf_mass_rep(precision)));
+      me.pc = gbf_patch_consts(m);
+      if (me.pc.n > 0) {  // zeroed: entries outside the interior are never written (nor used)
+        s |= ens_alloc(e, (void**)&me.patch, sizeof(float2) * (size_t)me.pc.n * me.pc.n);
+        if (!s) s |= gbf_cuda_check(cudaMemset(me.patch, 0, sizeof(float2) * (size_t)me.pc.n * me.pc.n),
+                                    "gbf_ensemble patch");
+        e->any_patch = true;
+      }
     } else {
       for (int b = 0; b < 2; b++) {
         s |= ens_alloc(e, (void**)&me.P[b], nc * sizeof(double));
@@ -1238,7 +1279,7 @@ int gbf_ensemble_kernel_times(gbf_ensemble* e, double* ms, int* launches, int nk
 int gbf_ensemble_launches_per_step(gbf_ensemble* e) {
   if (!e) return 0;
   const int mass = (e->out_flags & GBF_OUT_MASS) ? 2 : 0;
-  return (e->precision == GBF_PREC_F64 ? 3 : 2) + mass;
+  return (e->precision == GBF_PREC_F64 ? 3 : 2 + (e->any_patch ? 1 : 0)) + mass;
 }
 
 int gbf_ensemble_set_tuning(gbf_ensemble* e, int shape, int edge, int kchunk) {

@@ -21,6 +21,24 @@
 
 #include "gbf_split_tile.cuh"
 
+GbfPatchConsts gbf_patch_consts(const gbf_model& m) {
+  GbfPatchConsts P = {};
+  if (m.source_mode != GBF_SOURCE_DIRICHLET_PATCH || m.source < 0) return P;
+  P.n = 2 * m.source + 1;
+  P.i0 = m.nx / 2 - m.source;
+  P.k0 = m.nz / 2 - m.source;
+  P.S2 = m.S2_gr;
+  P.nmr2 = -m.ro02 / m.mu2;
+  P.gh2 = m.g * m.h2;
+  P.wy = m.dt * m.kv / (m.h2 * m.h2);
+  for (int md = 0; md < 2; md++) {
+    P.K[md] = m.K[md];
+    P.se_b[md] = -1.0 / (1.0 - m.S_wr[md]);
+    P.e2[md] = (2. + m.lambda[md]) / m.lambda[md];
+  }
+  return P;
+}
+
 GbfSplitConsts gbf_split_consts(const gbf_model& m) {
   GbfSplitConsts C = {};
   C.nx = m.nx; C.ny = m.ny; C.nz = m.nz;
@@ -32,6 +50,11 @@ GbfSplitConsts gbf_split_consts(const gbf_model& m) {
     C.ri0 = m.nx / 2 - m.rate_cells / 2;
     C.rk0 = m.nz / 2 - m.rate_cells / 2;
     src = m.rate / (double)(m.rate_cells * m.rate_cells) / V;
+  } else {  // the cells under the Dirichlet patch (the PATCH tiles; gbf_patch_consts)
+    const GbfPatchConsts P = gbf_patch_consts(m);
+    C.rn = P.n;
+    C.ri0 = P.i0;
+    C.rk0 = P.k0;
   }
   const double H = m.ro01 * m.g * m.h2;
   C.H = (float)H;
@@ -93,7 +116,7 @@ __host__ __device__ int tiles_x2(const GbfSplitConsts& C) { return (C.nx - 1 + k
 __host__ __device__ int tiles_y2(const GbfSplitConsts& C) { return (C.ny - 2 + kPairTY - 1) / kPairTY; }
 
 // The plain-load tile on one grid (grids without TMA staging).
-template <int MR, bool CFL>
+template <int MR, bool CFL, bool PATCH>
 __global__ void __launch_bounds__(kSplitThreads, 4) k_split_step(const GbfSplitConsts C, const GbfSplitGrid G,
                                                               const int kchunk) {
   __shared__ GbfSplitPlane pl[2];
@@ -103,14 +126,14 @@ __global__ void __launch_bounds__(kSplitThreads, 4) k_split_step(const GbfSplitC
   const int k0 = 1 + kc * kchunk;
   const int k1 = min(k0 + kchunk, C.nz - 1);
   GbfSplitAcc<MR> acc;
-  split_tile<MR, kSplitTX, kSplitTY, false, CFL>(C, G, 1 + tx * kSplitTX, 1 + ty * kSplitTY, k0, k1, pl, acc);
+  split_tile<MR, kSplitTX, kSplitTY, false, CFL, PATCH>(C, G, 1 + tx * kSplitTX, 1 + ty * kSplitTY, k0, k1, pl, acc);
   if (acc.bad) atomicOr(G.status, GBF_DEV_NONFINITE);
   if (G.mass_partials) split_block_mass<MR>(acc, C.V, G.mass_partials + 2 * blockIdx.x);
   if constexpr (CFL) split_block_cfl<kSplitThreads>(acc.cfl1, acc.cfl2, G.cfl_out);
 }
 
 // The x-pair tile on one grid: one tile (64 x 8 cells, a k range) per CTA.
-template <int MR, bool CFL>
+template <int MR, bool CFL, bool PATCH>
 __global__ void __launch_bounds__(kPairTX / 2 * kPairTY, gbf_pair_ctas(MR)) k_split_step_x2(const GbfSplitConsts C,
                                                                          const GbfSplitGrid G, const int kchunk,
                                                                          const GbfTmaSet* maps, int buf) {
@@ -130,8 +153,9 @@ __global__ void __launch_bounds__(kPairTX / 2 * kPairTY, gbf_pair_ctas(MR)) k_sp
   __syncthreads();
   unsigned phases = 0;
   GbfSplitAcc<MR> acc;
-  split_tile_x2<MR, kPairTX, kPairTY, CFL>(C, G, kPairTX * tx, 1 + kPairTY * ty, k0, k1, cta.bars, cta.body, acc,
-                                           maps, buf, &phases);
+  split_tile_x2<MR, kPairTX, kPairTY, CFL, kPairTX / 2 * kPairTY, PATCH>(C, G, kPairTX * tx, 1 + kPairTY * ty, k0,
+                                                                         k1, cta.bars, cta.body, acc, maps, buf,
+                                                                         &phases);
   if (acc.bad) atomicOr(G.status, GBF_DEV_NONFINITE);
   if (G.mass_partials) split_block_mass<MR, kPairTX / 2 * kPairTY>(acc, C.V, G.mass_partials + 2 * blockIdx.x);
   if constexpr (CFL) split_block_cfl<kPairTX / 2 * kPairTY>(acc.cfl1, acc.cfl2, G.cfl_out);
@@ -249,25 +273,44 @@ int gbf_split_kchunk_x2(const GbfSplitConsts& C, int mr) {
                                 (long long)gbf_pair_ctas(mr) * gbf_num_sms());
 }
 
-template <int MR, bool CFL>
+template <int MR, bool CFL, bool PATCH>
 int launch_x2(const GbfSplitConsts& C, const GbfSplitGrid& G, const GbfTmaSet* maps, int buf, cudaStream_t st,
               unsigned& blocks) {
   const int kchunk = gbf_split_kchunk_x2(C, MR);
   blocks = (unsigned)(tiles_x2(C) * tiles_y2(C) * ((C.nz - 2 + kchunk - 1) / kchunk));
   const int bytes = (int)sizeof(GbfPairCta<kPairTX, kPairTY, MR>);
-  GBF_CUDA(cudaFuncSetAttribute(k_split_step_x2<MR, CFL>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-  k_split_step_x2<MR, CFL><<<blocks, kPairTX / 2 * kPairTY, bytes, st>>>(C, G, kchunk, maps, buf);
+  GBF_CUDA(cudaFuncSetAttribute(k_split_step_x2<MR, CFL, PATCH>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  k_split_step_x2<MR, CFL, PATCH><<<blocks, kPairTX / 2 * kPairTY, bytes, st>>>(C, G, kchunk, maps, buf);
   return GBF_OK;
 }
 
+namespace {
+// The Dirichlet patch's pre-pass, one thread per patch cell (gbf_split_patch_cell).
+__global__ void __launch_bounds__(kThreads) k_split_patch(const GbfSplitConsts C, const GbfPatchConsts P,
+                                                          const GbfSplitGrid G) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < P.n * P.n; t += gridDim.x * blockDim.x)
+    gbf_split_patch_cell(C, P, G, t);
+}
+}  // namespace
+
+template <int MR, bool PATCH>
+int launch_tiles(const GbfSplitConsts& C, const GbfSplitGrid& G, const GbfTmaSet* maps, int buf, cudaStream_t st,
+                 unsigned& blocks, int kchunk) {
+  const bool cfl = G.cfl_out != nullptr;
+  if (maps)
+    return cfl ? launch_x2<MR, true, PATCH>(C, G, maps, buf, st, blocks)
+               : launch_x2<MR, false, PATCH>(C, G, maps, buf, st, blocks);
+  if (cfl) k_split_step<MR, true, PATCH><<<blocks, kSplitThreads, 0, st>>>(C, G, kchunk);
+  else k_split_step<MR, false, PATCH><<<blocks, kSplitThreads, 0, st>>>(C, G, kchunk);
+  return GBF_OK;
+}
+
+// The tiles under a Dirichlet patch (G.patch_in set) are the PATCH instantiations.
 template <int MR>
 int launch_form(const GbfSplitConsts& C, const GbfSplitGrid& G, const GbfTmaSet* maps, int buf, cudaStream_t st,
                 unsigned& blocks, int kchunk) {
-  const bool cfl = G.cfl_out != nullptr;
-  if (maps) return cfl ? launch_x2<MR, true>(C, G, maps, buf, st, blocks) : launch_x2<MR, false>(C, G, maps, buf, st, blocks);
-  if (cfl) k_split_step<MR, true><<<blocks, kSplitThreads, 0, st>>>(C, G, kchunk);
-  else k_split_step<MR, false><<<blocks, kSplitThreads, 0, st>>>(C, G, kchunk);
-  return GBF_OK;
+  return G.patch_in ? launch_tiles<MR, true>(C, G, maps, buf, st, blocks, kchunk)
+                    : launch_tiles<MR, false>(C, G, maps, buf, st, blocks, kchunk);
 }
 
 int gbf_split_launch_domain(const gbf_model& m, const GbfSplitConsts& C, const GbfSplitGrid& G, int mr,
@@ -277,6 +320,10 @@ int gbf_split_launch_domain(const gbf_model& m, const GbfSplitConsts& C, const G
   const int nkc = (C.nz - 2 + kchunk - 1) / kchunk;
   unsigned blocks = (unsigned)(tiles_x(C) * tiles_y(C) * nkc);
   cudaEvent_t e = gbf_timer_begin(tm, st);
+  if (G.patch_in) {  // the Dirichlet patch's FP64 inflow, timed with the step kernel
+    const GbfPatchConsts P = gbf_patch_consts(m);
+    k_split_patch<<<gbf_grid_for((size_t)P.n * P.n, kThreads), kThreads, 0, st>>>(C, P, G);
+  }
   // TMA staging (maps): the x-pair tile; else the plain-load tile
   const int s = mr == kMassDefect ? launch_form<kMassDefect>(C, G, maps, buf, st, blocks, kchunk)
                 : mr == kMassDF   ? launch_form<kMassDF>(C, G, maps, buf, st, blocks, kchunk)
@@ -326,6 +373,12 @@ int gbf_split_alloc(gbf_domain* d) {
     s |= gbf_defect_k1(d->m, d->cells.phi, d->cells.media, &d->defect_k1v, nullptr);  // after the cells' copies
   // per-block mass partials of the split step kernel
   if (!s) s |= gbf_domain_alloc(d, (void**)&d->split_partials, 2 * sizeof(double) * gbf_split_blocks(d->m, gbf_mass_rep(d->precision)));
+  // the Dirichlet patch's inflow, one FP32 pair per patch cell
+  const int pn = gbf_patch_consts(d->m).n;
+  if (!s && pn > 0) {  // zeroed: entries outside the interior are never written (nor used)
+    s |= gbf_domain_alloc(d, (void**)&d->split_patch, sizeof(float2) * (size_t)pn * pn);
+    if (!s) s |= gbf_cuda_check(cudaMemset(d->split_patch, 0, sizeof(float2) * (size_t)pn * pn), "gbf_split_alloc");
+  }
   if (s) return GBF_ERR_NOMEM;
   // TMA plane loads: FP32 K and phi fields, no media table, rows of whole 16-byte units
   const gbf_model& m = d->m;
@@ -416,6 +469,7 @@ int gbf_split_step(gbf_domain* d) {
   G.mass_partials = nullptr;
   G.status = d->status;
   G.cfl_out = nullptr;
+  G.patch_in = d->split_patch;
   double* mass_out = nullptr;
   if ((d->out_flags & GBF_OUT_MASS) && d->mass_hist && d->mass_count < d->mass_cap) {
     G.mass_partials = d->split_partials;
@@ -457,7 +511,9 @@ int gbf_split_state_to_f64(const gbf_model& m, const float* dPf, const float* Sf
   return GBF_OK;
 }
 
-int gbf_split_launches_per_step(gbf_domain* d) { return 2 + ((d->out_flags & GBF_OUT_MASS) ? 1 : 0); }
+int gbf_split_launches_per_step(gbf_domain* d) {
+  return 2 + ((d->out_flags & GBF_OUT_MASS) ? 1 : 0) + (d->split_patch ? 1 : 0);
+}
 
 // ----------------------------------------------------------- diagnostics
 // The bounded mbarrier wait of the TMA tiles, run on a barrier phase that

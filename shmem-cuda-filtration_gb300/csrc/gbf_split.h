@@ -9,7 +9,7 @@
 struct GbfSplitConsts {
   int nx, ny, nz;
   int noflow_bottom;  // GBF_BC_HYDROSTATIC_SIDES: no-flow bottom face and hydrostatic P on the i and k sides
-  int ri0, rk0, rn;  // rate-injection patch on the j = 1 layer (rn = 0: none)
+  int ri0, rk0, rn;  // the source's cells on the j = 1 layer: the rate injection's or those under the Dirichlet patch (rn = 0: none)
   float H;  // rho01 g h2: hydrostatic pressure step per cell (main.cpp:114)
   // Face potentials are kept as pressure differences (times h): their
   // gravity terms g rho01 beta1 h2, g rho02 beta2 h2, g (rho02 - rho01) h2,
@@ -34,6 +34,19 @@ struct GbfSplitConsts {
   double ro01b1_d, ro02b2_d;  // rho01 beta1, rho02 beta2 (the defect form's row densities)
 };
 GbfSplitConsts gbf_split_consts(const gbf_model& m);
+
+// The reference's Dirichlet patch (GBF_SOURCE_DIRICHLET_PATCH): top-face cells
+// i in [i0, i0 + n), k in [k0, k0 + n) that hold S2_gr and P_atm (cpu.cpp:346).
+// The split forms take the DNAPL inflow of the j = 1 cells below them in FP64
+// from the step's pre-pass (gbf_split_patch_cell); its constants, apart from
+// the tiles' GbfSplitConsts (where ri0, rk0, rn then mark the same cells).
+// n = 0: no patch.
+struct GbfPatchConsts {
+  int i0, k0, n;
+  double S2, nmr2, gh2, wy;     // S2_gr, -rho02 / mu2, g h2, dt kv / h2^2
+  double K[2], se_b[2], e2[2];  // media table: K, -1 / (1 - S_wr), (2 + lambda) / lambda
+};
+GbfPatchConsts gbf_patch_consts(const gbf_model& m);
 
 // How the split forms hold the per-cell phase masses M1, M2 (gbf_split_tile.cuh):
 // kMassDF FP32 pairs; kMassDefect FP32 defects over the mass of the FP32
@@ -62,6 +75,10 @@ struct GbfSplitGrid {
   double* mass_partials;  // NULL: no phase-mass sums
   unsigned* status;
   float* cfl_out;  // NULL: no CFL numbers; else the step's [2] slot (max-combined with atomicMax)
+  // Dirichlet patch (the PATCH tiles): the FP64 DNAPL inflow of the j = 1
+  // cells under it, (i - ri0) + rn (k - rk0), as FP32 pairs, written by the
+  // step's pre-pass (gbf_split_patch_cell); NULL without a patch
+  float2* patch_in;
 };
 
 int gbf_split_alloc(gbf_domain* d);

@@ -546,14 +546,22 @@ __device__ __forceinline__ unsigned split_row_flags(const GbfSplitConsts& C, int
 // the upwind selections, the MUFU functions and the rare branches (rate
 // source, second Newton iteration) run lane by lane. Lanes with count[n]
 // false are computed but neither added to the mass sums nor checked for
-// non-finite values.
-template <int MR, int N, bool CFL = false>
+// non-finite values. PATCH, for a grid with patch_in set: the source's cells
+// are those under the Dirichlet patch, whose DNAPL inflow through the patch
+// face comes in FP64 from the step's pre-pass (gbf_split_patch_cell) as
+// patch_in[(i - ri0) + rn (k - rk0)] (i0 the column of lane 0) and takes the
+// place of that face in the FP32 divergence. Grids without patch_in (an
+// ensemble's rate-source members beside a patch member) keep the rate source
+// in the PATCH tiles; the instantiations without PATCH, the tiles of every
+// workload without a patch, have no patch code at all.
+template <int MR, int N, bool CFL = false, bool PATCH = false>
 __device__ __forceinline__ void split_cells(const GbfSplitConsts& C, const GbfCellIn (&in)[N],
                                             const typename MassRep<MR>::T (&M1)[N],
                                             const typename MassRep<MR>::T (&M2)[N], typename WideOf<MR>::T R01,
                                             typename WideOf<MR>::T R02, const GbfDefectRow& rw, int md,
                                             unsigned rowf, int j, int k, bool phi_field, bool mass,
-                                            const bool (&count)[N], GbfSplitAcc<MR>& acc, GbfCellOut<MR> (&o)[N]) {
+                                            const bool (&count)[N], GbfSplitAcc<MR>& acc, GbfCellOut<MR> (&o)[N],
+                                            const float2* patch_in, int i0) {
   using W = WideOf<MR>;
   using WT = typename W::T;
   using L = Lanes<N>;
@@ -613,7 +621,13 @@ __device__ __forceinline__ void split_cells(const GbfSplitConsts& C, const GbfCe
     o[n].fz2 = L::get(bz2, n);
   }
   const F dy1 = vfma(y11, upw(y11, L1ym, L1c), vneg(ay2));  // ay1 - ay2
-  const F dy2 = vfma(y12, upw(y12, L2ym, L2c), vneg(by2));
+  F dy2 = vfma(y12, upw(y12, L2ym, L2c), vneg(by2));
+  bool patch = false;  // the source is the Dirichlet patch's FP64 inflow
+  if constexpr (PATCH) {  // the patch face leaves the FP32 divergence (its FP64 inflow is the source below)
+    patch = patch_in != nullptr;
+    if (patch && (rowf >> 1) != 0u && (unsigned)(k - C.rk0) < (unsigned)C.rn)
+      dy2 = L::make([&](int n) { return ((rowf >> (1 + n)) & 1u) ? -L::get(by2, n) : L::get(dy2, n); });
+  }
   // dt times the flux divergence: sum over directions of (in - out) dt / h^2
   // (kv in y), then the FP32 mass increments -(..) / phi
   const F f = vfma(vsub(az1, az2), sp(C.wz),
@@ -663,7 +677,22 @@ __device__ __forceinline__ void split_cells(const GbfSplitConsts& C, const GbfCe
     insrc[n] = ksrc && ((rowf >> (1 + n)) & 1u);
     anysrc |= insrc[n];
   }
-  if (anysrc) {
+  if (patch) {  // the Dirichlet patch's FP64 inflow (an FP32 pair) in place of the rate (PATCH only)
+    if (anysrc) {
+#pragma unroll
+      for (int n = 0; n < N; n++)
+        if (insrc[n]) {  // i0 + n in [ri0, ri0 + rn), k in [rk0, rk0 + rn): inside the rn x rn array
+          const float2 wp = patch_in[(i0 + n - C.ri0) + C.rn * (k - C.rk0)];
+          if constexpr (DEF) {
+            srcf[n] = wp.x;
+            srcl[n] = wp.y;
+          } else {
+            T2[n] = W::add(T2[n], W::c((double)wp.x + (double)wp.y, wp));
+            srcf[n] = wp.x;
+          }
+        }
+    }
+  } else if (anysrc) {
 #pragma unroll
     for (int n = 0; n < N; n++) {
       const WT src = phi_field ? W::div_f(W::c(C.dtsrc_d, C.dtsrc_df), in[n].phi)
@@ -963,7 +992,7 @@ __device__ __forceinline__ void split_cells(const GbfSplitConsts& C, const GbfCe
 // call returns false if a bounded wait gave up (the status word then carries
 // GBF_DEV_TIMEOUT). `phases` holds the barrier parities across calls.
 // TMA = false: plain loads, one plane prefetched in registers, two buffers.
-template <int MR, int TX = kSplitTX, int TY = kSplitTY, bool TMA = false, bool CFL = false>
+template <int MR, int TX = kSplitTX, int TY = kSplitTY, bool TMA = false, bool CFL = false, bool PATCH = false>
 __device__ bool split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i0, int j0, int k0, int k1,
                            GbfSplitPlaneT<TX, TY, gbf_plane_pitch<TX, TMA>()>* pl, GbfSplitAcc<MR>& acc,
                            GbfRawRing<TX, TY, MR>* raw = nullptr, const GbfTmaSet* maps = nullptr, int buf = 0,
@@ -1193,8 +1222,8 @@ __device__ bool split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i
       const MT m1s[1] = {M1}, m2s[1] = {M2};
       const bool cnt[1] = {true};
       GbfCellOut<MR> os[1];
-      split_cells<MR, 1, CFL>(C, ins, m1s, m2s, R01, R02, rw, md, rowf, j, k, G.phi != nullptr,
-                              G.mass_partials != nullptr, cnt, acc, os);
+      split_cells<MR, 1, CFL, PATCH>(C, ins, m1s, m2s, R01, R02, rw, md, rowf, j, k, G.phi != nullptr,
+                                     G.mass_partials != nullptr, cnt, acc, os, G.patch_in, i);
       G.dPn[c] = os[0].dPn;
       G.Sn[c] = os[0].Sn;
       MassRep<MR>::store(G.M1, c, os[0].M1n);
@@ -1480,7 +1509,7 @@ template <> struct WidePair<kMassDefect> {  // FP32 defects: two floats
 // updated by split_cell, so results equal the other tiles' bit for bit. The
 // CTA has NTB >= TXC / 2 * TY threads; the ones beyond the tile take part in
 // the barriers only.
-template <int MR, int TXC, int TY, bool CFL = false, int NTB = TXC / 2 * TY>
+template <int MR, int TXC, int TY, bool CFL = false, int NTB = TXC / 2 * TY, bool PATCH = false>
 __device__ bool split_tile_x2(const GbfSplitConsts& C, const GbfSplitGrid& G, int x0, int j0, int k0, int k1,
                               GbfPairBars<MR>& bars, GbfPairSmem<TXC, TY, MR>& sm, GbfSplitAcc<MR>& acc,
                               const GbfTmaSet* maps, int buf, unsigned* phases) {
@@ -1684,8 +1713,8 @@ __device__ bool split_tile_x2(const GbfSplitConsts& C, const GbfSplitGrid& G, in
       const MT m1s[2] = {M1a, M1b}, m2s[2] = {M2a, M2b};
       const bool cnt[2] = {act_a, act_b};
       GbfCellOut<MR> o[2];
-      split_cells<MR, 2, CFL>(C, in, m1s, m2s, R01, R02, rw, 0, rowf, j, k, true, G.mass_partials != nullptr, cnt,
-                              acc, o);
+      split_cells<MR, 2, CFL, PATCH>(C, in, m1s, m2s, R01, R02, rw, 0, rowf, j, k, true, G.mass_partials != nullptr,
+                                     cnt, acc, o, G.patch_in, ia);
       // The x faces i = 0 and i = nx - 1 (rows and planes interior) take the
       // boundary rules' values here: the new S of the x-neighbour and its dP
       // (cpu.cpp:327-331, 366-372), or the hydrostatic side value dP = 0 with
@@ -1704,4 +1733,47 @@ __device__ bool split_tile_x2(const GbfSplitConsts& C, const GbfSplitGrid& G, in
     u = t_next;
   }
   return true;
+}
+
+// ------------------------------------------------ the Dirichlet patch's inflow
+// The DNAPL mass per pore volume that the j = 1 cell c gains this step through
+// its face with the patch cell c - nx above it, in FP64 from the stored FP32
+// state: the face potential with the centre cell's density (cpu.cpp:257-258)
+// and the donor-cell product (cpu.cpp:260-262), the patch cell's mobility at
+// exactly S2_gr (the boundary rules, cpu.cpp:343-362). dPb, dPc: the stored
+// pressure deviations of the patch cell and of c; Sc the stored S of c.
+__device__ __forceinline__ double split_patch_inflow(const GbfSplitConsts& C, const GbfPatchConsts& P,
+                                                     const GbfSplitGrid& G, unsigned c, int md, int mdb, float dPb,
+                                                     float dPc, float Sc, double phi) {
+  const unsigned b = c - (unsigned)C.nx;
+  const double Ppc = C.H_d + (double)dPc;                   // P - P_atm at the cell (j = 1)
+  const double rho2c = C.ro02_d * (1.0 + C.beta2_d * Ppc);  // the centre cell's density
+  const double pot = ((double)dPb - (double)dPc) - C.H_d + rho2c * P.gh2;  // h2 times the potential
+  auto mobility = [&](double K, int mdx, double S, double Pp) {
+    const double Se = 1.0 + S * P.se_b[mdx];
+    const double kr2 = (1.0 - Se) * (1.0 - Se) * (1.0 - pow(Se, P.e2[mdx]));
+    return K * kr2 * P.nmr2 * (1.0 + C.beta2_d * Pp);
+  };
+  const double L = pot >= 0.0 ? mobility(G.K ? (double)G.K[b] : P.K[mdb], mdb, P.S2, (double)dPb)
+                              : mobility(G.K ? (double)G.K[c] : P.K[md], md, (double)Sc, Ppc);
+  return -(pot * L) * P.wy / phi;
+}
+
+// The pre-pass of a step under the Dirichlet patch, patch cell t of n x n
+// (i = i0 + t % n, k = k0 + t / n), on the state the step starts from: the
+// j = 1 cell's FP64 DNAPL inflow into G.patch_in[t], as an FP32 pair, which
+// the step's tiles (PATCH) take in place of that face's FP32 flux. Where DNAPL
+// enters through the patch, every kilogram of it crosses these faces, so FP32
+// mobilities there (the hardware log2 / exp2, about 2^-22) would set the
+// relative precision of the whole DNAPL total. Cells of the patch's columns
+// outside the grid's interior are skipped (no tile reads them).
+__device__ __forceinline__ void gbf_split_patch_cell(const GbfSplitConsts& C, const GbfPatchConsts& P,
+                                                     const GbfSplitGrid& G, int t) {
+  const int i = P.i0 + t % P.n, k = P.k0 + t / P.n;
+  if (i < 1 || i > C.nx - 2 || k < 1 || k > C.nz - 2 || C.ny < 3) return;
+  const unsigned c = (unsigned)(i + C.nx) + (unsigned)k * (unsigned)C.nx * (unsigned)C.ny;  // j = 1
+  const unsigned b = c - (unsigned)C.nx;                                                     // the patch cell
+  const int md = G.media ? G.media[c] : 0, mdb = G.media ? G.media[b] : 0;
+  const double phi = G.phi ? (double)G.phi[c] : C.m_d[md];
+  G.patch_in[t] = gbf_df_from_double(split_patch_inflow(C, P, G, c, md, mdb, G.dP[b], G.dP[c], G.S[c], phi));
 }

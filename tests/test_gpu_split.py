@@ -6,10 +6,17 @@ oracle; relative L2 of P reported and bounded; relative phase-mass drift
 <= 1e-9 per step for water, and for DNAPL where it enters through the
 mass-rate source (the wide source term is exact to ~1e-15). Where DNAPL enters
 through the reference's Dirichlet patch instead, every kilogram of it crosses
-the patch faces' FP32 fluxes, and FP32 mobilities alone, in an otherwise FP64
-oracle, already move its total by 2.7e-8 (test_oracle's FP32-mobility
-experiment): 1e-9 is out of reach of any FP32-flux form there, and the bar is
-a fixed multiple of that experiment's drift, computed per case.
+the patch faces. The split forms take that inflow in FP64 (a pre-pass, then
+the PATCH tiles), which removes the FP32 mobilities' share (2.7e-8, the
+oracle's level-1 experiment); what is left is the FP32 flux arithmetic of
+the patch cells' outflow, which the oracle's level-3 and level-4 experiments
+put at 1.05e-9 and 1.3e-9 in the reference parameter file's case even under
+correctly rounded FP32 (test_oracle.test_fp32_flux_stage_bounds_patch_dnapl_mass):
+1e-9 is out of reach of any form with FP32 face fluxes there, and the bar is a
+fixed multiple of those experiments' drift, computed per case. split_df has
+no residual-correction step: its state carries the FP32 Newton's residual,
+the FP64 inflow is evaluated on that state, and its bar stays the multiple of
+the FP32-mobility experiment.
 """
 import numpy as np
 import pytest
@@ -21,19 +28,22 @@ pytestmark = pytest.mark.gpu
 
 SPLITS = ["split", "split_df", "split_defect"]
 DS_TOL = 1e-5
-# Dirichlet-patch DNAPL: the bar is this multiple of what FP32 mobilities alone
-# do to the oracle's DNAPL total (test_oracle.fp32_mobility_drift): the split
-# forms' mobilities come from the FP32 hardware log2/exp2 (about 2^-22 relative,
-# four times a correctly rounded FP32 value's 2^-24) on FP32 pressure
-# differences, and the patch cells' inflow carries their rounding into every
-# kilogram of DNAPL.
+# Dirichlet-patch DNAPL: the bar is this multiple of the oracle's FP32
+# experiments' drift of the DNAPL total (test_oracle.fp32_mobility_drift). The
+# experiments round correctly; the tiles' mobilities come from the hardware
+# log2/exp2 (about 2^-22 relative, four times a correctly rounded FP32
+# value's 2^-24) on FP32 pressure differences, and the drift they leave is a
+# random walk of roundings whose size the experiments give, not its path.
 PATCH_FACTOR = 16.0
 
 
-def patch_bound(abi, O, lib, case):
+def patch_bound(abi, O, lib, case, form):
+    """The experiment drift that bounds a form's Dirichlet DNAPL drift: FP32
+    flux arithmetic with the FP64 patch inflow (levels 3 and 4) for the forms
+    with the residual-correction step; FP32 mobilities (level 1) for split_df."""
     from test_oracle import fp32_mobility_drift
-    drift, _ = fp32_mobility_drift(abi, O, O.Oracle(abi), lib, case)
-    return float(drift[1])
+    levels = (1,) if form == "split_df" else (3, 4)
+    return max(float(fp32_mobility_drift(abi, O, O.Oracle(abi), lib, case, lv)[0][1]) for lv in levels)
 
 
 def prec(abi, name):
@@ -77,7 +87,7 @@ def test_split_matches_fp64_oracle(gpu_lib, abi, O, oracle, pkg, case, form):
         if not mask.any():
             continue
         drift = np.abs(mass[mask, ph] - ref[mask]) / np.abs(ref[mask])
-        bar = 1e-9 if (rate_mode or ph == 0) else max(1e-9, PATCH_FACTOR * patch_bound(abi, O, gpu_lib, case))
+        bar = 1e-9 if (rate_mode or ph == 0) else max(1e-9, PATCH_FACTOR * patch_bound(abi, O, gpu_lib, case, form))
         print(f"\n{case} {form} phase {ph + 1}: mass drift {drift.max():.3e} (bar {bar:.1e})")
         assert drift.max() <= bar, f"phase {ph + 1} drift {drift.max():.3e} > {bar:.1e}"
     dom.close()

@@ -161,22 +161,26 @@ def test_rate_injection_adds_mass(O, oracle, abi):
     assert st["S2"].max() > 0
 
 
-def fp32_mobility_drift(abi, O, oracle, lib, case):
+def fp32_mobility_drift(abi, O, oracle, lib, case, level=1):
     """Largest relative phase-mass difference per phase over a case's steps
-    between the oracle and the oracle with only its upwinded face mobilities
-    rounded to FP32 (everything else FP64)."""
+    between the oracle and the oracle at one FP32 experiment level
+    (Oracle.fp32_mobilities): 1 its upwinded face mobilities rounded to FP32,
+    everything else FP64; 2 the same but the Dirichlet patch's DNAPL faces;
+    3 the split forms' FP32 flux arithmetic with FP64 mobilities and the
+    patch's DNAPL inflow in FP64; 4 that with FP32 mobilities and the tile's
+    FMA-fused minus faces."""
     from test_gpu_f64 import make_case
     out = []
-    for on in (False, True):
+    for lv in (0, level):
         m, st, steps = make_case(abi, O, lib, case)
         m.newton_tol = 0.0
         st.model = m
         oracle.initial(st)
-        oracle.fp32_mobilities(on)
+        oracle.fp32_mobilities(lv)
         try:
             out.append(oracle.step(st, steps, want_mass=True))
         finally:
-            oracle.fp32_mobilities(False)
+            oracle.fp32_mobilities(0)
     ref, exp = out
     scale = np.where(np.abs(ref) > 0, np.abs(ref), 1.0)
     return (np.abs(exp - ref) / scale).max(axis=0), m
@@ -199,3 +203,31 @@ def test_fp32_mobilities_alone_bound_patch_dnapl_mass(abi, O, oracle, pkg, case)
         assert drift[1] >= 1e-8, drift
     else:
         assert drift[1] <= 1e-12, drift
+
+
+@pytest.mark.parametrize("case", ["reference_ini_16", "reference_odd_5x7x6", "c0_rate_hydrostatic_40",
+                                  "heterogeneous_aniso_24x20x18"])
+def test_fp32_flux_stage_bounds_patch_dnapl_mass(abi, O, oracle, pkg, case):
+    """What is left of the Dirichlet-patch DNAPL drift once the patch inflow
+    is FP64 (the split forms): FP32 mobilities on every other face move the
+    DNAPL total by less than 1e-9 (level 2), but the FP32 flux arithmetic
+    itself does not stay within it. The patch cells pass on every kilogram
+    that enters, and each step rounds their FP32 outflow increments, so the
+    total carries a random walk of about 2^-24 / sqrt(patch cells x steps):
+    1.05e-9 in the reference parameter file's 16^3 case under correctly
+    rounded FP32 with FP64 mobilities (level 3), 1.3e-9 with the tile's FP32
+    mobilities and FMA-fused minus faces (level 4). The mass-rate cases, whose
+    DNAPL enters through the exact source term, stay at round-off."""
+    lib = pkg.load_library()
+    d2, m = fp32_mobility_drift(abi, O, oracle, lib, case, 2)
+    d3, _ = fp32_mobility_drift(abi, O, oracle, lib, case, 3)
+    d4, _ = fp32_mobility_drift(abi, O, oracle, lib, case, 4)
+    print(f"\n{case}: DNAPL drift, FP32 mobilities but the patch faces {d2[1]:.2e}, "
+          f"FP32 flux arithmetic {d3[1]:.2e}, with FP32 mobilities {d4[1]:.2e}")
+    assert max(d2[0], d3[0], d4[0]) <= 1e-9, (d2, d3, d4)
+    if m.source_mode == abi.GBF_SOURCE_DIRICHLET_PATCH:
+        assert d2[1] <= 1e-9 and d3[1] >= 1e-10 and d4[1] >= 1e-10, (d2, d3, d4)
+        if case == "reference_ini_16":
+            assert d3[1] > 1e-9 and d4[1] > 1e-9, (d3, d4)
+    else:
+        assert max(d2[1], d3[1], d4[1]) <= 1e-12, (d2, d3, d4)
