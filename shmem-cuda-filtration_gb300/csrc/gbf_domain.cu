@@ -354,7 +354,7 @@ int gbf_domain_write_plots(gbf_domain* d, const char* dir, double t) {
     a.u2y = w + 11 * n; a.u2z = w + 12 * n;
     const int prev = d->cur ^ 1;
     int s = d->precision == GBF_PREC_F64 ? gbf_cuda_check(cudaMemcpyAsync(a.P1, d->P[prev], b, cudaMemcpyDeviceToDevice, d->stream), "copy P")
-                                         : gbf_split_state_to_f64(m, d->Pf[prev], d->Sf[prev], a.P1, a.S2, d->stream);
+                                         : gbf_split_state_to_f64(m, d->split_rows, d->Pf[prev], d->Sf[prev], a.P1, a.S2, d->stream);
     if (!s && d->precision == GBF_PREC_F64)
       s = gbf_cuda_check(cudaMemcpyAsync(a.S2, d->S[prev], b, cudaMemcpyDeviceToDevice, d->stream), "copy S");
     if (!s) s = gbf_props_f64(&m, a, d->cells, d->stream);

@@ -66,6 +66,7 @@ struct gbf_domain {
   double *M1 = nullptr, *M2 = nullptr;
   double* split_partials = nullptr;
   float2* split_patch = nullptr;  // the Dirichlet patch's FP64 inflow (split forms; NULL without a patch)
+  struct GbfRowConst* split_rows = nullptr;  // the split state conversions' row table (ny entries)
   double defect_k1v = 0.0;  // defect form: V sum of c1(j) phi over interior cells (gbf_defect_k1)
   void* tma = nullptr;  // device GbfTmaSet of the split state (NULL: plain loads)
   // mass tracking

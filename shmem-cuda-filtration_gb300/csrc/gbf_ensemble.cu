@@ -42,6 +42,7 @@ struct EnsMember {
   // inflow array (pc.n = 0, patch NULL: no patch)
   GbfPatchConsts pc;
   float2* patch;
+  GbfRowConst* rows;  // split forms: the row constants of the state conversions (ny entries)
 };
 
 struct EnsChunk {
@@ -427,13 +428,20 @@ __global__ void __launch_bounds__(kThreads) k_ens_load(const EnsMember* __restri
     } else {
       const int j = (int)((c / (unsigned)m.nx) % (unsigned)m.ny);
       float dPf, Sf;
-      gbf_split_init_cell(m, p, s, j, dPf, Sf, me.M1, me.M2, c, gbf_mass_rep(precision));
+      gbf_split_init_cell(m, p, s, me.rows[j], dPf, Sf, me.M1, me.M2, c, gbf_mass_rep(precision));
       me.dPf[cur][c] = dPf;
       me.Sf[cur][c] = Sf;
       me.dPf[cur ^ 1][c] = dPf;
       me.Sf[cur ^ 1][c] = Sf;
     }
   }
+}
+
+// The row-constant tables of the split members, one block per member.
+__global__ void k_ens_rows(const EnsMember* __restrict__ mem) {
+  const EnsMember& me = mem[blockIdx.x];
+  if (!me.rows) return;
+  for (int j = threadIdx.x; j < me.m.ny; j += blockDim.x) me.rows[j] = gbf_row_const(me.m, j);
 }
 
 // Every member's current state -> packed all-members FP64 arrays.
@@ -450,18 +458,9 @@ __global__ void __launch_bounds__(kThreads) k_ens_store(const EnsMember* __restr
       S_all[me.off + c] = me.S[cur][c];
     } else {
       const int j = (int)((c / (unsigned)m.nx) % (unsigned)m.ny);
-      P_all[me.off + c] = gbf_p_hydrostatic(m, j) + (double)me.dPf[cur][c];
+      P_all[me.off + c] = me.rows[j].phs + (double)me.dPf[cur][c];
       S_all[me.off + c] = (double)me.Sf[cur][c];
     }
-  }
-}
-
-__global__ void k_ens_split_to_f64(const gbf_model m, const float* dPf, const float* Sf, double* P, double* S) {
-  const GbfGeo g = gbf_geo(m);
-  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < g.n; c += (size_t)gridDim.x * blockDim.x) {
-    const int j = (int)((c / g.nx) % g.ny);
-    if (P) P[c] = gbf_p_hydrostatic(m, j) + (double)dPf[c];
-    if (S) S[c] = (double)Sf[c];
   }
 }
 
@@ -969,6 +968,7 @@ int gbf_ensemble_create(int n, const gbf_model* models, const gbf_cells* host_ce
       }
       s |= ens_alloc(e, (void**)&me.M1, nc * gbf_mass_bytes(gbf_mass_rep(precision)));
       s |= ens_alloc(e, (void**)&me.M2, nc * gbf_mass_bytes(gbf_mass_rep(precision)));
+      s |= ens_alloc(e, (void**)&me.rows, sizeof(GbfRowConst) * (size_t)m.ny);
       me.pc = gbf_patch_consts(m);
       if (me.pc.n > 0) {  // zeroed: entries outside the interior are never written (nor used)
         s |= ens_alloc(e, (void**)&me.patch, sizeof(float2) * (size_t)me.pc.n * me.pc.n);
@@ -992,6 +992,10 @@ int gbf_ensemble_create(int n, const gbf_model* models, const gbf_cells* host_ce
     cudaMemset(e->d_status, 0, sizeof(unsigned));
     cudaMemset(e->d_mass_count, 0, sizeof(unsigned));
     s = build_lists(e);
+  }
+  if (!s && e->precision != GBF_PREC_F64) {  // the members' row-constant tables, once
+    k_ens_rows<<<e->n, 64>>>(e->d_mem);
+    s = gbf_cuda_check(cudaDeviceSynchronize(), "gbf_ensemble_create rows");
   }
   if (s) {
     gbf_ensemble_destroy(e);
@@ -1066,7 +1070,7 @@ int gbf_ensemble_upload(gbf_ensemble* e, int r, const double* P1, const double* 
     GBF_CUDA(cudaMallocAsync((void**)&tmp, 2 * b, e->stream));
     GBF_CUDA(cudaMemcpyAsync(tmp, P1, b, cudaMemcpyDefault, e->stream));
     GBF_CUDA(cudaMemcpyAsync(tmp + nc, S2, b, cudaMemcpyDefault, e->stream));
-    if (int s = gbf_split_init_state(m, tmp, tmp + nc, me.dPf[c], me.Sf[c], me.M1, me.M2,
+    if (int s = gbf_split_init_state(m, me.rows, tmp, tmp + nc, me.dPf[c], me.Sf[c], me.M1, me.M2,
                                      gbf_mass_rep(e->precision), e->stream))
       return s;
     // the next-state buffer's faces are rewritten every step; start them equal
@@ -1231,9 +1235,9 @@ int gbf_ensemble_download(gbf_ensemble* e, int r, int field, double* host) {
   } else {
     double* tmp = nullptr;
     GBF_CUDA(cudaMallocAsync((void**)&tmp, b, e->stream));
-    k_ens_split_to_f64<<<gbf_grid_for(nc, kThreads, 4), kThreads, 0, e->stream>>>(
-        m, me.dPf[e->cur], me.Sf[e->cur], field == GBF_FIELD_P1 ? tmp : nullptr, field == GBF_FIELD_S2 ? tmp : nullptr);
-    GBF_CUDA(cudaGetLastError());
+    if (int s = gbf_split_state_to_f64(m, me.rows, me.dPf[e->cur], me.Sf[e->cur], field == GBF_FIELD_P1 ? tmp : nullptr,
+                                       field == GBF_FIELD_S2 ? tmp : nullptr, e->stream))
+      return s;
     GBF_CUDA(cudaMemcpyAsync(host, tmp, b, cudaMemcpyDefault, e->stream));
     GBF_CUDA(cudaFreeAsync(tmp, e->stream));
   }

@@ -217,22 +217,30 @@ __global__ void k_split_mass_tail(const double* partials, int nblocks, double* o
   if (threadIdx.x == 0) { out[0] = red[0][0] + k1v; out[1] = red[1][0]; }
 }
 
-__global__ void k_split_init(const gbf_model m, const double* P, const double* S, float* dPf, float* Sf,
-                             double* M1, double* M2, int mr) {
+// rows: the grid's row table (GbfRowConst), or NULL to form each row's
+// values per cell (the same values either way).
+__global__ void k_split_init(const gbf_model m, const GbfRowConst* rows, const double* P, const double* S,
+                             float* dPf, float* Sf, double* M1, double* M2, int mr) {
   const GbfGeo g = gbf_geo(m);
   for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < g.n; c += (size_t)gridDim.x * blockDim.x) {
     const int j = (int)((c / g.nx) % g.ny);
-    gbf_split_init_cell(m, P[c], S[c], j, dPf[c], Sf[c], M1, M2, c, mr);
+    if (rows) gbf_split_init_cell(m, P[c], S[c], rows[j], dPf[c], Sf[c], M1, M2, c, mr);
+    else gbf_split_init_cell(m, P[c], S[c], j, dPf[c], Sf[c], M1, M2, c, mr);
   }
 }
 
-__global__ void k_split_to_f64(const gbf_model m, const float* dPf, const float* Sf, double* P, double* S) {
+__global__ void k_split_to_f64(const gbf_model m, const GbfRowConst* rows, const float* dPf, const float* Sf,
+                               double* P, double* S) {
   const GbfGeo g = gbf_geo(m);
   for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < g.n; c += (size_t)gridDim.x * blockDim.x) {
     const int j = (int)((c / g.nx) % g.ny);
-    if (P) P[c] = gbf_p_hydrostatic(m, j) + (double)dPf[c];
+    if (P) P[c] = (rows ? rows[j].phs : gbf_p_hydrostatic(m, j)) + (double)dPf[c];
     if (S) S[c] = (double)Sf[c];
   }
+}
+
+__global__ void k_split_rows(const gbf_model m, GbfRowConst* rows) {
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < m.ny; j += gridDim.x * blockDim.x) rows[j] = gbf_row_const(m, j);
 }
 
 }  // namespace
@@ -373,6 +381,9 @@ int gbf_split_alloc(gbf_domain* d) {
     s |= gbf_defect_k1(d->m, d->cells.phi, d->cells.media, &d->defect_k1v, nullptr);  // after the cells' copies
   // per-block mass partials of the split step kernel
   if (!s) s |= gbf_domain_alloc(d, (void**)&d->split_partials, 2 * sizeof(double) * gbf_split_blocks(d->m, gbf_mass_rep(d->precision)));
+  // the row table of the state conversions
+  if (!s) s |= gbf_domain_alloc(d, (void**)&d->split_rows, sizeof(GbfRowConst) * (size_t)d->m.ny);
+  if (!s) s |= gbf_split_fill_rows(d->m, d->split_rows, d->stream);
   // the Dirichlet patch's inflow, one FP32 pair per patch cell
   const int pn = gbf_patch_consts(d->m).n;
   if (!s && pn > 0) {  // zeroed: entries outside the interior are never written (nor used)
@@ -419,10 +430,16 @@ int gbf_defect_k1(const gbf_model& m, const float* phi_dev, const int* media_dev
   return GBF_OK;
 }
 
-int gbf_split_init_state(const gbf_model& m, const double* P_dev, const double* S_dev, float* dPf, float* Sf,
-                         double* M1, double* M2, int mr, cudaStream_t st) {
+int gbf_split_fill_rows(const gbf_model& m, GbfRowConst* rows, cudaStream_t st) {
+  k_split_rows<<<gbf_grid_for((size_t)m.ny, kThreads), kThreads, 0, st>>>(m, rows);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? GBF_OK : gbf_cuda_check(e, "gbf_split_fill_rows");
+}
+
+int gbf_split_init_state(const gbf_model& m, const GbfRowConst* rows, const double* P_dev, const double* S_dev,
+                         float* dPf, float* Sf, double* M1, double* M2, int mr, cudaStream_t st) {
   const size_t n = gbf_geo(m).n;
-  k_split_init<<<gbf_grid_for(n, kThreads, 4), kThreads, 0, st>>>(m, P_dev, S_dev, dPf, Sf, M1, M2, mr);
+  k_split_init<<<gbf_grid_for(n, kThreads, 4), kThreads, 0, st>>>(m, rows, P_dev, S_dev, dPf, Sf, M1, M2, mr);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? GBF_OK : gbf_cuda_check(e, "gbf_split_init_state");
 }
@@ -445,7 +462,7 @@ int gbf_split_upload(gbf_domain* d, const double* P1, const double* S2, cudaMemc
   }
   d->cur = 0;
   k_split_init<<<gbf_grid_for(n, kThreads, 4), kThreads, 0, d->stream>>>(
-      d->m, P, S, d->Pf[0], d->Sf[0], d->M1, d->M2, gbf_mass_rep(d->precision));
+      d->m, d->split_rows, P, S, d->Pf[0], d->Sf[0], d->M1, d->M2, gbf_mass_rep(d->precision));
   GBF_CUDA(cudaGetLastError());
   // the next-state buffer's faces are rewritten every step; start them equal
   GBF_CUDA(cudaMemcpyAsync(d->Pf[1], d->Pf[0], n * sizeof(float), cudaMemcpyDeviceToDevice, d->stream));
@@ -494,7 +511,8 @@ int gbf_split_download(gbf_domain* d, int field, double* host) {
   const bool staged = tmp == nullptr;
   if (staged) GBF_CUDA(cudaMallocAsync((void**)&tmp, b, d->stream));
   k_split_to_f64<<<gbf_grid_for(n, kThreads, 4), kThreads, 0, d->stream>>>(
-      d->m, d->Pf[d->cur], d->Sf[d->cur], field == GBF_FIELD_P1 ? tmp : nullptr, field == GBF_FIELD_S2 ? tmp : nullptr);
+      d->m, d->split_rows, d->Pf[d->cur], d->Sf[d->cur], field == GBF_FIELD_P1 ? tmp : nullptr,
+      field == GBF_FIELD_S2 ? tmp : nullptr);
   GBF_CUDA(cudaGetLastError());
   if (staged) {
     GBF_CUDA(cudaMemcpyAsync(host, tmp, b, cudaMemcpyDeviceToHost, d->stream));
@@ -504,9 +522,9 @@ int gbf_split_download(gbf_domain* d, int field, double* host) {
   return GBF_OK;
 }
 
-int gbf_split_state_to_f64(const gbf_model& m, const float* dPf, const float* Sf, double* P, double* S,
-                           cudaStream_t st) {
-  k_split_to_f64<<<gbf_grid_for(gbf_geo(m).n, kThreads, 4), kThreads, 0, st>>>(m, dPf, Sf, P, S);
+int gbf_split_state_to_f64(const gbf_model& m, const GbfRowConst* rows, const float* dPf, const float* Sf, double* P,
+                           double* S, cudaStream_t st) {
+  k_split_to_f64<<<gbf_grid_for(gbf_geo(m).n, kThreads, 4), kThreads, 0, st>>>(m, rows, dPf, Sf, P, S);
   GBF_CUDA(cudaGetLastError());
   return GBF_OK;
 }

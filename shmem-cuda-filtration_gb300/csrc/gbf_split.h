@@ -48,6 +48,18 @@ struct GbfPatchConsts {
 };
 GbfPatchConsts gbf_patch_consts(const gbf_model& m);
 
+// A row's constants for the conversions between the FP64 state and the split
+// state: the hydrostatic pressure P_hs(j) and the defect forms' row densities
+// c1(j), c2(j) (gbf_row_const). Grids keep a table of them, one entry per row
+// j, filled once on the device, so that converting a whole grid does the FP64
+// row arithmetic once per row instead of once per cell.
+struct GbfRowConst {
+  double phs;
+  float c1, c2;
+};
+// Fill rows[0, ny) for the model (stream-ordered on st).
+int gbf_split_fill_rows(const gbf_model& m, GbfRowConst* rows, cudaStream_t st);
+
 // How the split forms hold the per-cell phase masses M1, M2 (gbf_split_tile.cuh):
 // kMassDF FP32 pairs; kMassDefect FP32 defects over the mass of the FP32
 // state at the row's hydrostatic density (4 bytes); kMassDefectDF the same
@@ -86,12 +98,14 @@ int gbf_split_upload(gbf_domain* d, const double* P1, const double* S2, cudaMemc
 int gbf_split_step(gbf_domain* d);
 int gbf_split_download(gbf_domain* d, int field, double* host);
 int gbf_split_launches_per_step(gbf_domain* d);
-// FP64 (P, S) of every cell from a split state (device arrays; either output may be NULL).
-int gbf_split_state_to_f64(const gbf_model& m, const float* dPf, const float* Sf, double* P, double* S,
-                           cudaStream_t st);
-// FP32 state and wide masses of one grid from FP64 device arrays.
-int gbf_split_init_state(const gbf_model& m, const double* P_dev, const double* S_dev, float* dPf, float* Sf,
-                         double* M1, double* M2, int mr, cudaStream_t st);
+// FP64 (P, S) of every cell from a split state (device arrays; either output
+// may be NULL; rows: the grid's row table, or NULL to form each row's values
+// per cell).
+int gbf_split_state_to_f64(const gbf_model& m, const GbfRowConst* rows, const float* dPf, const float* Sf, double* P,
+                           double* S, cudaStream_t st);
+// FP32 state and wide masses of one grid from FP64 device arrays (rows as above).
+int gbf_split_init_state(const gbf_model& m, const GbfRowConst* rows, const double* P_dev, const double* S_dev,
+                         float* dPf, float* Sf, double* M1, double* M2, int mr, cudaStream_t st);
 // V sum over interior cells of c1(j) phi (the defect form's water mass of a
 // fully water-saturated grid at the row densities): the part of the phase-1
 // mass the tiles' sums leave out. Written to *k1v_host; 0 for other forms.

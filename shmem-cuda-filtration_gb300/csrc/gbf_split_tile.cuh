@@ -1247,20 +1247,24 @@ __device__ bool split_tile(const GbfSplitConsts& C, const GbfSplitGrid& G, int i
 // the phase masses ro1 (1 - S2), ro2 S2 with P2 = P1 (cpu.cpp:72-73, 224-225)
 // in the representation `mr` (defect form: minus c1 (1 - S), c2 S of the
 // FP32 S, products that are exact in FP64).
-__device__ __forceinline__ void gbf_split_init_cell(const gbf_model& m, double p, double s, int j, float& dPf,
-                                                    float& Sf, double* M1, double* M2, size_t c, int mr) {
-  dPf = (float)(p - gbf_p_hydrostatic(m, j));
+// A row's constants for the state conversions (GbfRowConst), as
+// gbf_p_hydrostatic and gbf_defect_row give them.
+__device__ __forceinline__ GbfRowConst gbf_row_const(const gbf_model& m, int j) {
+  const GbfDefectRow w = gbf_defect_row(m, j);
+  return {gbf_p_hydrostatic(m, j), w.c1, w.c2};
+}
+__device__ __forceinline__ void gbf_split_init_cell(const gbf_model& m, double p, double s, const GbfRowConst& rc,
+                                                    float& dPf, float& Sf, double* M1, double* M2, size_t c, int mr) {
+  dPf = (float)(p - rc.phs);
   Sf = (float)s;
   const double m1 = m.ro01 * (1. + m.beta1 * (p - m.P_atm)) * (1. - s);
   const double m2 = m.ro02 * (1. + m.beta2 * (p - m.P_atm)) * s;
   if (mr == kMassDefect) {
-    const GbfDefectRow w = gbf_defect_row(m, j);
-    reinterpret_cast<float*>(M1)[c] = (float)(m1 - (double)w.c1 * (1. - (double)Sf));
-    reinterpret_cast<float*>(M2)[c] = (float)(m2 - (double)w.c2 * (double)Sf);
+    reinterpret_cast<float*>(M1)[c] = (float)(m1 - (double)rc.c1 * (1. - (double)Sf));
+    reinterpret_cast<float*>(M2)[c] = (float)(m2 - (double)rc.c2 * (double)Sf);
   } else if (mr == kMassDefectDF) {
-    const GbfDefectRow w = gbf_defect_row(m, j);
-    reinterpret_cast<float2*>(M1)[c] = gbf_df_from_double(m1 - (double)w.c1 * (1. - (double)Sf));
-    reinterpret_cast<float2*>(M2)[c] = gbf_df_from_double(m2 - (double)w.c2 * (double)Sf);
+    reinterpret_cast<float2*>(M1)[c] = gbf_df_from_double(m1 - (double)rc.c1 * (1. - (double)Sf));
+    reinterpret_cast<float2*>(M2)[c] = gbf_df_from_double(m2 - (double)rc.c2 * (double)Sf);
   } else if (mr == kMassDF) {
     reinterpret_cast<float2*>(M1)[c] = gbf_df_from_double(m1);
     reinterpret_cast<float2*>(M2)[c] = gbf_df_from_double(m2);
@@ -1268,6 +1272,10 @@ __device__ __forceinline__ void gbf_split_init_cell(const gbf_model& m, double p
     M1[c] = m1;
     M2[c] = m2;
   }
+}
+__device__ __forceinline__ void gbf_split_init_cell(const gbf_model& m, double p, double s, int j, float& dPf,
+                                                    float& Sf, double* M1, double* M2, size_t c, int mr) {
+  gbf_split_init_cell(m, p, s, gbf_row_const(m, j), dPf, Sf, M1, M2, c, mr);
 }
 
 // Value the reference's boundary sweep leaves in P1 (cpu.cpp:366-403), in
