@@ -564,14 +564,12 @@ def run_ours(args, rank, world):
             api = ("load_data_to_device(P1), load_data_to_device(S2), time_step_function's five calls, "
                    "load_data_to_host(P1), load_data_to_host(S2) (defines.h)")
         else:
-            def rt():
-                run.upload(0, hostP, hostS)
-                run.step(1)
-                run.download(0, "P1", hostP)
-                run.download(0, "S2", hostS)
+            def rt():  # one call: upload, the step and the download pipelined over slabs of planes
+                run.obj.advance_host(hostP, hostS, 1)
             run.download(0, "P1", hostP)
             run.download(0, "S2", hostS)
-            api = "gbf_domain_upload + gbf_domain_step(1) + gbf_domain_download(P1, S2)"
+            api = ("gbf_domain_advance_host(P, S, 1, P, S): P1, S2 host->device, one step, device->host, "
+                   "pipelined over slabs of planes (split forms without a Dirichlet patch; else the three calls)")
         for _ in range(max(1, args.warmup)):
             rt()
         torch.cuda.synchronize()

@@ -219,6 +219,19 @@ int gbf_domain_upload_device(gbf_domain* d, const double* P1_dev, const double* 
 int gbf_domain_step(gbf_domain* d, int nsteps);
 /* Copy one field (GBF_FIELD_*) of the current state to the host; synchronises. */
 int gbf_domain_download(gbf_domain* d, int field, double* host);
+/* Host-resident grid in one call: upload(P_in, S_in), `nsteps` steps,
+   download of P1 into P_out and S2 into S_out. For one step of a split-
+   precision grid without a Dirichlet patch, of 2M cells or more, it is
+   pipelined over slabs of planes (about 1M cells each, at most 16) on three
+   streams (host-to-device copies; conversion, the step's
+   chunk layer and the boundary rules of each slab; device-to-host copies),
+   so that the two copy directions overlap; otherwise the three calls in
+   turn. The outputs may alias the inputs. The state equals the three calls'
+   bit for bit; the step's phase masses (GBF_OUT_MASS) sum the same cells in
+   other partial blocks (within 1e-11 relative). Overlap needs page-locked
+   host arrays. Returns after the last copy. */
+int gbf_domain_advance_host(gbf_domain* d, const double* P_in, const double* S_in, int nsteps, double* P_out,
+                            double* S_out);
 /* Phase masses [step][2] recorded since the last upload (GBF_OUT_MASS). */
 int gbf_domain_mass_history(gbf_domain* d, double* host, int max_steps, int* nsteps_out);
 /* CFL numbers [step][2] (water, DNAPL) of the same steps (GBF_OUT_CFL): the

@@ -140,6 +140,7 @@ def _declare(lib) -> None:
         "gbf_domain_upload_device": (c_int, [c_void_p, c_void_p, c_void_p]),
         "gbf_domain_step": (c_int, [c_void_p, c_int]),
         "gbf_domain_download": (c_int, [c_void_p, c_int, c_void_p]),
+        "gbf_domain_advance_host": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_void_p]),
         "gbf_domain_mass_history": (c_int, [c_void_p, c_void_p, c_int, ctypes.POINTER(c_int)]),
         "gbf_domain_cfl_history": (c_int, [c_void_p, c_void_p, c_int, ctypes.POINTER(c_int)]),
         "gbf_ensemble_cfl_history": (c_int, [c_void_p, c_void_p, c_int, ctypes.POINTER(c_int)]),

@@ -64,6 +64,11 @@ int alloc_common(gbf_domain* d) {
 
 void free_all(gbf_domain* d) {
   gbf_timer_free(&d->timer);
+  for (cudaEvent_t e : d->pipe_ev) cudaEventDestroy(e);
+  d->pipe_ev.clear();
+  if (d->pipe_in) cudaStreamDestroy(d->pipe_in);
+  if (d->pipe_out) cudaStreamDestroy(d->pipe_out);
+  d->pipe_in = d->pipe_out = nullptr;
   for (void* p : d->owned) cudaFree(p);
   d->owned.clear();
   if (d->own_stream && d->stream) cudaStreamDestroy(d->stream);
@@ -260,6 +265,18 @@ int gbf_domain_upload(gbf_domain* d, const double* P1, const double* S2) {
   if (d->cfl_hist) GBF_CUDA(cudaMemsetAsync(d->cfl_hist, 0, 2 * sizeof(float) * (size_t)d->mass_cap, d->stream));
   GBF_CUDA(cudaMemsetAsync(d->status, 0, sizeof(unsigned), d->stream));
   return GBF_OK;
+}
+
+int gbf_domain_advance_host(gbf_domain* d, const double* P_in, const double* S_in, int nsteps, double* P_out,
+                            double* S_out) {
+  if (!d || !P_in || !S_in || !P_out || !S_out || nsteps < 0) return gbf_fail(GBF_ERR_ARG, "gbf_domain_advance_host");
+  if (d->borrowed) return gbf_fail(GBF_ERR_STATE, "gbf_domain_advance_host on a drop-in domain");
+  if (d->precision != GBF_PREC_F64 && nsteps == 1 && !d->split_patch && gbf_split_pipelined(d->m))
+    return gbf_split_advance_host(d, P_in, S_in, P_out, S_out);
+  if (int s = gbf_domain_upload(d, P_in, S_in)) return s;
+  if (int s = gbf_domain_step(d, nsteps)) return s;
+  if (int s = gbf_domain_download(d, GBF_FIELD_P1, P_out)) return s;
+  return gbf_domain_download(d, GBF_FIELD_S2, S_out);
 }
 
 int gbf_domain_step(gbf_domain* d, int nsteps) {

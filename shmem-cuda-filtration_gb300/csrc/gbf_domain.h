@@ -67,6 +67,11 @@ struct gbf_domain {
   double* split_partials = nullptr;
   float2* split_patch = nullptr;  // the Dirichlet patch's FP64 inflow (split forms; NULL without a patch)
   struct GbfRowConst* split_rows = nullptr;  // the split state conversions' row table (ny entries)
+  // host-resident pipeline of the split forms (gbf_domain_advance_host): copy
+  // streams, their events, an FP64 staging copy of (P, S) (allocated on first use)
+  cudaStream_t pipe_in = nullptr, pipe_out = nullptr;
+  std::vector<cudaEvent_t> pipe_ev;
+  double* pipe_stage = nullptr;
   double defect_k1v = 0.0;  // defect form: V sum of c1(j) phi over interior cells (gbf_defect_k1)
   void* tma = nullptr;  // device GbfTmaSet of the split state (NULL: plain loads)
   // mass tracking

@@ -115,14 +115,17 @@ constexpr int kPairTX = 64, kPairTY = 8;
 __host__ __device__ int tiles_x2(const GbfSplitConsts& C) { return (C.nx - 1 + kPairTX - 1) / kPairTX; }
 __host__ __device__ int tiles_y2(const GbfSplitConsts& C) { return (C.ny - 2 + kPairTY - 1) / kPairTY; }
 
-// The plain-load tile on one grid (grids without TMA staging).
+// The plain-load tile on one grid (grids without TMA staging). Block b runs
+// tile b mod (tiles of a chunk layer) of the k chunk kc0 + b / (tiles of a
+// layer), kchunk planes from 1 + kchunk kc; G.mass_partials is that launch's
+// first partial.
 template <int MR, bool CFL, bool PATCH>
 __global__ void __launch_bounds__(kSplitThreads, 4) k_split_step(const GbfSplitConsts C, const GbfSplitGrid G,
-                                                              const int kchunk) {
+                                                              const int kchunk, const int kc0) {
   __shared__ GbfSplitPlane pl[2];
   const int ntx = (C.nx - 2 + kSplitTX - 1) / kSplitTX, nty = (C.ny - 2 + kSplitTY - 1) / kSplitTY;
   const int b = blockIdx.x;
-  const int tx = b % ntx, ty = (b / ntx) % nty, kc = b / (ntx * nty);
+  const int tx = b % ntx, ty = (b / ntx) % nty, kc = kc0 + b / (ntx * nty);
   const int k0 = 1 + kc * kchunk;
   const int k1 = min(k0 + kchunk, C.nz - 1);
   GbfSplitAcc<MR> acc;
@@ -132,11 +135,13 @@ __global__ void __launch_bounds__(kSplitThreads, 4) k_split_step(const GbfSplitC
   if constexpr (CFL) split_block_cfl<kSplitThreads>(acc.cfl1, acc.cfl2, G.cfl_out);
 }
 
-// The x-pair tile on one grid: one tile (64 x 8 cells, a k range) per CTA.
+// The x-pair tile on one grid: one tile (64 x 8 cells, a k range) per CTA,
+// blocks mapped to tiles and k chunks as in k_split_step.
 template <int MR, bool CFL, bool PATCH>
 __global__ void __launch_bounds__(kPairTX / 2 * kPairTY, gbf_pair_ctas(MR)) k_split_step_x2(const GbfSplitConsts C,
                                                                          const GbfSplitGrid G, const int kchunk,
-                                                                         const GbfTmaSet* maps, int buf) {
+                                                                         const int kc0, const GbfTmaSet* maps,
+                                                                         int buf) {
   extern __shared__ __align__(128) unsigned char dyn[];
   using Cta = GbfPairCta<kPairTX, kPairTY, MR>;
   Cta& cta = *reinterpret_cast<Cta*>(dyn);
@@ -146,7 +151,7 @@ __global__ void __launch_bounds__(kPairTX / 2 * kPairTY, gbf_pair_ctas(MR)) k_sp
   }
   const int ntx = tiles_x2(C), nty = tiles_y2(C);
   const int b = blockIdx.x;
-  const int tx = b % ntx, ty = (b / ntx) % nty, kc = b / (ntx * nty);
+  const int tx = b % ntx, ty = (b / ntx) % nty, kc = kc0 + b / (ntx * nty);
   const int k0 = 1 + kc * kchunk;
   const int k1 = min(k0 + kchunk, C.nz - 1);
   if (threadIdx.x == 0) gbf_pair_bars_init(cta.bars);
@@ -164,11 +169,12 @@ __global__ void __launch_bounds__(kPairTX / 2 * kPairTY, gbf_pair_ctas(MR)) k_sp
 // Boundary cells [0, nb) of gbf_boundary_cell's enumeration (all, or all but
 // the x faces that the x-pair tile writes).
 __global__ void __launch_bounds__(kThreads) k_split_boundary(const gbf_model m, const GbfSplitGrid G, float H,
-                                                             size_t nb) {
+                                                             size_t nb, int k_lo, int k_hi) {
   const GbfGeo g = gbf_geo(m);
   for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < nb; t += (size_t)gridDim.x * blockDim.x) {
     int i, j, k;
     gbf_boundary_cell(g, t, i, j, k);
+    if (k < k_lo || k >= k_hi) continue;  // planes [k_lo, k_hi) only (a slab of the host pipeline)
     const size_t c = gbf_idx(g, i, j, k);
     G.Sn[c] = gbf_sweep_S<float>(m, g, G.Sn, G.S, i, j, k);
     G.dPn[c] = gbf_split_sweep_dP(m, g, G.dPn, G.dP, i, j, k, H);
@@ -220,9 +226,9 @@ __global__ void k_split_mass_tail(const double* partials, int nblocks, double* o
 // rows: the grid's row table (GbfRowConst), or NULL to form each row's
 // values per cell (the same values either way).
 __global__ void k_split_init(const gbf_model m, const GbfRowConst* rows, const double* P, const double* S,
-                             float* dPf, float* Sf, double* M1, double* M2, int mr) {
+                             float* dPf, float* Sf, double* M1, double* M2, int mr, size_t c0, size_t c1) {
   const GbfGeo g = gbf_geo(m);
-  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < g.n; c += (size_t)gridDim.x * blockDim.x) {
+  for (size_t c = c0 + blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < c1; c += (size_t)gridDim.x * blockDim.x) {
     const int j = (int)((c / g.nx) % g.ny);
     if (rows) gbf_split_init_cell(m, P[c], S[c], rows[j], dPf[c], Sf[c], M1, M2, c, mr);
     else gbf_split_init_cell(m, P[c], S[c], j, dPf[c], Sf[c], M1, M2, c, mr);
@@ -230,9 +236,9 @@ __global__ void k_split_init(const gbf_model m, const GbfRowConst* rows, const d
 }
 
 __global__ void k_split_to_f64(const gbf_model m, const GbfRowConst* rows, const float* dPf, const float* Sf,
-                               double* P, double* S) {
+                               double* P, double* S, size_t c0, size_t c1) {
   const GbfGeo g = gbf_geo(m);
-  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < g.n; c += (size_t)gridDim.x * blockDim.x) {
+  for (size_t c = c0 + blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < c1; c += (size_t)gridDim.x * blockDim.x) {
     const int j = (int)((c / g.nx) % g.ny);
     if (P) P[c] = (rows ? rows[j].phs : gbf_p_hydrostatic(m, j)) + (double)dPf[c];
     if (S) S[c] = (double)Sf[c];
@@ -281,14 +287,15 @@ int gbf_split_kchunk_x2(const GbfSplitConsts& C, int mr) {
                                 (long long)gbf_pair_ctas(mr) * gbf_num_sms());
 }
 
+// The step tiles of k chunks [kc0, kc0 + nkc) (kchunk planes each): the
+// x-pair tile with TMA staging (maps), else the plain-load tile.
 template <int MR, bool CFL, bool PATCH>
 int launch_x2(const GbfSplitConsts& C, const GbfSplitGrid& G, const GbfTmaSet* maps, int buf, cudaStream_t st,
-              unsigned& blocks) {
-  const int kchunk = gbf_split_kchunk_x2(C, MR);
-  blocks = (unsigned)(tiles_x2(C) * tiles_y2(C) * ((C.nz - 2 + kchunk - 1) / kchunk));
+              int kchunk, int kc0, int nkc) {
+  const unsigned blocks = (unsigned)(tiles_x2(C) * tiles_y2(C) * nkc);
   const int bytes = (int)sizeof(GbfPairCta<kPairTX, kPairTY, MR>);
   GBF_CUDA(cudaFuncSetAttribute(k_split_step_x2<MR, CFL, PATCH>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-  k_split_step_x2<MR, CFL, PATCH><<<blocks, kPairTX / 2 * kPairTY, bytes, st>>>(C, G, kchunk, maps, buf);
+  k_split_step_x2<MR, CFL, PATCH><<<blocks, kPairTX / 2 * kPairTY, bytes, st>>>(C, G, kchunk, kc0, maps, buf);
   return GBF_OK;
 }
 
@@ -303,46 +310,56 @@ __global__ void __launch_bounds__(kThreads) k_split_patch(const GbfSplitConsts C
 
 template <int MR, bool PATCH>
 int launch_tiles(const GbfSplitConsts& C, const GbfSplitGrid& G, const GbfTmaSet* maps, int buf, cudaStream_t st,
-                 unsigned& blocks, int kchunk) {
+                 int kchunk, int kc0, int nkc) {
   const bool cfl = G.cfl_out != nullptr;
   if (maps)
-    return cfl ? launch_x2<MR, true, PATCH>(C, G, maps, buf, st, blocks)
-               : launch_x2<MR, false, PATCH>(C, G, maps, buf, st, blocks);
-  if (cfl) k_split_step<MR, true, PATCH><<<blocks, kSplitThreads, 0, st>>>(C, G, kchunk);
-  else k_split_step<MR, false, PATCH><<<blocks, kSplitThreads, 0, st>>>(C, G, kchunk);
+    return cfl ? launch_x2<MR, true, PATCH>(C, G, maps, buf, st, kchunk, kc0, nkc)
+               : launch_x2<MR, false, PATCH>(C, G, maps, buf, st, kchunk, kc0, nkc);
+  const unsigned blocks = (unsigned)(tiles_x(C) * tiles_y(C) * nkc);
+  if (cfl) k_split_step<MR, true, PATCH><<<blocks, kSplitThreads, 0, st>>>(C, G, kchunk, kc0);
+  else k_split_step<MR, false, PATCH><<<blocks, kSplitThreads, 0, st>>>(C, G, kchunk, kc0);
   return GBF_OK;
 }
 
 // The tiles under a Dirichlet patch (G.patch_in set) are the PATCH instantiations.
-template <int MR>
-int launch_form(const GbfSplitConsts& C, const GbfSplitGrid& G, const GbfTmaSet* maps, int buf, cudaStream_t st,
-                unsigned& blocks, int kchunk) {
-  return G.patch_in ? launch_tiles<MR, true>(C, G, maps, buf, st, blocks, kchunk)
-                    : launch_tiles<MR, false>(C, G, maps, buf, st, blocks, kchunk);
+int launch_chunks(const GbfSplitConsts& C, const GbfSplitGrid& G, int mr, const GbfTmaSet* maps, int buf,
+                  cudaStream_t st, int kchunk, int kc0, int nkc) {
+  auto form = [&](auto tag) {
+    constexpr int MR = decltype(tag)::value;
+    return G.patch_in ? launch_tiles<MR, true>(C, G, maps, buf, st, kchunk, kc0, nkc)
+                      : launch_tiles<MR, false>(C, G, maps, buf, st, kchunk, kc0, nkc);
+  };
+  return mr == kMassDefect ? form(std::integral_constant<int, kMassDefect>{})
+         : mr == kMassDF   ? form(std::integral_constant<int, kMassDF>{})
+                           : form(std::integral_constant<int, kMassDefectDF>{});
+}
+// A step's k chunking: kchunk planes a chunk, and the tiles of a chunk layer.
+int step_kchunk(const GbfSplitConsts& C, int mr, const GbfTmaSet* maps) {
+  return maps ? gbf_split_kchunk_x2(C, mr) : gbf_split_kchunk(C);
+}
+long long layer_tiles(const GbfSplitConsts& C, const GbfTmaSet* maps) {
+  return maps ? (long long)tiles_x2(C) * tiles_y2(C) : (long long)tiles_x(C) * tiles_y(C);
 }
 
 int gbf_split_launch_domain(const gbf_model& m, const GbfSplitConsts& C, const GbfSplitGrid& G, int mr,
                             double* mass_out, cudaStream_t st, GbfTimer* tm, const GbfTmaSet* maps, int buf,
                             double k1v) {
-  const int kchunk = gbf_split_kchunk(C);
+  const int kchunk = step_kchunk(C, mr, maps);
   const int nkc = (C.nz - 2 + kchunk - 1) / kchunk;
-  unsigned blocks = (unsigned)(tiles_x(C) * tiles_y(C) * nkc);
+  const unsigned blocks = (unsigned)(layer_tiles(C, maps) * nkc);
   cudaEvent_t e = gbf_timer_begin(tm, st);
   if (G.patch_in) {  // the Dirichlet patch's FP64 inflow, timed with the step kernel
     const GbfPatchConsts P = gbf_patch_consts(m);
     k_split_patch<<<gbf_grid_for((size_t)P.n * P.n, kThreads), kThreads, 0, st>>>(C, P, G);
   }
   // TMA staging (maps): the x-pair tile; else the plain-load tile
-  const int s = mr == kMassDefect ? launch_form<kMassDefect>(C, G, maps, buf, st, blocks, kchunk)
-                : mr == kMassDF   ? launch_form<kMassDF>(C, G, maps, buf, st, blocks, kchunk)
-                                  : launch_form<kMassDefectDF>(C, G, maps, buf, st, blocks, kchunk);
-  if (s) return s;
+  if (int s = launch_chunks(C, G, mr, maps, buf, st, kchunk, 0, nkc)) return s;
   gbf_timer_end(tm, GBF_K_SPLIT_STEP, e, st);
   e = gbf_timer_begin(tm, st);
   // one cell per thread (row segments, as the ensembles' face pass walks
   // them, measured 8.6 -> 10.4 us on 256^3: too few warps for a latency-bound pass)
   const size_t nb = maps ? gbf_boundary_count_no_xfaces(gbf_geo(m)) : gbf_boundary_count(gbf_geo(m));
-  k_split_boundary<<<gbf_grid_for(nb, kThreads, 4), kThreads, 0, st>>>(m, G, C.H, nb);
+  k_split_boundary<<<gbf_grid_for(nb, kThreads, 4), kThreads, 0, st>>>(m, G, C.H, nb, 0, C.nz);
   gbf_timer_end(tm, GBF_K_SPLIT_BOUNDARY, e, st);
   if (G.mass_partials && mass_out) {
     e = gbf_timer_begin(tm, st);
@@ -354,12 +371,30 @@ int gbf_split_launch_domain(const gbf_model& m, const GbfSplitConsts& C, const G
 }
 
 // Mass-partial slots: the larger of the two tilings' CTA counts.
+// The host-resident pipeline's slabs (gbf_split_advance_host): one k chunk
+// layer of the step each, about 1M cells (16 MB each way) or more, so that a
+// slab's copies outlast its few launches, at most 16, at least 4 planes.
+constexpr long long kPipeSlabCells = 1ll << 20;
+int pipe_slabs(const GbfSplitConsts& C) {
+  const long long cells = (long long)C.nx * C.ny * C.nz;
+  return (int)std::min(16ll, std::max(1ll, cells / kPipeSlabCells));
+}
+int pipe_kchunk(const GbfSplitConsts& C) {
+  const int s = pipe_slabs(C);
+  return std::max(4, (C.nz - 2 + s - 1) / s);
+}
+bool gbf_split_pipelined(const gbf_model& m) {
+  const GbfSplitConsts C = gbf_split_consts(m);
+  return pipe_slabs(C) >= 2 && (C.nz - 2 + pipe_kchunk(C) - 1) / pipe_kchunk(C) >= 2;
+}
+
 unsigned gbf_split_blocks(const gbf_model& m, int mr) {
   const GbfSplitConsts C = gbf_split_consts(m);
-  const int kchunk = gbf_split_kchunk(C), kc2 = gbf_split_kchunk_x2(C, mr);
+  const int kchunk = gbf_split_kchunk(C), kc2 = gbf_split_kchunk_x2(C, mr), kp = pipe_kchunk(C);
   const unsigned a = (unsigned)(tiles_x(C) * tiles_y(C) * ((C.nz - 2 + kchunk - 1) / kchunk));
   const unsigned b = (unsigned)(tiles_x2(C) * tiles_y2(C) * ((C.nz - 2 + kc2 - 1) / kc2));
-  return a > b ? a : b;
+  const unsigned p = (unsigned)(std::max(tiles_x(C) * tiles_y(C), tiles_x2(C) * tiles_y2(C)) * ((C.nz - 2 + kp - 1) / kp));
+  return std::max(a, std::max(b, p));
 }
 
 // ----------------------------------------------------------------- host side
@@ -439,7 +474,7 @@ int gbf_split_fill_rows(const gbf_model& m, GbfRowConst* rows, cudaStream_t st) 
 int gbf_split_init_state(const gbf_model& m, const GbfRowConst* rows, const double* P_dev, const double* S_dev,
                          float* dPf, float* Sf, double* M1, double* M2, int mr, cudaStream_t st) {
   const size_t n = gbf_geo(m).n;
-  k_split_init<<<gbf_grid_for(n, kThreads, 4), kThreads, 0, st>>>(m, rows, P_dev, S_dev, dPf, Sf, M1, M2, mr);
+  k_split_init<<<gbf_grid_for(n, kThreads, 4), kThreads, 0, st>>>(m, rows, P_dev, S_dev, dPf, Sf, M1, M2, mr, 0, n);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? GBF_OK : gbf_cuda_check(e, "gbf_split_init_state");
 }
@@ -462,7 +497,7 @@ int gbf_split_upload(gbf_domain* d, const double* P1, const double* S2, cudaMemc
   }
   d->cur = 0;
   k_split_init<<<gbf_grid_for(n, kThreads, 4), kThreads, 0, d->stream>>>(
-      d->m, d->split_rows, P, S, d->Pf[0], d->Sf[0], d->M1, d->M2, gbf_mass_rep(d->precision));
+      d->m, d->split_rows, P, S, d->Pf[0], d->Sf[0], d->M1, d->M2, gbf_mass_rep(d->precision), 0, n);
   GBF_CUDA(cudaGetLastError());
   // the next-state buffer's faces are rewritten every step; start them equal
   GBF_CUDA(cudaMemcpyAsync(d->Pf[1], d->Pf[0], n * sizeof(float), cudaMemcpyDeviceToDevice, d->stream));
@@ -512,7 +547,7 @@ int gbf_split_download(gbf_domain* d, int field, double* host) {
   if (staged) GBF_CUDA(cudaMallocAsync((void**)&tmp, b, d->stream));
   k_split_to_f64<<<gbf_grid_for(n, kThreads, 4), kThreads, 0, d->stream>>>(
       d->m, d->split_rows, d->Pf[d->cur], d->Sf[d->cur], field == GBF_FIELD_P1 ? tmp : nullptr,
-      field == GBF_FIELD_S2 ? tmp : nullptr);
+      field == GBF_FIELD_S2 ? tmp : nullptr, 0, n);
   GBF_CUDA(cudaGetLastError());
   if (staged) {
     GBF_CUDA(cudaMemcpyAsync(host, tmp, b, cudaMemcpyDeviceToHost, d->stream));
@@ -524,8 +559,117 @@ int gbf_split_download(gbf_domain* d, int field, double* host) {
 
 int gbf_split_state_to_f64(const gbf_model& m, const GbfRowConst* rows, const float* dPf, const float* Sf, double* P,
                            double* S, cudaStream_t st) {
-  k_split_to_f64<<<gbf_grid_for(gbf_geo(m).n, kThreads, 4), kThreads, 0, st>>>(m, rows, dPf, Sf, P, S);
+  k_split_to_f64<<<gbf_grid_for(gbf_geo(m).n, kThreads, 4), kThreads, 0, st>>>(m, rows, dPf, Sf, P, S, 0,
+                                                                                gbf_geo(m).n);
   GBF_CUDA(cudaGetLastError());
+  return GBF_OK;
+}
+
+// One step of a grid from host FP64 arrays to host FP64 arrays, pipelined
+// over slabs of planes (one k chunk layer of the step each): the copy engines
+// move slab s + 1 in and slab s - 1 out while the compute stream converts slab
+// s, steps the chunk layer of slab s - 1 (its tiles read the first plane of
+// slab s), applies the boundary rules to its planes (they read nothing outside
+// the slab but the start-of-step state) and converts it back. The state equals
+// upload + step + download bit for bit; the phase masses sum the same cells in
+// other partial blocks (within 1e-11 relative). Grids without a Dirichlet patch.
+int gbf_split_advance_host(gbf_domain* d, const double* P_in, const double* S_in, double* P_out, double* S_out) {
+  const gbf_model& m = d->m;
+  const GbfGeo g = gbf_geo(m);
+  const size_t n = g.n, pl = g.pl;
+  const int mr = gbf_mass_rep(d->precision);
+  const GbfSplitConsts C = gbf_split_consts(m);
+  const GbfTmaSet* maps = (const GbfTmaSet*)d->tma;
+  const int kp = pipe_kchunk(C), ns = (C.nz - 2 + kp - 1) / kp;  // slabs = k chunks
+  auto pa = [&](int q) { return q == 0 ? 0 : 1 + q * kp; };
+  auto pb = [&](int q) { return q == ns - 1 ? C.nz : 1 + (q + 1) * kp; };
+  if (!d->pipe_in) {
+    GBF_CUDA(cudaStreamCreateWithFlags(&d->pipe_in, cudaStreamNonBlocking));
+    GBF_CUDA(cudaStreamCreateWithFlags(&d->pipe_out, cudaStreamNonBlocking));
+  }
+  while ((int)d->pipe_ev.size() < 2 + 2 * ns) {
+    cudaEvent_t e;
+    GBF_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    d->pipe_ev.push_back(e);
+  }
+  if (!d->pipe_stage && gbf_domain_alloc(d, (void**)&d->pipe_stage, 2 * sizeof(double) * n))
+    return gbf_fail(GBF_ERR_NOMEM, "gbf_domain_advance_host");
+  double *stP = d->pipe_stage, *stS = d->pipe_stage + n;
+  cudaStream_t cs = d->stream;
+  // the upload's resets (gbf_domain_upload), then everything on the stream so far first
+  d->cur = 0;
+  d->mass_count = 0;
+  d->steps = 0;
+  if (d->cfl_hist) GBF_CUDA(cudaMemsetAsync(d->cfl_hist, 0, 2 * sizeof(float) * (size_t)d->mass_cap, cs));
+  GBF_CUDA(cudaMemsetAsync(d->status, 0, sizeof(unsigned), cs));
+  GBF_CUDA(cudaEventRecord(d->pipe_ev[0], cs));
+  GBF_CUDA(cudaStreamWaitEvent(d->pipe_in, d->pipe_ev[0], 0));
+  GBF_CUDA(cudaStreamWaitEvent(d->pipe_out, d->pipe_ev[0], 0));
+  for (int q = 0; q < ns; q++) {  // host -> device, every slab in order
+    const size_t c0 = (size_t)pa(q) * pl, b = ((size_t)pb(q) * pl - c0) * sizeof(double);
+    GBF_CUDA(cudaMemcpyAsync(stP + c0, P_in + c0, b, cudaMemcpyDefault, d->pipe_in));
+    GBF_CUDA(cudaMemcpyAsync(stS + c0, S_in + c0, b, cudaMemcpyDefault, d->pipe_in));
+    GBF_CUDA(cudaEventRecord(d->pipe_ev[2 + q], d->pipe_in));
+  }
+  GbfSplitGrid G;
+  G.dP = d->Pf[0];
+  G.S = d->Sf[0];
+  G.dPn = d->Pf[1];
+  G.Sn = d->Sf[1];
+  G.K = d->cells.K;
+  G.phi = d->cells.phi;
+  G.media = d->cells.media;
+  G.M1 = d->M1;
+  G.M2 = d->M2;
+  G.mass_partials = nullptr;
+  G.status = d->status;
+  G.cfl_out = nullptr;
+  G.patch_in = nullptr;
+  double* mass_out = nullptr;
+  if ((d->out_flags & GBF_OUT_MASS) && d->mass_hist && d->mass_cap > 0) {
+    G.mass_partials = d->split_partials;
+    mass_out = d->mass_hist;
+    if ((d->out_flags & GBF_OUT_CFL) && d->cfl_hist) G.cfl_out = d->cfl_hist;
+    d->mass_count = 1;
+  }
+  const long long tiles = layer_tiles(C, maps);
+  const size_t nb = maps ? gbf_boundary_count_no_xfaces(g) : gbf_boundary_count(g);
+  for (int q = 0; q <= ns; q++) {
+    if (q < ns) {  // slab q in: FP64 -> split state, both buffers
+      const size_t c0 = (size_t)pa(q) * pl, c1 = (size_t)pb(q) * pl;
+      GBF_CUDA(cudaStreamWaitEvent(cs, d->pipe_ev[2 + q], 0));
+      k_split_init<<<gbf_grid_for(c1 - c0, kThreads, 4), kThreads, 0, cs>>>(m, d->split_rows, stP, stS, d->Pf[0],
+                                                                          d->Sf[0], d->M1, d->M2, mr, c0, c1);
+      GBF_CUDA(cudaMemcpyAsync(d->Pf[1] + c0, d->Pf[0] + c0, (c1 - c0) * sizeof(float), cudaMemcpyDeviceToDevice, cs));
+      GBF_CUDA(cudaMemcpyAsync(d->Sf[1] + c0, d->Sf[0] + c0, (c1 - c0) * sizeof(float), cudaMemcpyDeviceToDevice, cs));
+    }
+    if (q > 0) {  // slab q - 1: its chunk layer of the step, its boundary cells, out
+      const int r = q - 1;
+      const size_t c0 = (size_t)pa(r) * pl, c1 = (size_t)pb(r) * pl;
+      GbfSplitGrid Gr = G;
+      if (Gr.mass_partials) Gr.mass_partials += 2 * (size_t)tiles * r;
+      if (int s = launch_chunks(C, Gr, mr, maps, 0, cs, kp, r, 1)) return s;
+      k_split_boundary<<<gbf_grid_for(nb, kThreads, 4), kThreads, 0, cs>>>(m, G, C.H, nb, pa(r), pb(r));
+      k_split_to_f64<<<gbf_grid_for(c1 - c0, kThreads, 4), kThreads, 0, cs>>>(m, d->split_rows, d->Pf[1], d->Sf[1],
+                                                                            stP, stS, c0, c1);
+      GBF_CUDA(cudaGetLastError());
+      GBF_CUDA(cudaEventRecord(d->pipe_ev[2 + ns + r], cs));
+      GBF_CUDA(cudaStreamWaitEvent(d->pipe_out, d->pipe_ev[2 + ns + r], 0));
+      const size_t b = (c1 - c0) * sizeof(double);
+      GBF_CUDA(cudaMemcpyAsync(P_out + c0, stP + c0, b, cudaMemcpyDefault, d->pipe_out));
+      GBF_CUDA(cudaMemcpyAsync(S_out + c0, stS + c0, b, cudaMemcpyDefault, d->pipe_out));
+    }
+  }
+  if (mass_out)
+    k_split_mass_tail<<<1, 256, 0, cs>>>(G.mass_partials, (int)(tiles * ns), mass_out,
+                                         gbf_is_defect(mr) ? d->defect_k1v : 0.0);
+  GBF_CUDA(cudaGetLastError());
+  GBF_CUDA(cudaEventRecord(d->pipe_ev[1], d->pipe_out));
+  GBF_CUDA(cudaStreamWaitEvent(cs, d->pipe_ev[1], 0));
+  d->cur = 1;
+  d->steps = 1;
+  d->uploaded = true;
+  GBF_CUDA(cudaStreamSynchronize(cs));
   return GBF_OK;
 }
 

@@ -98,6 +98,11 @@ int gbf_split_upload(gbf_domain* d, const double* P1, const double* S2, cudaMemc
 int gbf_split_step(gbf_domain* d);
 int gbf_split_download(gbf_domain* d, int field, double* host);
 int gbf_split_launches_per_step(gbf_domain* d);
+// upload + one step + download from and to host FP64 arrays, pipelined over
+// slabs of planes (gbf_domain_advance_host; grids without a Dirichlet patch,
+// large enough for two slabs of about 1M cells: gbf_split_pipelined).
+int gbf_split_advance_host(gbf_domain* d, const double* P_in, const double* S_in, double* P_out, double* S_out);
+bool gbf_split_pipelined(const gbf_model& m);
 // FP64 (P, S) of every cell from a split state (device arrays; either output
 // may be NULL; rows: the grid's row table, or NULL to form each row's values
 // per cell).

@@ -69,6 +69,19 @@ class Domain:
     def status(self) -> int:
         return self.lib.gbf_domain_status(self.h)
 
+    def advance_host(self, P_in: np.ndarray, S_in: np.ndarray, nsteps: int,
+                     P_out: np.ndarray | None = None, S_out: np.ndarray | None = None):
+        """upload + nsteps steps + download of P1 and S2 in one call, pipelined
+        over slabs of planes for one split-form step (outputs default to the
+        inputs, updated in place)."""
+        P_out = P_in if P_out is None else P_out
+        S_out = S_in if S_out is None else S_out
+        for a in (P_in, S_in, P_out, S_out):
+            assert a.dtype == np.float64 and a.size == self.model.nx * self.model.ny * self.model.nz
+            assert a.flags.c_contiguous
+        abi.check(self.lib.gbf_domain_advance_host(self.h, P_in.ctypes.data, S_in.ctypes.data, nsteps,
+                                                   P_out.ctypes.data, S_out.ctypes.data), "advance_host")
+
     def download(self, field: str, out: np.ndarray | None = None) -> np.ndarray:
         if out is None:
             out = np.empty(self.model.shape, np.float64)
