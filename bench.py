@@ -432,33 +432,42 @@ def step_budget(args):
 
 # ------------------------------------------------------------------- our arm
 
-def link_bandwidth(torch, nbytes=1 << 30):
-    """Pinned host <-> device copy rates (GB/s), each direction alone and both at once."""
+def link_bandwidth(torch, nbytes=1 << 30, reps=3):
+    """Pinned host <-> device copy rates (GB/s), each direction alone and both
+    at once: the best of `reps` timed copies after one untimed round of each
+    (the first use of a stream or buffer carries one-off costs)."""
     h = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
     h2 = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
     d = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
     d2 = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
     s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
-    for _ in range(2):
+
+    def h2d():
         d.copy_(h, non_blocking=True)
+
+    def d2h():
         h.copy_(d, non_blocking=True)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    d.copy_(h, non_blocking=True)
-    torch.cuda.synchronize()
-    t1 = time.perf_counter()
-    h.copy_(d, non_blocking=True)
-    torch.cuda.synchronize()
-    t2 = time.perf_counter()
-    with torch.cuda.stream(s1):
-        d.copy_(h, non_blocking=True)
-    with torch.cuda.stream(s2):
-        h2.copy_(d2, non_blocking=True)
-    torch.cuda.synchronize()
-    t3 = time.perf_counter()
+
+    def both():
+        with torch.cuda.stream(s1):
+            d.copy_(h, non_blocking=True)
+        with torch.cuda.stream(s2):
+            h2.copy_(d2, non_blocking=True)
+
+    best = {}
+    for name, f in (("h2d", h2d), ("d2h", d2h), ("both", both)):
+        f()
+        torch.cuda.synchronize()
+        t = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            f()
+            torch.cuda.synchronize()
+            t.append(time.perf_counter() - t0)
+        best[name] = min(t)
     del h, h2, d, d2
-    return {"h2d_gbs": nbytes / (t1 - t0) / 1e9, "d2h_gbs": nbytes / (t2 - t1) / 1e9,
-            "both_gbs": 2 * nbytes / (t3 - t2) / 1e9}
+    return {"h2d_gbs": nbytes / best["h2d"] / 1e9, "d2h_gbs": nbytes / best["d2h"] / 1e9,
+            "both_gbs": 2 * nbytes / best["both"] / 1e9}
 
 
 def run_ours(args, rank, world):
