@@ -64,14 +64,19 @@ extern "C" {
 /* 0 = eager (one kernel per reference function, reference intermediate
    arrays written by every call; the default), 1 = fused (the five calls of a
    step are deferred and run as one fused FP64 step at boundary_conditions;
-   intermediate arrays are materialised on demand by load_data_to_host). A
-   process starts in mode 1 when its environment holds GBF_DROPIN_MODE=1, so
-   that a driver which cannot call this function (the reference's main.cpp)
-   can select it. */
+   intermediate arrays are materialised on demand by load_data_to_host),
+   2 = split (as 1, with the step in the headline split form: FP32 state and
+   fluxes, FP64-precision masses and one residual-correction Newton step per
+   cell, kept beside the caller's arrays; P1 and S2 are written back when the
+   host reads them; results within the split form's bars, max|dS| <= 1e-5 and
+   rel-L2(P) <= 1e-6, of the reference arithmetic). A process starts in mode
+   1 or 2 when its environment holds GBF_DROPIN_MODE=1 or 2, so that a driver
+   which cannot call this function (the reference's main.cpp) can select it.
+   Changing the mode brings every caller array up to date first. */
 int gbf_dropin_set_mode(int mode);
 int gbf_dropin_get_mode(void);
 /* The gbflow domain behind arrays from device_memory_alloc (keyed by their
-   device P1 pointer) in fused mode, once the first step created it; NULL
+   device P1 pointer) in fused or split mode, once the first step created it; NULL
    otherwise. It accepts the gbf_domain_* timing and status calls of
    gbflow.h (gbf_domain_set_timing, gbf_domain_kernel_times,
    gbf_domain_status); the drop-in owns it and frees it in

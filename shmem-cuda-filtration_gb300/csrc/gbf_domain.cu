@@ -473,12 +473,13 @@ int gbf_domain_mass_history(gbf_domain* d, double* host, int max_steps, int* nst
 
 // ------------------------------------------------------------------ drop-in
 
-int gbf_domain_attach_dropin(const gbf_model* m, gbf_arrays caller, gbf_cells cells, gbf_domain** out) {
+int gbf_domain_attach_dropin(const gbf_model* m, gbf_arrays caller, gbf_cells cells, int precision, gbf_domain** out) {
   *out = nullptr;
   if (int s = gbf_model_validate(m, nullptr, 0)) return s;
   gbf_domain* d = new gbf_domain();
   d->m = *m;
   d->d = gbf_derive(*m);
+  d->precision = precision;
   d->borrowed = true;
   d->caller = caller;
   d->cells = cells;
@@ -490,7 +491,7 @@ int gbf_domain_attach_dropin(const gbf_model* m, gbf_arrays caller, gbf_cells ce
   d->S[0] = caller.S2;
   if (!s) s |= gbf_domain_alloc(d, (void**)&d->P[1], n * sizeof(double));
   if (!s) s |= gbf_domain_alloc(d, (void**)&d->S[1], n * sizeof(double));
-  if (!s) s = alloc_f64_work(d);
+  if (!s) s = precision == GBF_PREC_F64 ? alloc_f64_work(d) : gbf_split_alloc(d);
   if (!s) s = gbf_domain_alloc(d, (void**)&d->bscratch, gbf_boundary_scratch_doubles(m) * sizeof(double));
   if (s) {
     free_all(d);
@@ -513,6 +514,11 @@ int gbf_dropin_materialize(gbf_domain* d) {
   gbf_arrays a = d->caller;
   a.P1 = d->P[1];
   a.S2 = d->S[1];
+  if (d->precision != GBF_PREC_F64) {  // split mode: the step-start state is the other split buffer
+    if (int s = gbf_split_state_to_f64(d->m, d->split_rows, d->Pf[d->cur ^ 1], d->Sf[d->cur ^ 1], d->P[1], d->S[1],
+                                       d->stream))
+      return s;
+  }
   int s = gbf_props_f64(&d->m, a, d->cells, nullptr);
   s |= gbf_velocity_f64(&d->m, a, nullptr);
   s |= gbf_mass_f64(&d->m, a, d->cells, nullptr);
@@ -536,12 +542,25 @@ void gbf_domain_detach_dropin(gbf_domain* d) {
   delete d;
 }
 
+int gbf_dropin_writeback(gbf_domain* d) {
+  if (!d || !d->caller_stale) return GBF_OK;
+  d->caller_stale = false;
+  return gbf_split_state_to_f64(d->m, d->split_rows, d->Pf[d->cur], d->Sf[d->cur], d->caller.P1, d->caller.S2,
+                                d->stream);
+}
+
+void gbf_dropin_host_wrote(gbf_domain* d, const double* dev) {
+  if (d && d->precision != GBF_PREC_F64 && (dev == d->caller.P1 || dev == d->caller.S2)) d->split_stale = true;
+}
+
 // Run the pending stages (bitmask of stages 1..4) one kernel each, in order.
 int gbf_dropin_flush(gbf_domain* d) {
   if (!d || !d->pending) return GBF_OK;
   const gbf_arrays a = d->caller;
   // the arrays these stages do not rewrite keep the last fused step's values
   int s = gbf_dropin_materialize(d);
+  s |= gbf_dropin_writeback(d);  // split mode: the stages run on the caller's P1, S2
+  if (d->precision != GBF_PREC_F64 && (d->pending & 8)) d->split_stale = true;  // the Newton rewrites them
   if (d->pending & 1) s |= gbf_props_f64(&d->m, a, d->cells, nullptr);
   if (d->pending & 2) s |= gbf_velocity_f64(&d->m, a, nullptr);
   if (d->pending & 4) s |= gbf_mass_f64(&d->m, a, d->cells, nullptr);
@@ -558,6 +577,8 @@ int gbf_dropin_defer(gbf_domain* d, const gbf_model& m, int stage) {
     if (int s = gbf_dropin_flush(d)) return s;
     d->m = m;
     d->d = gbf_derive(m);
+    if (d->precision != GBF_PREC_F64)  // split mode: its row constants, and the state formed anew
+      if (int s = gbf_split_fill_rows(d->m, d->split_rows, d->stream)) return s;
   }
   const int prefix = (1 << (stage - 1)) - 1;
   if (stage <= 4) {
@@ -571,9 +592,22 @@ int gbf_dropin_defer(gbf_domain* d, const gbf_model& m, int stage) {
   }
   if (d->pending == 15) {  // the whole step: fused (its derived arrays are left to materialise on demand)
     d->pending = 0;
-    return f64_step(d, 0);
+    if (d->precision == GBF_PREC_F64) return f64_step(d, 0);
+    // split mode: the split state from the caller's arrays when they were
+    // written since, one split step (the caller's P1, S2 are written back
+    // when read)
+    if (d->split_stale) {
+      if (int s = gbf_split_upload(d, d->caller.P1, d->caller.S2, cudaMemcpyDeviceToDevice)) return s;
+      d->split_stale = false;
+    }
+    if (int s = gbf_split_step(d)) return s;
+    d->caller_stale = true;
+    d->lazy_dirty = true;
+    return GBF_OK;
   }
   int s = gbf_dropin_flush(d);
   if (!s) s = gbf_dropin_materialize(d);
+  if (!s) s = gbf_dropin_writeback(d);
+  if (d->precision != GBF_PREC_F64) d->split_stale = true;  // the boundary rules rewrite P1, S2
   return s | gbf_boundary_f64(&d->m, d->caller, d->bscratch, nullptr);
 }

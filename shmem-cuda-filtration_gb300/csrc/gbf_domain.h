@@ -89,6 +89,11 @@ struct gbf_domain {
   int pending = 0;
   double* bscratch = nullptr;  // boundary gather scratch of the one-kernel-per-stage fallback
   bool lazy_dirty = false;     // drop-in: derived arrays not yet materialised for the last fused step
+  // drop-in split mode (a split-precision domain behind the caller's FP64
+  // arrays): split_stale, the caller's P1/S2 were written since the split
+  // state was formed from them; caller_stale, the split state is ahead of the
+  // caller's P1/S2 (written back when the host reads them)
+  bool split_stale = true, caller_stale = false;
   std::vector<void*> owned;  // every cudaMalloc of this domain
   GbfTimer timer;
 };
@@ -101,9 +106,15 @@ int gbf_roS_old_launch(const gbf_model& m, const double* P, const double* S, con
                        double* o1, double* o2, cudaStream_t st);
 
 // Drop-in helpers (gbf_domain.cu).
-int gbf_domain_attach_dropin(const gbf_model* m, gbf_arrays caller, gbf_cells cells, gbf_domain** out);
+// precision: GBF_PREC_F64 (the fused mode) or a split form (the split mode).
+int gbf_domain_attach_dropin(const gbf_model* m, gbf_arrays caller, gbf_cells cells, int precision, gbf_domain** out);
 int gbf_dropin_defer(gbf_domain* d, const gbf_model& m, int stage);
 int gbf_dropin_flush(gbf_domain* d);
 void gbf_domain_detach_dropin(gbf_domain* d);
 int gbf_dropin_materialize(gbf_domain* d);
 bool gbf_dropin_is_derived(const gbf_domain* d, const double* p);
+// Split mode: the caller's P1 and S2 from the split state when it is ahead of
+// them (before the host reads them or an eager stage runs on them), and the
+// note that the host wrote one of them (the split state is formed anew).
+int gbf_dropin_writeback(gbf_domain* d);
+void gbf_dropin_host_wrote(gbf_domain* d, const double* dev);

@@ -12,6 +12,14 @@
 //   * errors are printed like checkErrors (gpu.cu:7-27) and also kept as a
 //     sticky status readable through gbf_last_status();
 //   * single domain only (size == 1, the no_communication path);
+//   * split mode (gbf_dropin_set_mode(2)) is the fused mode in the headline
+//     split form: the step runs on an FP32 state with FP64-precision masses
+//     (GBF_PREC_SPLIT) kept beside the caller's arrays, formed anew from the
+//     caller's P1 and S2 whenever the host wrote them; P1 and S2 are written
+//     back, and the derived arrays formed as in the fused mode from the state
+//     the step started from, when the host reads them. Its results are the
+//     split form's (max|dS| <= 1e-5, rel-L2(P) <= 1e-6 against the reference
+//     arithmetic), not the reference's to round-off;
 //   * fused mode (gbf_dropin_set_mode(1)) runs time_step_function's five
 //     calls as one fused step that writes P1, S2, ro1, ro2 only; the other
 //     arrays of the step (P2, Xi, velocities, roS, roS_old) are computed when
@@ -42,12 +50,13 @@ struct DropinDomain {
 
 std::mutex g_mu;
 std::unordered_map<const double*, DropinDomain> g_domains;
-// The mode a process starts in: GBF_DROPIN_MODE=1 in the environment selects
-// the fused mode for drivers that cannot call gbf_dropin_set_mode (the
+// The mode a process starts in: GBF_DROPIN_MODE=1 (fused) or 2 (split) in the
+// environment, for drivers that cannot call gbf_dropin_set_mode (the
 // reference's own main.cpp); anything else, or nothing, the eager mode.
 int initial_mode() {
   const char* e = getenv("GBF_DROPIN_MODE");
-  return (e && e[0] == '1' && e[1] == '\0') ? 1 : 0;
+  if (!e || e[1] != '\0') return 0;
+  return e[0] == '1' ? 1 : e[0] == '2' ? 2 : 0;
 }
 int g_mode = initial_mode();
 constexpr double kFusedNewtonTol = 1e-11;  // converge-and-exit Newton of the fused mode
@@ -55,7 +64,7 @@ constexpr double kFusedNewtonTol = 1e-11;  // converge-and-exit Newton of the fu
 gbf_model model_from(const consts& def, int localNx) {
   gbf_model m;
   gbf_model_reference(&m, localNx, def.Ny, def.Nz, def.dt);
-  if (g_mode == 1) m.newton_tol = kFusedNewtonTol;
+  if (g_mode != 0) m.newton_tol = kFusedNewtonTol;
   for (int md = 0; md < 2; md++) {
     m.K[md] = def.K[md];
     m.lambda[md] = def.lambda[md];
@@ -105,23 +114,54 @@ DropinDomain* find_domain(const double* P1) {
 gbf_domain* fused_of(const ptr_Arrays& D, const gbf_model& m) {
   DropinDomain* dd = find_domain(D.P1);
   if (!dd) {
-    gbf_fail(GBF_ERR_STATE, "fused mode needs arrays from device_memory_alloc");
+    gbf_fail(GBF_ERR_STATE, "fused and split modes need arrays from device_memory_alloc");
     return nullptr;
   }
   if (!dd->fused) {
-    if (gbf_domain_attach_dropin(&m, arrays_from(D), cells_from(D), &dd->fused) != GBF_OK) return nullptr;
+    const int precision = g_mode == 2 ? GBF_PREC_SPLIT : GBF_PREC_F64;
+    if (gbf_domain_attach_dropin(&m, arrays_from(D), cells_from(D), precision, &dd->fused) != GBF_OK) return nullptr;
   }
   return dd->fused;
 }
 
-// Any host access observes completed stages: run what is deferred, and
-// materialise the derived arrays of a fused step when `dev` is one of them.
+// Any host access observes completed stages: run what is deferred, bring the
+// caller's P1 and S2 up to the split state when `dev` is one of them, and
+// materialise the derived arrays of a fused step when `dev` is one of those.
 void flush_all(const double* dev = nullptr) {
   std::lock_guard<std::mutex> lk(g_mu);
   for (auto& kv : g_domains)
     if (gbf_domain* f = kv.second.fused) {
       gbf_dropin_flush(f);
+      if (dev && (dev == f->caller.P1 || dev == f->caller.S2)) gbf_dropin_writeback(f);
       if (dev && gbf_dropin_is_derived(f, dev)) gbf_dropin_materialize(f);
+    }
+}
+
+// The host writes `dev`: the caller's arrays current first (the host may
+// overwrite one of P1, S2 and keep the other), then the note of the write.
+void before_host_write(const double* dev) {
+  flush_all(dev);
+  std::lock_guard<std::mutex> lk(g_mu);
+  for (auto& kv : g_domains)
+    if (gbf_domain* f = kv.second.fused) gbf_dropin_writeback(f);
+}
+void after_host_write(const double* dev) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  for (auto& kv : g_domains)
+    if (gbf_domain* f = kv.second.fused) gbf_dropin_host_wrote(f, dev);
+}
+
+// Every caller array current, and the fused or split domains released (a mode
+// change; they are created again on first use in the new mode).
+void settle_all() {
+  std::lock_guard<std::mutex> lk(g_mu);
+  for (auto& kv : g_domains)
+    if (gbf_domain* f = kv.second.fused) {
+      gbf_dropin_flush(f);
+      gbf_dropin_materialize(f);
+      gbf_dropin_writeback(f);
+      gbf_domain_detach_dropin(f);
+      kv.second.fused = nullptr;
     }
 }
 
@@ -134,7 +174,7 @@ void ro_P2_Xi_calculation(ptr_Arrays HostArraysPtr, ptr_Arrays DevArraysPtr, con
   (void)HostArraysPtr; (void)rank; (void)blocksX; (void)blocksY; (void)blocksZ;
   if (!single_domain(size, "ro_P2_Xi_calculation")) return;
   gbf_model m = model_from(def, localNx);
-  if (g_mode == 1) {
+  if (g_mode != 0) {
     if (gbf_domain* f = fused_of(DevArraysPtr, m)) gbf_dropin_defer(f, m, 1);
     return;
   }
@@ -146,7 +186,7 @@ void u_calculation(ptr_Arrays HostArraysPtr, ptr_Arrays DevArraysPtr, int localN
   (void)HostArraysPtr; (void)rank; (void)blocksX; (void)blocksY; (void)blocksZ;
   if (!single_domain(size, "u_calculation")) return;
   gbf_model m = model_from(def, localNx);
-  if (g_mode == 1) {
+  if (g_mode != 0) {
     if (gbf_domain* f = fused_of(DevArraysPtr, m)) gbf_dropin_defer(f, m, 2);
     return;
   }
@@ -158,7 +198,7 @@ void roS_calculation(ptr_Arrays HostArraysPtr, ptr_Arrays DevArraysPtr, consts d
   (void)HostArraysPtr; (void)t; (void)rank; (void)blocksX; (void)blocksY; (void)blocksZ;
   if (!single_domain(size, "roS_calculation")) return;
   gbf_model m = model_from(def, localNx);
-  if (g_mode == 1) {
+  if (g_mode != 0) {
     if (gbf_domain* f = fused_of(DevArraysPtr, m)) gbf_dropin_defer(f, m, 3);
     return;
   }
@@ -170,7 +210,7 @@ void P1_S2_calculation(ptr_Arrays HostArraysPtr, ptr_Arrays DevArraysPtr, consts
   (void)HostArraysPtr; (void)rank; (void)blocksX; (void)blocksY; (void)blocksZ;
   if (!single_domain(size, "P1_S2_calculation")) return;
   gbf_model m = model_from(def, localNx);
-  if (g_mode == 1) {
+  if (g_mode != 0) {
     if (gbf_domain* f = fused_of(DevArraysPtr, m)) gbf_dropin_defer(f, m, 4);
     return;
   }
@@ -182,7 +222,7 @@ void boundary_conditions(ptr_Arrays HostArraysPtr, ptr_Arrays DevArraysPtr, int 
   (void)HostArraysPtr; (void)rank; (void)blocksX; (void)blocksY; (void)blocksZ;
   if (!single_domain(size, "boundary_conditions")) return;
   gbf_model m = model_from(def, localNx);
-  if (g_mode == 1) {
+  if (g_mode != 0) {
     if (gbf_domain* f = fused_of(DevArraysPtr, m)) gbf_dropin_defer(f, m, 5);
     return;
   }
@@ -201,14 +241,15 @@ void boundary_conditions(ptr_Arrays HostArraysPtr, ptr_Arrays DevArraysPtr, int 
 
 void load_data_to_host(double* HostArrayPtr, double* DevArrayPtr, int localNx, consts def) {
   size_t n = (size_t)localNx * def.Ny * def.Nz;
-  if (g_mode == 1) flush_all(DevArrayPtr);
+  if (g_mode != 0) flush_all(DevArrayPtr);
   gbf_cuda_check(cudaMemcpy(HostArrayPtr, DevArrayPtr, n * sizeof(double), cudaMemcpyDeviceToHost), "copy data to host");
 }
 
 void load_data_to_device(double* HostArrayPtr, double* DevArrayPtr, int localNx, consts def) {
   size_t n = (size_t)localNx * def.Ny * def.Nz;
-  if (g_mode == 1) flush_all(DevArrayPtr);  // the other derived arrays keep their values
+  if (g_mode != 0) before_host_write(DevArrayPtr);  // the other derived arrays keep their values
   gbf_cuda_check(cudaMemcpy(DevArrayPtr, HostArrayPtr, n * sizeof(double), cudaMemcpyHostToDevice), "copy double data to device");
+  if (g_mode != 0) after_host_write(DevArrayPtr);
 }
 
 void load_data_to_device_int(int* HostArrayPtr, int* DevArrayPtr, int localNx, consts def) {
@@ -322,7 +363,8 @@ void save_exchange_data(double* HostArrayPtr, double* DevArrayPtr, double* HostB
 
 extern "C" {
 int gbf_dropin_set_mode(int mode) {
-  if (mode != 0 && mode != 1) return gbf_fail(GBF_ERR_ARG, "gbf_dropin_set_mode");
+  if (mode != 0 && mode != 1 && mode != 2) return gbf_fail(GBF_ERR_ARG, "gbf_dropin_set_mode");
+  if (mode != g_mode) settle_all();
   g_mode = mode;
   return GBF_OK;
 }

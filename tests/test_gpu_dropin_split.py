@@ -1,0 +1,121 @@
+"""The drop-in's split mode (gbf_dropin_set_mode(2), GBF_DROPIN_MODE=2): the
+reference's defines.h calls, time_step_function's five per step, run the
+headline split form (FP32 state and fluxes, FP64-precision masses, one
+residual-correction Newton step per cell) beside the caller's FP64 arrays.
+Against the oracle (the reference's cpu.cpp arithmetic) on a reference grid
+with its Dirichlet patch and the reference parameter file's physics, at the
+split form's bars: max|dS| <= 1e-5, rel-L2(P) <= 1e-6; the derived arrays
+the host reads (P2, ro1, ro2, from the state the last step started from)
+as well. Also: P1 and S2 written by the host in the middle of a run (the
+split state is formed anew from them), and a change to the eager mode in the
+middle of a run (the caller's arrays are brought up to date first).
+"""
+import ctypes
+from importlib import import_module
+
+import numpy as np
+import pytest
+
+from gpu_util import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+SHAPE = (48, 40, 44)
+DT = 0.02
+DS_TOL, P_TOL = 1e-5, 1e-6
+
+
+@pytest.fixture
+def dropin(pkg, gpu_lib):
+    dp = import_module(pkg.__name__ + ".dropin")
+    di = dp.DropIn()
+    yield dp, di
+    di.set_mode(0)
+
+
+def oracle_states(abi, O, steps):
+    """The oracle from initial_data: the state after each of `steps` (dict of copies)."""
+    m = abi.reference_model(*SHAPE, DT)
+    st = O.State(m)
+    orc = O.Oracle(abi)
+    orc.initial(st)
+    out = {0: st.copy()}
+    for s in steps:
+        orc.step(st, s - max(out))
+        out[s] = st.copy()
+    return m, out
+
+
+class Run:
+    """Arrays from device_memory_alloc, the oracle's initial state loaded."""
+
+    def __init__(self, dp, di, m, st0):
+        self.dp, self.di, self.m = dp, di, m
+        self.c = dp.consts_from_model(m)
+        self.H, self.D = dp.PtrArrays(), dp.PtrArrays()
+        self.buf = ctypes.c_void_p()
+        di.f["device_memory_alloc"](ctypes.byref(self.D), ctypes.byref(self.buf), m.nx, self.c)
+        self.put("P1", st0["P1"])
+        self.put("S2", st0["S2"])
+        self.t = 0
+
+    def put(self, name, a):
+        a = np.ascontiguousarray(a, np.float64)
+        self.di.f["load_data_to_device"](a.ctypes.data, getattr(self.D, name), self.m.nx, self.c)
+
+    def get(self, name):
+        out = np.empty(self.m.shape, np.float64)
+        self.di.f["load_data_to_host"](out.ctypes.data, getattr(self.D, name), self.m.nx, self.c)
+        return out
+
+    def steps(self, n):
+        for _ in range(n):
+            self.t += 1
+            self.di.time_step(self.H, self.D, self.c, self.t * self.m.dt)
+
+    def close(self):
+        self.di.f["device_memory_free"](self.D, self.buf)
+
+
+def check(tag, run, st, derived=False):
+    P, S = run.get("P1"), run.get("S2")
+    ds, pl2 = float(np.abs(S - st["S2"]).max()), rel_l2(P, st["P1"])
+    line = f"{tag}: max|dS| {ds:.2e}, rel-L2(P) {pl2:.2e}"
+    assert ds <= DS_TOL and pl2 <= P_TOL, line
+    if derived:
+        P2, r1, r2 = rel_l2(run.get("P2"), st["P2"]), rel_l2(run.get("ro1"), st["ro1"]), rel_l2(run.get("ro2"), st["ro2"])
+        line += f", P2 {P2:.2e}, ro1 {r1:.2e}, ro2 {r2:.2e}"
+        assert P2 <= P_TOL and r1 <= P_TOL and r2 <= P_TOL, line
+    print("\n" + line)
+
+
+def test_split_mode_matches_oracle(gpu_lib, abi, O, dropin):
+    dp, di = dropin
+    m, st = oracle_states(abi, O, [20])
+    assert np.abs(st[20]["S2"] - st[0]["S2"]).max() > 1e-3  # DNAPL enters through the patch
+    di.set_mode(2)
+    run = Run(dp, di, m, st[0])
+    run.steps(20)
+    assert gpu_lib.gbf_last_status() == abi.GBF_OK
+    check("split mode, 20 steps", run, st[20], derived=True)
+    run.close()
+
+
+def test_split_mode_host_writes_and_mode_change(gpu_lib, abi, O, dropin):
+    dp, di = dropin
+    m, st = oracle_states(abi, O, [10, 20, 30])
+    di.set_mode(2)
+    run = Run(dp, di, m, st[0])
+    run.steps(10)
+    check("split mode, 10 steps", run, st[10])
+    # the host writes the oracle's state at step 10: the split state is formed anew from it
+    run.put("P1", st[10]["P1"])
+    run.put("S2", st[10]["S2"])
+    run.steps(10)
+    check("split mode, 10 more steps from a state the host wrote", run, st[20])
+    # the eager mode from here: the caller's arrays are brought up to date first
+    di.set_mode(0)
+    run.steps(10)
+    check("eager mode, 10 steps after 20 in split mode", run, st[30])
+    assert gpu_lib.gbf_last_status() == abi.GBF_OK
+    run.close()

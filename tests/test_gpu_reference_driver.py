@@ -1,10 +1,12 @@
 """The reference's own driver on the GPU: main.cpp and no_communication.cpp,
 compiled unmodified from the reference sources and linked against
 libgbflow.so in place of gpu.cu, run for 25000 steps of a 15^3 grid (fresh
-and restarted from a checkpoint), eager and fused drop-in modes. Every
-Tecplot file it writes in eager mode must equal, byte for byte, the one the
-reference CPU build (cpu.cpp) writes; in fused mode its values must agree
-within 1e-8 of each column's scale
+and restarted from a checkpoint), eager, fused and split drop-in modes.
+Every Tecplot file it writes in eager mode must equal, byte for byte, the one
+the reference CPU build (cpu.cpp) writes; in fused mode its values must agree
+within 1e-8 of each column's scale, in split mode (GBF_DROPIN_MODE=2, the
+headline split form) within 1e-6 of it, the scale being a column's largest
+magnitude over its plot kind's files
 (tests/reference_driver/run_reference_driver.py).
 
 Needs the reference sources, named by GBF_REFERENCE_DIR; skipped without
@@ -35,7 +37,7 @@ def test_unmodified_reference_driver_matches_cpu_build(gpu_lib, tmp_path):
     for scen in ("fresh", "restart"):
         res = s["scenarios"][scen]
         assert res["files"] >= 15
-        for mode in ("gb300_eager", "gb300_fused"):
+        for mode in ("gb300_eager", "gb300_fused", "gb300_split"):
             c = res["compare"][mode]
             assert not c["missing"] and c["byte_equal"] + len(c["differing"]) == res["files"]
         assert res["compare"]["gb300_eager"]["byte_equal"] == res["files"]
