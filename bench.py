@@ -8,8 +8,9 @@ as seeded synthetic inputs, see workloads.py) and the forms f64 (plain FP64),
 split (FP32 state and fluxes, phase masses at FP64 precision as FP32-pair
 defects, one residual-correction Newton step per cell), splitdf (FP32-pair
 masses), splitdefect (FP32 mass defects, no correction step); and
-config1_dropin, config 1's grid through the reference's own host function set
-(defines.h: the five calls of time_step_function, fused mode).
+config1_dropin / config1_dropinsplit, config 1's grid through the reference's
+own host function set (defines.h: the five calls of time_step_function) in
+fused FP64 mode / split mode.
 The default, config4_split, is the combined precision + batching form on the
 256-member ensemble; the same line also reports plain FP64 and the other split
 forms on the same members.
@@ -159,7 +160,11 @@ PRECISIONS = {"f64": ("GBF_PREC_F64", "plain FP64", "f64"),
               "splitdefect": ("GBF_PREC_SPLIT_DEFECT", "FP32 state and fluxes, phase masses as FP32 defects over "
                               "the state's mass at the row's hydrostatic density, no correction step", "f32"),
               "dropin": ("GBF_PREC_F64", "plain FP64 through the reference's host function set (defines.h), "
-                         "fused mode", "f64")}
+                         "fused mode", "f64"),
+              "dropinsplit": ("GBF_PREC_SPLIT", "the split form (FP32 state and fluxes, phase masses at FP64 "
+                              "precision, one residual-correction Newton step per cell) through the reference's "
+                              "host function set (defines.h), split mode", "f32+f32x2")}
+DROPIN_MODES = {"dropin": 1, "dropinsplit": 2}  # gbf_dropin_set_mode: fused FP64, split
 ENSEMBLE_BASE = {"config3": 96, "config4": 256}
 DESC = {"config0": "config 0: 40^3 homogeneous single grid",
         "config1": "config 1: {n}^3 heterogeneous single grid",
@@ -182,8 +187,8 @@ class Workload:
             raise SystemExit(f"unknown form in {name}")
         self.name, self.cfg, self.form = name, cfg, form
         self.ensemble = cfg in ENSEMBLE_BASE
-        if form == "dropin" and cfg != "config1":
-            raise SystemExit("the drop-in form runs config 1's grid only (config1_dropin)")
+        if form in DROPIN_MODES and cfg != "config1":
+            raise SystemExit("the drop-in forms run config 1's grid only (config1_dropin, config1_dropinsplit)")
         n = cube or 256
         if self.ensemble:
             specs = (wl.config3_specs if cfg == "config3" else wl.config4_specs)(ENSEMBLE_BASE[cfg] * world)
@@ -199,7 +204,7 @@ class Workload:
             if cfg == "config0":
                 mem = wl.config0(lib)
             elif cfg == "config1":
-                mem = wl.config1_dropin(lib, n=n) if form == "dropin" else wl.config1(lib, n=n)
+                mem = wl.config1_dropin(lib, n=n) if form in DROPIN_MODES else wl.config1(lib, n=n)
             elif cfg == "config2":
                 mem = wl.config2(lib)
             else:
@@ -207,7 +212,7 @@ class Workload:
             self.members = [mem]
             self.members_all = world
             self.cells_all = world * mem.ncells
-            self.desc = DESC["config1_dropin" if form == "dropin" else cfg].format(n=n)
+            self.desc = DESC["config1_dropin" if form in DROPIN_MODES else cfg].format(n=n)
             self.partition = "replicas: one grid per rank" if world > 1 else "one grid"
 
     @property
@@ -271,16 +276,17 @@ class Runner:
 class DropinRunner:
     """Config 1's grid through the reference's host function set, called like
     main.cpp: device_memory_alloc, load_data_to_device(_int), then per step
-    time_step_function's five calls (main.cpp:83-94) in fused mode."""
+    time_step_function's five calls (main.cpp:83-94) in fused mode (1) or
+    split mode (2)."""
 
-    def __init__(self, pkg, member):
+    def __init__(self, pkg, member, mode=1):
         import ctypes
         from importlib import import_module
         self.abi = pkg.abi
         self.dp = dp = import_module(pkg.__name__ + ".dropin")
         self.mem = member
         self.di = dp.DropIn()
-        self.di.set_mode(1)
+        self.di.set_mode(mode)
         m = member.model
         self.c = dp.consts_from_model(m)
         self.H = dp.PtrArrays()
@@ -335,6 +341,11 @@ class DropinRunner:
         h = self.handle
         return self.lib.gbf_domain_status(h) if h else self.lib.gbf_last_status()
 
+    @property
+    def uses_tma(self):
+        h = self.handle
+        return bool(h and self.lib.gbf_domain_uses_tma(h))
+
     def sync(self):
         import torch
         torch.cuda.synchronize()
@@ -359,7 +370,9 @@ ALGO_BYTES = {
 ALGO_BYTES_DEFECT = {"split_step": (40.0, "interior"), "ensemble_step": (40.0, "interior")}
 # The drop-in's media-table grid reads an int media index instead of K, phi (props: P, S, media;
 # flux/Newton: no phi read).
-ALGO_BYTES_DROPIN = {"f64_props": (60.0, "all"), "f64_flux_newton": (72.0, "interior")}
+# Split mode: read dP, S (8), media (4), M1, M2 (16); write dP, S (8), M1, M2 (16).
+ALGO_BYTES_DROPIN = {"f64_props": (60.0, "all"), "f64_flux_newton": (72.0, "interior"),
+                     "split_step": (52.0, "interior")}
 
 
 def timed(runner, steps, stream, world):
@@ -483,9 +496,9 @@ def run_ours(args, rank, world):
     prec = getattr(abi, PRECISIONS[p][0])
     cap = args.warmup + 2 * args.steps + 8
     tuning = None
-    if p == "dropin":
+    if p in DROPIN_MODES:
         stream = torch.cuda.default_stream()  # the drop-in runs on the legacy default stream, like gpu.cu
-        run = DropinRunner(pkg, members[0])
+        run = DropinRunner(pkg, members[0], DROPIN_MODES[p])
         run.upload_initial()
         run.step(1)  # the first fused step creates the domain behind the arrays
     else:
@@ -516,7 +529,7 @@ def run_ours(args, rank, world):
     hbm, peak_kind = peaks()
     kname, (kms, klaunch) = max(ktimes.items(), key=lambda kv: kv[1][0])
     per_launch_s = kms / 1e3 / max(klaunch, 1)
-    table = ALGO_BYTES_DROPIN if p == "dropin" else ALGO_BYTES_DEFECT if p == "splitdefect" else ALGO_BYTES
+    table = ALGO_BYTES_DROPIN if p in DROPIN_MODES else ALGO_BYTES_DEFECT if p == "splitdefect" else ALGO_BYTES
     bpc, which = table.get(kname, ALGO_BYTES.get(kname, (0.0, "all")))
     algo = bpc * (icells if which == "interior" else cells)
     achieved = algo / per_launch_s / 1e9 if per_launch_s > 0 else 0.0
@@ -562,7 +575,7 @@ def run_ours(args, rank, world):
         shape = members[0].model.shape
         hostP = torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
         hostS = torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
-        if p == "dropin":
+        if p in DROPIN_MODES:
             def rt():
                 run.upload(hostP, hostS)
                 run.step(1)
@@ -607,13 +620,15 @@ def run_ours(args, rank, world):
            "config": W.config(),
            "details": {"dt_used_range": [min(m.model.dt for m in members), max(m.model.dt for m in members)],
                        "newton": ("converge-and-exit (tol 1e-11, at most the reference's 7)" if p == "dropin" else
+                                  "increment Newton, a second iteration where nonlinear, one residual-correction "
+                                  "step" if p == "dropinsplit" else
                                   "FP64: converge-and-exit (tol 1e-11, max 7); split: increment Newton, a second "
                                   "iteration where nonlinear, and (split) one residual-correction step"),
                        "tuning": tuning, "graphs": ensemble, "rank_cells": cells,
                        "plane_staging": ("none (FP64)" if p in ("f64", "dropin") else
                                          "TMA" if run.uses_tma else "plain loads")},
            "clocks": clk.summary(), "e2e": e2e,
-           "gpu_launches": (run.launches_per_step if p != "dropin" else run.lib.gbf_domain_launches_per_step(
+           "gpu_launches": (run.launches_per_step if p not in DROPIN_MODES else run.lib.gbf_domain_launches_per_step(
                run.handle)) * args.steps,
            "roofline": roof, "status": lib.gbf_status_string(status).decode()}
     run.close()
@@ -641,7 +656,9 @@ def run_ours(args, rank, world):
         out["same_members"] = comp
         if "f64" in comp:
             out["split_batched_over_fp64_batched"] = (cells * args.steps / (ms / 1e3)) / comp["f64"]["value"]
-    if rank == 0 and not args.no_compare and prec != abi.GBF_PREC_F64:
+    if rank == 0 and not args.no_compare and p == "dropinsplit":
+        out["accuracy"] = accuracy_dropin(pkg, members[0])
+    elif rank == 0 and not args.no_compare and prec != abi.GBF_PREC_F64:
         O = ge.load_oracle_module()
         out["accuracy"] = accuracy_block(pkg, O, members, prec, ensemble)
         out["accuracy_stiff"] = accuracy_stiff(pkg, lib, W.wl, members, prec, ensemble)
@@ -686,6 +703,28 @@ def compare(pkg, members, prec, ensemble, steps, flags=0):
     if cfl is not None:
         block["cfl_max"] = [float(cfl[..., 0].max()), float(cfl[..., 1].max())]
     return block, got
+
+
+def accuracy_dropin(pkg, member, steps=20):
+    """The drop-in's split mode against its fused FP64 mode (itself pinned to
+    the oracle at 1e-12), both through the reference's calls from the same
+    initial state for the same steps: max|dS|, relative L2 of P, and how far
+    S moved (the DNAPL entering under the Dirichlet patch)."""
+    out = {}
+    for mode in (2, 1):
+        run = DropinRunner(pkg, member, mode)
+        run.upload_initial()
+        run.step(steps)
+        P = run.download("P1", np.empty(member.model.shape))
+        S = run.download("S2", np.empty(member.model.shape))
+        out[mode] = (P, S, int(run.status()))
+        run.close()
+    (Pg, Sg, s2), (Pr, Sr, s1) = out[2], out[1]
+    S0 = member.initial_state()[1]
+    return {"vs": "the drop-in's fused FP64 mode (pinned to the oracle at 1e-12), same calls and steps",
+            "steps": steps, "max_dS": float(np.abs(Sg - Sr).max()),
+            "rel_l2_P": float(np.linalg.norm(Pg - Pr) / np.linalg.norm(Pr)),
+            "S_moved_max": float(np.abs(Sr - S0).max()), "status": [s2, s1]}
 
 
 def accuracy_block(pkg, O, members, prec, ensemble, steps=20):

@@ -66,3 +66,24 @@ def test_reference_arm_loads_no_gpu_library_and_prints_the_same_config():
     pkg = ge.load_package()
     W = bench.Workload(pkg, pkg.load_library(), "config4_split", 0, 0, 1, 3)
     assert W.config() == d["config"]
+
+
+def test_dropin_split_workload_names_its_form_and_grid():
+    """config1_dropinsplit: config 1's media-table grid through the defines.h
+    calls in split mode; the drop-in forms refuse other configurations."""
+    import pytest
+    import __graft_entry__ as ge
+    sys.path.insert(0, str(ROOT))
+    import bench
+    pkg = ge.load_package()
+    lib = pkg.load_library()
+    W = bench.Workload(pkg, lib, "config1_dropinsplit", 16, 0, 1)
+    fused = bench.Workload(pkg, lib, "config1_dropin", 16, 0, 1)
+    assert bench.DROPIN_MODES == {"dropin": 1, "dropinsplit": 2}
+    c, cf = W.config(), fused.config()
+    assert c["workload"] == "config1_dropinsplit" and c["desc"] == cf["desc"] and c["cells"] == 16 ** 3
+    assert "split mode" in c["form"] and "fused mode" in cf["form"]
+    assert W.members[0].media is not None and W.members[0].K is None
+    assert bench.ALGO_BYTES_DROPIN["split_step"] == (52.0, "interior")
+    with pytest.raises(SystemExit):
+        bench.Workload(pkg, lib, "config2_dropinsplit", 0, 0, 1)
