@@ -553,6 +553,11 @@ void gbf_dropin_host_wrote(gbf_domain* d, const double* dev) {
   if (d && d->precision != GBF_PREC_F64 && (dev == d->caller.P1 || dev == d->caller.S2)) d->split_stale = true;
 }
 
+int gbf_dropin_media_wrote(gbf_domain* d, const int* dev) {
+  if (!d || dev != d->cells.media || !gbf_is_defect(gbf_mass_rep(d->precision))) return GBF_OK;
+  return gbf_defect_k1(d->m, d->cells.phi, d->cells.media, &d->defect_k1v, nullptr);
+}
+
 // Run the pending stages (bitmask of stages 1..4) one kernel each, in order.
 int gbf_dropin_flush(gbf_domain* d) {
   if (!d || !d->pending) return GBF_OK;

@@ -118,3 +118,7 @@ bool gbf_dropin_is_derived(const gbf_domain* d, const double* p);
 // note that the host wrote one of them (the split state is formed anew).
 int gbf_dropin_writeback(gbf_domain* d);
 void gbf_dropin_host_wrote(gbf_domain* d, const double* dev);
+// The host rewrote the media array `dev`, which the domain reads in place:
+// the split defect form's porosity sum over the rows (a constant of its mass
+// sums, taken from the media at creation) is taken again.
+int gbf_dropin_media_wrote(gbf_domain* d, const int* dev);

@@ -55,7 +55,7 @@ std::unordered_map<const double*, DropinDomain> g_domains;
 // reference's own main.cpp); anything else, or nothing, the eager mode.
 int initial_mode() {
   const char* e = getenv("GBF_DROPIN_MODE");
-  if (!e || e[1] != '\0') return 0;
+  if (!e || e[0] == '\0' || e[1] != '\0') return 0;
   return e[0] == '1' ? 1 : e[0] == '2' ? 2 : 0;
 }
 int g_mode = initial_mode();
@@ -254,7 +254,13 @@ void load_data_to_device(double* HostArrayPtr, double* DevArrayPtr, int localNx,
 
 void load_data_to_device_int(int* HostArrayPtr, int* DevArrayPtr, int localNx, consts def) {
   size_t n = (size_t)localNx * def.Ny * def.Nz;
+  if (g_mode != 0) flush_all();  // deferred stages read the media array
   gbf_cuda_check(cudaMemcpy(DevArrayPtr, HostArrayPtr, n * sizeof(int), cudaMemcpyHostToDevice), "copy int data to device");
+  if (g_mode != 0) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    for (auto& kv : g_domains)
+      if (gbf_domain* f = kv.second.fused) gbf_dropin_media_wrote(f, DevArrayPtr);
+  }
 }
 
 void device_memory_alloc(ptr_Arrays* A, double** DevBuffer, int nX, consts def) {

@@ -8,7 +8,9 @@ split form's bars: max|dS| <= 1e-5, rel-L2(P) <= 1e-6; the derived arrays
 the host reads (P2, ro1, ro2, from the state the last step started from)
 as well. Also: P1 and S2 written by the host in the middle of a run (the
 split state is formed anew from them), and a change to the eager mode in the
-middle of a run (the caller's arrays are brought up to date first).
+middle of a run (the caller's arrays are brought up to date first), and a
+media array rewritten by the host after the split domain exists (its mass
+sums then use the new porosities).
 """
 import ctypes
 from importlib import import_module
@@ -62,6 +64,10 @@ class Run:
     def put(self, name, a):
         a = np.ascontiguousarray(a, np.float64)
         self.di.f["load_data_to_device"](a.ctypes.data, getattr(self.D, name), self.m.nx, self.c)
+
+    def put_media(self, media):
+        a = np.ascontiguousarray(media, np.int32)
+        self.di.f["load_data_to_device_int"](a.ctypes.data, self.D.media, self.m.nx, self.c)
 
     def get(self, name):
         out = np.empty(self.m.shape, np.float64)
@@ -117,5 +123,45 @@ def test_split_mode_host_writes_and_mode_change(gpu_lib, abi, O, dropin):
     di.set_mode(0)
     run.steps(10)
     check("eager mode, 10 steps after 20 in split mode", run, st[30])
+    assert gpu_lib.gbf_last_status() == abi.GBF_OK
+    run.close()
+
+
+def test_split_mode_media_rewrite_updates_mass_sums(gpu_lib, abi, O, pkg, dropin):
+    """The host rewrites the media array after the first step created the
+    split domain: the next step reads it in place, and the phase masses the
+    drop-in's domain sums (GBF_OUT_MASS on gbf_dropin_domain) take the new
+    porosities, as a split domain created with the new media from the same
+    state does. The water mass carries the grid's porosity sum over the rows,
+    taken from the media: kept from the old media it would be off by percent;
+    the two paths differ by the split step's residual (1e-9 bar)."""
+    import ctypes
+    from importlib import import_module
+    Domain = import_module(pkg.__name__ + ".domain").Domain
+    dp, di = dropin
+    m, st = oracle_states(abi, O, [])
+    assert m.m[0] != m.m[1]  # the two media differ in porosity
+    di.set_mode(2)
+    run = Run(dp, di, m, st[0])
+    run.put_media(np.zeros(m.shape, np.int32))
+    run.steps(1)
+    h = di.domain(run.D.P1)
+    assert h and gpu_lib.gbf_domain_set_outputs(h, abi.GBF_OUT_MASS, 8) == abi.GBF_OK
+    media1 = (np.random.default_rng(5).random(m.shape) < 0.5).astype(np.int32)
+    run.put_media(media1)
+    P, S = run.get("P1"), run.get("S2")
+    run.steps(1)
+    got = np.zeros((8, 2))
+    n = ctypes.c_int()
+    assert gpu_lib.gbf_domain_mass_history(h, got.ctypes.data, 8, ctypes.byref(n)) == abi.GBF_OK and n.value == 1
+    ref = Domain(m, media1, None, None, precision=abi.GBF_PREC_SPLIT)
+    ref.set_outputs(abi.GBF_OUT_MASS, 8)
+    ref.upload(P, S)
+    ref.step(1)
+    want = ref.mass_history(1)
+    ref.close()
+    rel = np.abs(got[0] - want[0]) / np.abs(want[0])
+    print(f"\nmedia rewritten: masses {got[0]} vs {want[0]}, relative {rel}")
+    assert rel[0] <= 1e-9 and rel[1] <= 1e-4, rel
     assert gpu_lib.gbf_last_status() == abi.GBF_OK
     run.close()
