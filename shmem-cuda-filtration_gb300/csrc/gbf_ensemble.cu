@@ -1140,10 +1140,9 @@ int gbf_ensemble_download_all(gbf_ensemble* e, double* P_all, double* S_all) {
   return GBF_OK;
 }
 
-int gbf_ensemble_advance_host(gbf_ensemble* e, const double* P_in, const double* S_in, int nsteps, double* P_out,
-                              double* S_out) {
-  if (!e || !P_in || !S_in || !P_out || !S_out || nsteps < 0)
-    return gbf_fail(GBF_ERR_ARG, "gbf_ensemble_advance_host");
+namespace {
+int ens_advance_host(gbf_ensemble* e, const double* P_in, const double* S_in, int nsteps, double* P_out,
+                     double* S_out) {
   if (int s = ensure_stage(e)) return s;
   const std::vector<int> first = pipe_groups(e);
   const int G = (int)first.size() - 1;
@@ -1195,6 +1194,20 @@ int gbf_ensemble_advance_host(gbf_ensemble* e, const double* P_in, const double*
     GBF_CUDA(cudaMemsetAsync(e->d_cfl_hist, 0, 2 * sizeof(float) * (size_t)e->mass_cap * e->n, cs));
   GBF_CUDA(cudaStreamSynchronize(cs));
   return GBF_OK;
+}
+}  // namespace
+
+int gbf_ensemble_advance_host(gbf_ensemble* e, const double* P_in, const double* S_in, int nsteps, double* P_out,
+                              double* S_out) {
+  if (!e || !P_in || !S_in || !P_out || !S_out || nsteps < 0)
+    return gbf_fail(GBF_ERR_ARG, "gbf_ensemble_advance_host");
+  const int s = ens_advance_host(e, P_in, S_in, nsteps, P_out, S_out);
+  if (s) {  // an error part-way: no copy may still read or write the caller's arrays after the return
+    if (e->s_in) cudaStreamSynchronize(e->s_in);
+    if (e->s_out) cudaStreamSynchronize(e->s_out);
+    cudaStreamSynchronize(e->stream);
+  }
+  return s;
 }
 
 int gbf_ensemble_set_pipeline_groups(gbf_ensemble* e, int groups) {

@@ -573,7 +573,8 @@ int gbf_split_state_to_f64(const gbf_model& m, const GbfRowConst* rows, const fl
 // the slab but the start-of-step state) and converts it back. The state equals
 // upload + step + download bit for bit; the phase masses sum the same cells in
 // other partial blocks (within 1e-11 relative). Grids without a Dirichlet patch.
-int gbf_split_advance_host(gbf_domain* d, const double* P_in, const double* S_in, double* P_out, double* S_out) {
+namespace {
+int split_advance_host(gbf_domain* d, const double* P_in, const double* S_in, double* P_out, double* S_out) {
   const gbf_model& m = d->m;
   const GbfGeo g = gbf_geo(m);
   const size_t n = g.n, pl = g.pl;
@@ -671,6 +672,17 @@ int gbf_split_advance_host(gbf_domain* d, const double* P_in, const double* S_in
   d->uploaded = true;
   GBF_CUDA(cudaStreamSynchronize(cs));
   return GBF_OK;
+}
+}  // namespace
+
+int gbf_split_advance_host(gbf_domain* d, const double* P_in, const double* S_in, double* P_out, double* S_out) {
+  const int s = split_advance_host(d, P_in, S_in, P_out, S_out);
+  if (s) {  // an error part-way: no copy may still read or write the caller's arrays after the return
+    if (d->pipe_in) cudaStreamSynchronize(d->pipe_in);
+    if (d->pipe_out) cudaStreamSynchronize(d->pipe_out);
+    cudaStreamSynchronize(d->stream);
+  }
+  return s;
 }
 
 int gbf_split_launches_per_step(gbf_domain* d) {
