@@ -579,11 +579,20 @@ int gbf_dropin_flush(gbf_domain* d) {
 // last step. Any other sequence falls back to one kernel per stage.
 int gbf_dropin_defer(gbf_domain* d, const gbf_model& m, int stage) {
   if (memcmp(&m, &d->m, sizeof(gbf_model)) != 0) {  // parameters changed between calls
+    // under the old parameters: the deferred stages, the last step's derived
+    // arrays, and (split mode) the caller's P1, S2 from the split state, whose
+    // dP and mass defects are taken against the old rows' hydrostatic values
     if (int s = gbf_dropin_flush(d)) return s;
+    if (int s = gbf_dropin_materialize(d)) return s;
+    if (int s = gbf_dropin_writeback(d)) return s;
     d->m = m;
     d->d = gbf_derive(m);
-    if (d->precision != GBF_PREC_F64)  // split mode: its row constants, and the state formed anew
+    if (d->precision != GBF_PREC_F64) {  // split mode: its row constants, and the state formed anew
       if (int s = gbf_split_fill_rows(d->m, d->split_rows, d->stream)) return s;
+      d->split_stale = true;
+      if (gbf_is_defect(gbf_mass_rep(d->precision)))
+        if (int s = gbf_defect_k1(d->m, d->cells.phi, d->cells.media, &d->defect_k1v, nullptr)) return s;
+    }
   }
   const int prefix = (1 << (stage - 1)) - 1;
   if (stage <= 4) {

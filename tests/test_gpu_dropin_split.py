@@ -165,3 +165,28 @@ def test_split_mode_media_rewrite_updates_mass_sums(gpu_lib, abi, O, pkg, dropin
     assert rel[0] <= 1e-9 and rel[1] <= 1e-4, rel
     assert gpu_lib.gbf_last_status() == abi.GBF_OK
     run.close()
+
+
+def test_split_mode_parameter_change_forms_the_state_anew(gpu_lib, abi, O, dropin):
+    """The compressibilities in consts change between two steps (they enter
+    the split state's row densities): the split state is written back to the
+    caller's P1, S2 under the old rows and formed anew under the new ones, so
+    the run keeps to the fused FP64 mode making the same change (the split
+    form's bars). Taken against the old rows, every water-mass defect would be
+    off by the change of the row density (about a fifth here)."""
+    dp, di = dropin
+    m, st = oracle_states(abi, O, [])
+    out = {}
+    for mode in (2, 1):
+        di.set_mode(mode)
+        run = Run(dp, di, m, st[0])
+        run.steps(10)
+        run.c.beta1, run.c.beta2 = 5e-5, 5e-9
+        run.steps(10)
+        out[mode] = run.get("P1"), run.get("S2")
+        assert gpu_lib.gbf_last_status() == abi.GBF_OK
+        run.close()
+    (Ps, Ss), (Pf, Sf) = out[2], out[1]
+    ds, pl2 = float(np.abs(Ss - Sf).max()), rel_l2(Ps, Pf)
+    print(f"\nparameters changed after 10 steps: max|dS| {ds:.2e}, rel-L2(P) {pl2:.2e}")
+    assert ds <= DS_TOL and pl2 <= P_TOL, (ds, pl2)
